@@ -1,0 +1,199 @@
+/*
+ * nans_gb300.h -- C ABI of the GB300 (sm_103a) physics step.
+ *
+ * Drop-in for the physics step of L4v/nans_projekat: the stage sequence that the
+ * reference's frame entry point runs (code/nans.cpp:1756-1764)
+ *     Pairs.clear -> IntegrateForces -> DetectCollisions -> SolveConstraints
+ *     -> IntegrateVelocities, then the render code's Model rebuild (:1909-1942)
+ * with RK4 integration, GJK detection, EPA contact generation and sequential impulses.
+ *
+ * Conventions
+ *   - Host buffers belong to the caller; device buffers belong to the library.
+ *   - Every call returns an int status: NANS_OK (0) or one of the NANS_ERR_* codes; a
+ *     one-line description of the last failure on the calling thread is available from
+ *     nans_last_error(). No C++ exception crosses this boundary.
+ *   - One CUDA stream per world. A world is not thread safe; distinct worlds are.
+ *   - Results are bit-identical to the reference step compiled with IEEE single precision
+ *     and no FP contraction, for every pair list and every body state.
+ *
+ * The record types keep the reference's layouts byte for byte (code/nans.h:303-372).
+ */
+#ifndef NANS_GB300_H
+#define NANS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- reference record layouts ---------------------------------------------------- */
+
+/* struct cube (code/nans.h:303-319), 244 bytes; Model is a column-major glm::mat4. */
+typedef struct nans_cube
+{
+    float Model[16];
+    float Vertices[8][3];
+    float Position[3];
+    float V[3];
+    float Forces[3];
+    float Angles[3];
+    float W[3];
+    float Torque[3];
+    float Size;
+    float Mass;
+    float MOI;
+} nans_cube;
+
+/* struct sphere (code/nans.h:321-336), 148 bytes. */
+typedef struct nans_sphere
+{
+    float Model[16];
+    float Position[3];
+    float V[3];
+    float Forces[3];
+    float Angles[3];
+    float W[3];
+    float Torque[3];
+    float Radius;
+    float Mass;
+    float MOI;
+} nans_sphere;
+
+/* enum collision_type (code/nans.h:73-89) */
+enum nans_collision_type
+{
+    NANS_CC = 0,
+    NANS_CS = 1,
+    NANS_CF = 2,
+    NANS_SS = 3,
+    NANS_SF = 4
+};
+
+/* struct contact_pair (code/nans.h:338-372), 96 bytes. Pairs returned by nans_get_pairs
+ * carry Type, PointA, PointB, N, IndexA, IndexB as DetectCollisions leaves them
+ * (accumulators and tangents zero); IndexB = IndexA for floor pairs. */
+typedef struct nans_contact_pair
+{
+    int32_t Type;
+    float DLNormal;
+    float DLNormalSum;
+    float DLTangent1;
+    float DLTangent1Sum;
+    float DLTangent2;
+    float DLTangent2Sum;
+    float PointA[3];
+    float PointB[3];
+    float N[3];
+    float T1[3];
+    float T2[3];
+    int32_t IndexA;
+    int32_t IndexB;
+} nans_contact_pair;
+
+/* ---- status codes ------------------------------------------------------------------ */
+#define NANS_OK 0
+#define NANS_ERR_INVALID_ARGUMENT 1 /* null pointer, zero count, bad scene index */
+#define NANS_ERR_CAPACITY 2         /* more candidate pairs than the world's capacity */
+#define NANS_ERR_NAN_INPUT 3        /* non-finite or non-positive mass / MOI / size input */
+#define NANS_ERR_CUDA 4             /* a CUDA runtime call failed (see nans_last_error) */
+#define NANS_ERR_EPA_CAPACITY 5     /* an EPA polytope outgrew its shared-memory buffers */
+#define NANS_ERR_NOT_UPLOADED 6     /* the world holds no scene yet */
+#define NANS_ERR_SCENE_TOO_LARGE 7  /* a scene has more bodies than the solver supports */
+
+/* ---- world ------------------------------------------------------------------------- */
+
+/* Upload flags */
+#define NANS_UPLOAD_KEEP_MODEL 1u  /* first step uses the records' Model matrices as given
+                                      (exact continuation of a reference state); default:
+                                      rebuild Model from Position/Angles/scale first */
+
+/* World flags */
+#define NANS_WORLD_ALL_PAIRS 1u    /* run GJK on every pair (the reference's all-pairs
+                                      loop); default: conservative AABB cull first */
+
+typedef struct nans_world_desc
+{
+    int32_t device;          /* CUDA device ordinal */
+    uint32_t flags;          /* NANS_WORLD_* */
+    uint32_t max_candidates; /* candidate-pair capacity; 0 = 16 per dynamic body + 4096 */
+} nans_world_desc;
+
+/* Solver constants. The reference keeps them as literals: restitution Cr = 0.1
+ * (code/nans.cpp:1154), friction Cf = 0.1 (:1159), 70 impulse iterations (:1176). */
+typedef struct nans_step_params
+{
+    float cr;
+    float cf;
+    int32_t iterations;
+} nans_step_params;
+
+typedef struct nans_world nans_world;
+
+int nans_world_create(const nans_world_desc *desc, nans_world **out);
+int nans_world_destroy(nans_world *world);
+
+/* One scene: the reference's sdl_state bodies (code/nans.h:374-386). cube_scale holds
+ * ncubes x 3 model scales or NULL (Size on every axis, code/nans.cpp:1921-1923); the floor's
+ * scale is (Size, 1, Size) (code/nans.cpp:1878-1879). Constants default to the reference's
+ * literals until nans_step receives others. */
+int nans_world_upload(nans_world *world, const nans_cube *cubes, uint32_t ncubes, const nans_sphere *spheres,
+                      uint32_t nspheres, const nans_cube *floor, const float *cube_scale, uint32_t flags);
+
+/* Many independent scenes (the batched form). Records are concatenated scene by scene.
+ * hull_npts (per cube, 0 = unit-cube corners) and hull_pts (packed local points) describe
+ * convex hulls, a shape the reference does not have; pass NULL for boxes only.
+ * scene_params (nscenes entries) or NULL for the reference literals. */
+int nans_batch_upload(nans_world *world, uint32_t nscenes, const uint32_t *scene_ncubes,
+                      const uint32_t *scene_nspheres, const nans_cube *cubes, const nans_sphere *spheres,
+                      const nans_cube *floors, const float *cube_scale, const int32_t *hull_npts,
+                      const float *hull_pts, const nans_step_params *scene_params, uint32_t flags);
+
+/* The plain drop-in step: nsteps reference steps on every scene of the world, launched
+ * stage by stage, synchronised before returning. params (or NULL to keep the current
+ * constants) applies to every scene. */
+int nans_step(nans_world *world, const nans_step_params *params, float dt, uint32_t nsteps);
+
+/* The batched step: the same stages as persistent kernels with work queues, nsteps steps
+ * replayed from a CUDA graph of graph_steps steps (0 = 60). Synchronised before returning. */
+int nans_batch_step(nans_world *world, float dt, uint32_t nsteps, uint32_t graph_steps);
+
+/* Picks narrowphase / solver launch shapes by timing a few steps on the world's own
+ * scenes; the state is restored afterwards. */
+int nans_batch_autotune(nans_world *world, float dt);
+
+/* Bodies back in the reference layouts, all scenes concatenated in upload order; any of
+ * the pointers may be NULL. Applies the last step's pending IntegrateVelocities first. */
+int nans_world_download(nans_world *world, nans_cube *cubes, nans_sphere *spheres, nans_cube *floors);
+
+/* Overwrites the dynamic fields (Position, V, Forces, Angles, W, Torque and, with
+ * NANS_UPLOAD_KEEP_MODEL, Model) of every body from records laid out as at upload. */
+int nans_world_set_state(nans_world *world, const nans_cube *cubes, const nans_sphere *spheres, uint32_t flags);
+
+/* Contact list of one scene after its last DetectCollisions, in the reference's order
+ * (CC i<j, CF, SF, CS, SS). *count receives the full count even when it exceeds cap. */
+int nans_get_pairs(nans_world *world, uint32_t scene, nans_contact_pair *out, uint32_t cap, uint32_t *count);
+
+/* Device status bits accumulated since the last call (EPA buffer overflow, ...), cleared. */
+int nans_world_status(nans_world *world, uint32_t *status_bits);
+
+/* Counts of the last step: candidate pairs after the cull and contacts. */
+int nans_world_counts(nans_world *world, uint32_t *candidates, uint32_t *contacts);
+
+/* The world's CUDA stream (a cudaStream_t), for event timing by the caller. */
+void *nans_world_stream(nans_world *world);
+
+/* Kernel launches per step on the batched path and on the plain path. */
+int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain);
+
+/* The project sine/cosine used by the Model rebuild, evaluated on the device (n values). */
+int nans_device_sincos(const float *x, float *s, float *c, uint32_t n);
+
+/* Description of the last failure on the calling thread ("" if none). */
+const char *nans_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NANS_GB300_H */

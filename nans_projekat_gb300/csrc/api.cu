@@ -1,0 +1,926 @@
+// Host runtime behind the C ABI (include/nans_gb300.h).
+//
+// A world owns one CUDA stream and every device buffer of its scenes. The step is the
+// stage sequence of the reference's frame function (code/nans.cpp:1758-1762) plus the
+// render code's Model rebuild, as six kernels:
+//   k_sweep        IntegrateVelocities(prev) + rebuild + IntegrateForces + vertices + AABB
+//   k_cull_mask / k_scan_blocks / k_cull_write   ordered candidate pairs
+//   k_narrow       GJK + EPA                      (DetectCollisions)
+//   k_solve        sequential impulses by waves   (SolveConstraints)
+// The last step's IntegrateVelocities is folded into the next step's sweep, or applied by
+// nans_world_download.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/nans_gb300.h"
+#include "nans_kernels.cuh"
+
+using namespace nans;
+
+static_assert(sizeof(nans_cube) == 244, "cube record layout");
+static_assert(sizeof(nans_sphere) == 148, "sphere record layout");
+static_assert(sizeof(nans_contact_pair) == 96, "contact_pair record layout");
+
+namespace
+{
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                                    \
+    do                                                                                                              \
+    {                                                                                                               \
+        cudaError_t e_ = (call);                                                                                    \
+        if (e_ != cudaSuccess)                                                                                      \
+            return fail(NANS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                         \
+    } while (0)
+
+constexpr int kSolveThreadsHost = 256;
+constexpr int kSweepThreads = 256;
+constexpr size_t kSolveSmemMax = 200 * 1024;
+} // namespace
+
+struct nans_world
+{
+    int device = 0;
+    uint32_t flags = 0;
+    uint32_t max_cand_req = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+
+    int n_scenes = 0, n_dyn = 0, n_all = 0, n_cubes = 0, n_spheres = 0;
+    long long pair_total = 0;
+    int cand_cap = 0;
+    int cull_blocks = 0;
+    int max_scene_bodies = 0;
+
+    std::vector<void *> allocs;     // per-upload device buffers
+    std::vector<void *> cand_allocs; // candidate-sized buffers
+    DevWorld dw{};
+    float4 *d_prm = nullptr, *d_scl = nullptr, *d_model_in = nullptr;
+    int *d_body_rec = nullptr;
+    float2 *d_size_moi = nullptr;
+    float *d_rec_cube = nullptr, *d_rec_sphere = nullptr, *d_rec_floor = nullptr;
+    float *d_pairs_out = nullptr;
+    int pairs_out_cap = 0;
+    int *d_small = nullptr; // [0] pair count for k_pairs_out, [1] contact count
+    float4 *d_snap = nullptr;
+
+    bool uploaded = false;
+    bool pending = false;
+    float pending_dt = 0.0f;
+    bool model_input = false;
+    bool forces_pending = false;
+    long long steps_run = 0;
+
+    int narrow_warps = 4;
+    int narrow_bpsm = 0; // 0 = occupancy limit
+    int solve_bpsm = 0;
+
+    cudaGraphExec_t gexec = nullptr;
+    int g_steps = 0;
+    float g_dt = 0.0f;
+    int g_cfg = -1;
+};
+
+namespace
+{
+
+template <class T> int dalloc(nans_world *w, std::vector<void *> &list, T **p, size_t n)
+{
+    size_t bytes = std::max<size_t>(1, n) * sizeof(T);
+    void *q = nullptr;
+    CK(cudaMalloc(&q, bytes));
+    list.push_back(q);
+    *p = (T *)q;
+    return NANS_OK;
+}
+
+void free_list(std::vector<void *> &list)
+{
+    for (void *p : list)
+        cudaFree(p);
+    list.clear();
+}
+
+void drop_graph(nans_world *w)
+{
+    if (w->gexec)
+    {
+        cudaGraphExecDestroy(w->gexec);
+        w->gexec = nullptr;
+    }
+    w->g_steps = 0;
+    w->g_cfg = -1;
+}
+
+int cfg_id(const nans_world *w) { return w->narrow_warps * 10000 + w->narrow_bpsm * 100 + w->solve_bpsm; }
+
+int narrow_grid(nans_world *w)
+{
+    int per = narrow_blocks_per_sm(w->narrow_warps);
+    if (per < 1)
+        per = 1;
+    if (w->narrow_bpsm > 0)
+        per = std::min(per, w->narrow_bpsm);
+    return per * w->sm_count;
+}
+
+size_t solve_smem(const nans_world *w) { return (size_t)std::max(1, w->max_scene_bodies) * sizeof(int); }
+
+int solve_grid(nans_world *w)
+{
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve, kSolveThreadsHost, solve_smem(w));
+    if (per < 1)
+        per = 1;
+    if (w->solve_bpsm > 0)
+        per = std::min(per, w->solve_bpsm);
+    return std::max(1, std::min(w->n_scenes, per * w->sm_count));
+}
+
+int alloc_candidates(nans_world *w, int cap)
+{
+    free_list(w->cand_allocs);
+    drop_graph(w);
+    w->cand_cap = cap;
+    DevWorld &d = w->dw;
+    d.cand_cap = cap;
+    int rc = NANS_OK;
+    auto &L = w->cand_allocs;
+    if ((rc = dalloc(w, L, &d.cand_a, cap)) || (rc = dalloc(w, L, &d.cand_b, cap)) ||
+        (rc = dalloc(w, L, &d.cand_meta, cap)) || (rc = dalloc(w, L, &d.hit, cap)) ||
+        (rc = dalloc(w, L, &d.c_pa, cap)) || (rc = dalloc(w, L, &d.c_pb, cap)) || (rc = dalloc(w, L, &d.c_n, cap)) ||
+        (rc = dalloc(w, L, &d.s_order, cap)) || (rc = dalloc(w, L, &d.s_wave, cap)) ||
+        (rc = dalloc(w, L, &d.s_perm, cap)) || (rc = dalloc(w, L, &d.s_wcnt, (size_t)cap + 1)) ||
+        (rc = dalloc(w, L, &d.s_k, (size_t)9 * cap)))
+        return rc;
+    return NANS_OK;
+}
+
+bool finite_pos(float x) { return std::isfinite(x) && x > 0.0f; }
+
+struct SceneIn
+{
+    uint32_t nc, ns;
+};
+
+// Builds every static table on the host and uploads records; shared by the single-scene
+// and the batched upload.
+int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint32_t *sns, const nans_cube *cubes,
+                const nans_sphere *spheres, const nans_cube *floors, const float *cube_scale, const int32_t *hull_npts,
+                const float *hull_pts, const nans_step_params *sp, uint32_t flags)
+{
+    if (!w || nscenes == 0 || !snc || !sns || !floors)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "upload: null world/counts/floors or zero scenes");
+    long long tc = 0, ts = 0;
+    for (uint32_t s = 0; s < nscenes; ++s)
+    {
+        tc += snc[s];
+        ts += sns[s];
+    }
+    if ((tc > 0 && !cubes) || (ts > 0 && !spheres))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "upload: null body records");
+    if (tc + ts + nscenes > (long long)INT32_MAX / 4)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "upload: too many bodies");
+    // validate inputs the step divides by
+    for (long long i = 0; i < tc; ++i)
+        if (!finite_pos(cubes[i].Mass) || !finite_pos(cubes[i].MOI))
+            return fail(NANS_ERR_NAN_INPUT, "upload: cube " + std::to_string(i) + " has a non-finite or non-positive Mass/MOI");
+    for (long long i = 0; i < ts; ++i)
+        if (!finite_pos(spheres[i].Mass) || !finite_pos(spheres[i].MOI) || !finite_pos(spheres[i].Radius))
+            return fail(NANS_ERR_NAN_INPUT, "upload: sphere " + std::to_string(i) + " has a non-finite or non-positive Mass/MOI/Radius");
+    for (uint32_t s = 0; s < nscenes; ++s)
+        if (!finite_pos(floors[s].Mass) || !finite_pos(floors[s].MOI) || !std::isfinite(floors[s].Size))
+            return fail(NANS_ERR_NAN_INPUT, "upload: floor " + std::to_string(s) + " has a non-finite Mass/MOI/Size");
+    if (cube_scale)
+        for (long long i = 0; i < 3 * tc; ++i)
+            if (!std::isfinite(cube_scale[i]))
+                return fail(NANS_ERR_NAN_INPUT, "upload: non-finite cube scale");
+    if (hull_npts)
+        for (long long i = 0; i < tc; ++i)
+            if (hull_npts[i] < 0 || hull_npts[i] > 255)
+                return fail(NANS_ERR_INVALID_ARGUMENT, "upload: hull point count outside [0, 255]");
+
+    CK(cudaSetDevice(w->device));
+    CK(cudaStreamSynchronize(w->stream));
+    free_list(w->allocs);
+    free_list(w->cand_allocs);
+    drop_graph(w);
+    w->uploaded = false;
+
+    const int S = (int)nscenes;
+    const int ndyn = (int)(tc + ts);
+    const int nall = ndyn + S;
+    w->n_scenes = S;
+    w->n_dyn = ndyn;
+    w->n_all = nall;
+    w->n_cubes = (int)tc;
+    w->n_spheres = (int)ts;
+
+    std::vector<int> sc_cube0(S), sc_nc(S), sc_ns(S), sc_iters(S), sc_order(S), body_scene(nall), body_rec(nall);
+    std::vector<long long> sc_pair0(S + 1);
+    std::vector<float> sc_cr(S), sc_cf(S);
+    std::vector<int4> shape(nall);
+    std::vector<float4> scl(nall);
+    std::vector<float2> size_moi(nall);
+    std::vector<float> local;
+    long long vert_floats = 0;
+    int cube_rank = 0, sphere_rank = 0, b = 0, max_bodies = 0;
+    long long pair_acc = 0;
+    long long hull_off = 0;
+    for (int s = 0; s < S; ++s)
+    {
+        sc_cube0[s] = b;
+        sc_nc[s] = (int)snc[s];
+        sc_ns[s] = (int)sns[s];
+        sc_pair0[s] = pair_acc;
+        pair_acc += scene_pair_count(snc[s], sns[s]);
+        max_bodies = std::max(max_bodies, (int)(snc[s] + sns[s]));
+        if (sp)
+        {
+            sc_cr[s] = sp[s].cr;
+            sc_cf[s] = sp[s].cf;
+            sc_iters[s] = sp[s].iterations;
+        }
+        else
+        {
+            sc_cr[s] = (float)0.1;
+            sc_cf[s] = 0.1f;
+            sc_iters[s] = 70;
+        }
+        for (uint32_t i = 0; i < snc[s]; ++i, ++b)
+        {
+            const nans_cube &r = cubes[cube_rank];
+            int np = hull_npts ? hull_npts[cube_rank] : 0;
+            int4 sh;
+            sh.x = (int)vert_floats;
+            if (np > 0)
+            {
+                sh.y = np;
+                sh.z = (int)local.size();
+                for (int k = 0; k < 3 * np; ++k)
+                    local.push_back(hull_pts[3 * hull_off + k]);
+                hull_off += np;
+            }
+            else
+            {
+                sh.y = 8;
+                sh.z = -1;
+            }
+            sh.w = 0;
+            // whole groups of four vertices (12 floats): hull_support reads group-wise
+            vert_floats += ((sh.y + 3LL) / 4) * 12;
+            shape[b] = sh;
+            if (cube_scale)
+                scl[b] = make_float4(cube_scale[3 * cube_rank], cube_scale[3 * cube_rank + 1],
+                                     cube_scale[3 * cube_rank + 2], 0.0f);
+            else
+                scl[b] = make_float4(r.Size, r.Size, r.Size, 0.0f);
+            size_moi[b] = make_float2(r.Size, r.MOI);
+            body_scene[b] = s;
+            body_rec[b] = cube_rank++;
+        }
+        for (uint32_t i = 0; i < sns[s]; ++i, ++b)
+        {
+            const nans_sphere &r = spheres[sphere_rank];
+            shape[b] = make_int4(0, 0, -1, 0);
+            scl[b] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+            size_moi[b] = make_float2(0.0f, r.MOI);
+            body_scene[b] = s;
+            body_rec[b] = -(sphere_rank++) - 1;
+        }
+    }
+    sc_pair0[S] = pair_acc;
+    for (int s = 0; s < S; ++s)
+    {
+        int fb = ndyn + s;
+        shape[fb] = make_int4((int)vert_floats, 8, -1, 0);
+        vert_floats += 24;
+        scl[fb] = make_float4(floors[s].Size, 1.0f, floors[s].Size, 0.0f);
+        size_moi[fb] = make_float2(floors[s].Size, floors[s].MOI);
+        body_scene[fb] = s;
+        body_rec[fb] = s;
+    }
+    for (int s = 0; s < S; ++s)
+        sc_order[s] = s;
+    std::stable_sort(sc_order.begin(), sc_order.end(),
+                     [&](int x, int y) { return sc_nc[x] + sc_ns[x] > sc_nc[y] + sc_ns[y]; });
+    if ((size_t)max_bodies * sizeof(int) > kSolveSmemMax)
+        return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: a scene has more bodies than the solver's wave table holds");
+
+    w->pair_total = pair_acc;
+    w->cull_blocks = (int)((pair_acc + kPairsPerBlock - 1) / kPairsPerBlock);
+    w->max_scene_bodies = max_bodies;
+
+    DevWorld &d = w->dw;
+    d = DevWorld{};
+    d.n_scenes = S;
+    d.n_dyn = ndyn;
+    d.n_all = nall;
+    d.pair_total = pair_acc;
+    auto &L = w->allocs;
+    int rc;
+    int *p_cube0, *p_nc, *p_ns, *p_iters, *p_order, *p_bscene;
+    long long *p_pair0;
+    float *p_cr, *p_cf, *p_local;
+    int4 *p_shape;
+    if ((rc = dalloc(w, L, &p_cube0, S)) || (rc = dalloc(w, L, &p_nc, S)) || (rc = dalloc(w, L, &p_ns, S)) ||
+        (rc = dalloc(w, L, &p_iters, S)) || (rc = dalloc(w, L, &p_order, S)) || (rc = dalloc(w, L, &p_pair0, S + 1)) ||
+        (rc = dalloc(w, L, &p_cr, S)) || (rc = dalloc(w, L, &p_cf, S)) || (rc = dalloc(w, L, &p_bscene, nall)) ||
+        (rc = dalloc(w, L, &w->d_body_rec, nall)) || (rc = dalloc(w, L, &p_shape, nall)) ||
+        (rc = dalloc(w, L, &w->d_scl, nall)) || (rc = dalloc(w, L, &w->d_size_moi, nall)) ||
+        (rc = dalloc(w, L, &p_local, local.size())) || (rc = dalloc(w, L, &d.verts, vert_floats)) ||
+        (rc = dalloc(w, L, &d.pos, nall)) || (rc = dalloc(w, L, &d.ang, nall)) || (rc = dalloc(w, L, &d.vel, nall)) ||
+        (rc = dalloc(w, L, &d.omg, nall)) || (rc = dalloc(w, L, &d.frc, nall)) || (rc = dalloc(w, L, &d.trq, nall)) ||
+        (rc = dalloc(w, L, &w->d_prm, nall)) || (rc = dalloc(w, L, &w->d_model_in, (size_t)4 * nall)) ||
+        (rc = dalloc(w, L, &d.box_lo, nall)) || (rc = dalloc(w, L, &d.box_hi, nall)) ||
+        (rc = dalloc(w, L, &d.pair_mask, (size_t)((pair_acc + 31) / 32))) ||
+        (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.n_cand, 1)) ||
+        (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
+        (rc = dalloc(w, L, &d.work_counter, 2)) || (rc = dalloc(w, L, &d.status, 1)) ||
+        (rc = dalloc(w, L, &w->d_rec_cube, (size_t)61 * tc)) || (rc = dalloc(w, L, &w->d_rec_sphere, (size_t)37 * ts)) ||
+        (rc = dalloc(w, L, &w->d_rec_floor, (size_t)61 * S)) || (rc = dalloc(w, L, &w->d_small, 2)) ||
+        (rc = dalloc(w, L, &d.s_last, 1)))
+        return rc;
+    d.sc_cube0 = p_cube0;
+    d.sc_nc = p_nc;
+    d.sc_ns = p_ns;
+    d.sc_iters = p_iters;
+    d.sc_order = p_order;
+    d.sc_pair0 = p_pair0;
+    d.sc_cr = p_cr;
+    d.sc_cf = p_cf;
+    d.body_scene = p_bscene;
+    d.shape = p_shape;
+    d.local_pts = p_local;
+    d.scl = w->d_scl;
+    d.prm = w->d_prm;
+    d.model_in = w->d_model_in;
+    cudaStream_t st = w->stream;
+    CK(cudaMemcpyAsync(p_cube0, sc_cube0.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_nc, sc_nc.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_ns, sc_ns.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_iters, sc_iters.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_order, sc_order.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_pair0, sc_pair0.data(), (S + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_cr, sc_cr.data(), S * sizeof(float), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_cf, sc_cf.data(), S * sizeof(float), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_bscene, body_scene.data(), nall * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w->d_body_rec, body_rec.data(), nall * sizeof(int), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_shape, shape.data(), nall * sizeof(int4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w->d_scl, scl.data(), nall * sizeof(float4), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w->d_size_moi, size_moi.data(), nall * sizeof(float2), cudaMemcpyHostToDevice, st));
+    if (!local.empty())
+        CK(cudaMemcpyAsync(p_local, local.data(), local.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    if (tc)
+        CK(cudaMemcpyAsync(w->d_rec_cube, cubes, tc * sizeof(nans_cube), cudaMemcpyHostToDevice, st));
+    if (ts)
+        CK(cudaMemcpyAsync(w->d_rec_sphere, spheres, ts * sizeof(nans_sphere), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(w->d_rec_floor, floors, S * sizeof(nans_cube), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
+    CK(cudaMemsetAsync(d.n_cand, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(d.cand_begin, 0, S * sizeof(int), st));
+    CK(cudaMemsetAsync(d.cand_end, 0, S * sizeof(int), st));
+    const int mode = 1 | ((flags & NANS_UPLOAD_KEEP_MODEL) ? 2 : 0);
+    k_unpack<<<(nall + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(
+        d, w->d_rec_cube, w->d_rec_sphere, w->d_rec_floor, w->d_body_rec, mode, w->d_prm, w->d_model_in);
+    CK(cudaGetLastError());
+
+    int cap = (int)(w->max_cand_req ? w->max_cand_req : std::min<long long>(16LL * ndyn + 4096, INT32_MAX / 16));
+    if ((rc = alloc_candidates(w, std::max(1, cap))))
+        return rc;
+    if ((size_t)max_bodies * sizeof(int) > 48 * 1024)
+        CK(cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)solve_smem(w)));
+    CK(cudaStreamSynchronize(st));
+    w->uploaded = true;
+    w->pending = false;
+    w->pending_dt = 0.0f;
+    w->model_input = (flags & NANS_UPLOAD_KEEP_MODEL) != 0;
+    w->forces_pending = true;
+    w->steps_run = 0;
+    return NANS_OK;
+}
+
+// Enqueues the cull (three kernels) on the world's stream.
+void enqueue_cull(nans_world *w)
+{
+    cudaStream_t st = w->stream;
+    int all_pairs = (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0;
+    if (w->cull_blocks > 0)
+        k_cull_mask<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw, all_pairs);
+    k_scan_blocks<<<1, 1024, 0, st>>>(w->dw, w->cull_blocks);
+    if (w->cull_blocks > 0)
+        k_cull_write<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
+}
+
+void enqueue_narrow_solve(nans_world *w, float dt)
+{
+    cudaStream_t st = w->stream;
+    launch_narrow(w->narrow_warps, narrow_grid(w), st, w->dw);
+    k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+}
+
+int sweep_flags(const nans_world *w)
+{
+    int f = SW_INTEGRATE;
+    if (w->pending)
+        f |= SW_APPLY_VEL;
+    if (w->model_input)
+        f |= SW_MODEL_INPUT;
+    if (w->forces_pending)
+        f |= SW_FORCES;
+    return f;
+}
+
+void after_step(nans_world *w, float dt)
+{
+    w->pending = true;
+    w->pending_dt = dt;
+    w->model_input = false;
+    w->forces_pending = false;
+    ++w->steps_run;
+}
+
+// One step, stage by stage. With check_capacity the candidate count is read back after the
+// scan and the candidate buffers grow if needed (the plain path).
+int step_eager(nans_world *w, float dt, bool check_capacity)
+{
+    cudaStream_t st = w->stream;
+    DevWorld &d = w->dw;
+    CK(cudaMemsetAsync(d.work_counter, 0, 2 * sizeof(int), st));
+    CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
+    CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
+    k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
+                                                                                       sweep_flags(w));
+    enqueue_cull(w);
+    CK(cudaGetLastError());
+    if (check_capacity)
+    {
+        unsigned status = 0;
+        CK(cudaMemcpyAsync(&status, d.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (status & ST_CANDIDATES)
+        {
+            // count again without the cap: the block offsets hold the exact total
+            long long total = 0;
+            std::vector<int> off(std::max(1, w->cull_blocks));
+            // recount: rerun the mask pass to get per-block counts, then sum on the host
+            int all_pairs = (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0;
+            k_cull_mask<<<w->cull_blocks, kCullThreads, 0, st>>>(d, all_pairs);
+            CK(cudaMemcpyAsync(off.data(), d.block_hits, w->cull_blocks * sizeof(int), cudaMemcpyDeviceToHost, st));
+            CK(cudaStreamSynchronize(st));
+            for (int v : off)
+                total += v;
+            int rc = alloc_candidates(w, (int)std::min<long long>(total + total / 4 + 1024, INT32_MAX / 16));
+            if (rc)
+                return rc;
+            CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
+            k_scan_blocks<<<1, 1024, 0, st>>>(w->dw, w->cull_blocks);
+            k_cull_write<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
+            CK(cudaGetLastError());
+        }
+    }
+    enqueue_narrow_solve(w, dt);
+    CK(cudaGetLastError());
+    after_step(w, dt);
+    return NANS_OK;
+}
+
+int check_status(nans_world *w)
+{
+    unsigned status = 0;
+    CK(cudaMemcpyAsync(&status, w->dw.status, sizeof(unsigned), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    if (status & ST_CANDIDATES)
+        return fail(NANS_ERR_CAPACITY, "step: more candidate pairs than the world's capacity");
+    if (status & (ST_EPA_FACES | ST_EPA_EDGES))
+        return fail(NANS_ERR_EPA_CAPACITY, "step: an EPA polytope outgrew its shared-memory buffers");
+    return NANS_OK;
+}
+
+void set_params_all(nans_world *w, const nans_step_params *p)
+{
+    std::vector<float> cr(w->n_scenes, p->cr), cf(w->n_scenes, p->cf);
+    std::vector<int> it(w->n_scenes, p->iterations);
+    cudaMemcpyAsync((void *)w->dw.sc_cr, cr.data(), cr.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream);
+    cudaMemcpyAsync((void *)w->dw.sc_cf, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream);
+    cudaMemcpyAsync((void *)w->dw.sc_iters, it.data(), it.size() * sizeof(int), cudaMemcpyHostToDevice, w->stream);
+    cudaStreamSynchronize(w->stream);
+}
+
+bool steady(const nans_world *w, float dt)
+{
+    return w->pending && w->pending_dt == dt && !w->model_input && !w->forces_pending;
+}
+
+int ensure_graph(nans_world *w, float dt, int gsteps)
+{
+    if (w->gexec && w->g_steps == gsteps && w->g_dt == dt && w->g_cfg == cfg_id(w))
+        return NANS_OK;
+    drop_graph(w);
+    cudaStream_t st = w->stream;
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    DevWorld &d = w->dw;
+    for (int i = 0; i < gsteps; ++i)
+    {
+        cudaMemsetAsync(d.work_counter, 0, 2 * sizeof(int), st);
+        cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st);
+        cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st);
+        k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, dt, dt,
+                                                                                           SW_INTEGRATE | SW_APPLY_VEL);
+        enqueue_cull(w);
+        enqueue_narrow_solve(w, dt);
+    }
+    cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e != cudaSuccess)
+        return fail(NANS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&w->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+    {
+        w->gexec = nullptr;
+        return fail(NANS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    w->g_steps = gsteps;
+    w->g_dt = dt;
+    w->g_cfg = cfg_id(w);
+    return NANS_OK;
+}
+
+int batch_steps(nans_world *w, float dt, uint32_t nsteps, uint32_t gsteps)
+{
+    uint32_t done = 0;
+    int rc;
+    while (done < nsteps && !steady(w, dt))
+    {
+        if ((rc = step_eager(w, dt, false)))
+            return rc;
+        ++done;
+    }
+    uint32_t rem = nsteps - done;
+    if (gsteps > 0 && rem >= gsteps)
+    {
+        if ((rc = ensure_graph(w, dt, (int)gsteps)))
+            return rc;
+        for (uint32_t g = 0; g < rem / gsteps; ++g)
+            CK(cudaGraphLaunch(w->gexec, w->stream));
+        w->steps_run += (rem / gsteps) * gsteps;
+        rem %= gsteps;
+    }
+    for (uint32_t i = 0; i < rem; ++i)
+        if ((rc = step_eager(w, dt, false)))
+            return rc;
+    return NANS_OK;
+}
+
+int valid_dt(float dt) { return std::isfinite(dt) && dt > 0.0f; }
+
+} // namespace
+
+extern "C" {
+
+const char *nans_last_error(void) { return g_err.c_str(); }
+
+int nans_world_create(const nans_world_desc *desc, nans_world **out)
+{
+    if (!out)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "create: null output pointer");
+    *out = nullptr;
+    nans_world *w = new nans_world();
+    if (desc)
+    {
+        w->device = desc->device;
+        w->flags = desc->flags;
+        w->max_cand_req = desc->max_candidates;
+    }
+    cudaError_t e = cudaSetDevice(w->device);
+    if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&w->sm_count, cudaDevAttrMultiProcessorCount, w->device);
+    if (e != cudaSuccess)
+    {
+        delete w;
+        return fail(NANS_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
+    }
+    *out = w;
+    return NANS_OK;
+}
+
+int nans_world_destroy(nans_world *w)
+{
+    if (!w)
+        return NANS_OK;
+    cudaSetDevice(w->device);
+    if (w->stream)
+        cudaStreamSynchronize(w->stream);
+    drop_graph(w);
+    free_list(w->allocs);
+    free_list(w->cand_allocs);
+    if (w->d_pairs_out)
+        cudaFree(w->d_pairs_out);
+    if (w->d_snap)
+        cudaFree(w->d_snap);
+    if (w->stream)
+        cudaStreamDestroy(w->stream);
+    delete w;
+    return NANS_OK;
+}
+
+int nans_world_upload(nans_world *w, const nans_cube *cubes, uint32_t ncubes, const nans_sphere *spheres,
+                      uint32_t nspheres, const nans_cube *floor, const float *cube_scale, uint32_t flags)
+{
+    uint32_t nc = ncubes, ns = nspheres;
+    return upload_impl(w, 1, &nc, &ns, cubes, spheres, floor, cube_scale, nullptr, nullptr, nullptr, flags);
+}
+
+int nans_batch_upload(nans_world *w, uint32_t nscenes, const uint32_t *scene_ncubes, const uint32_t *scene_nspheres,
+                      const nans_cube *cubes, const nans_sphere *spheres, const nans_cube *floors,
+                      const float *cube_scale, const int32_t *hull_npts, const float *hull_pts,
+                      const nans_step_params *scene_params, uint32_t flags)
+{
+    return upload_impl(w, nscenes, scene_ncubes, scene_nspheres, cubes, spheres, floors, cube_scale, hull_npts,
+                       hull_pts, scene_params, flags);
+}
+
+int nans_step(nans_world *w, const nans_step_params *params, float dt, uint32_t nsteps)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "step: null world");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "step: no scene uploaded");
+    if (!valid_dt(dt))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "step: dt must be finite and positive");
+    CK(cudaSetDevice(w->device));
+    if (params)
+        set_params_all(w, params);
+    CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), w->stream));
+    for (uint32_t i = 0; i < nsteps; ++i)
+    {
+        int rc = step_eager(w, dt, true);
+        if (rc)
+            return rc;
+    }
+    return check_status(w);
+}
+
+int nans_batch_step(nans_world *w, float dt, uint32_t nsteps, uint32_t graph_steps)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "batch_step: null world");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "batch_step: no scene uploaded");
+    if (!valid_dt(dt))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "batch_step: dt must be finite and positive");
+    CK(cudaSetDevice(w->device));
+    CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), w->stream));
+    int rc = batch_steps(w, dt, nsteps, graph_steps ? graph_steps : 60);
+    if (rc)
+        return rc;
+    return check_status(w);
+}
+
+int nans_batch_autotune(nans_world *w, float dt)
+{
+    if (!w || !w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "autotune: no scene uploaded");
+    if (!valid_dt(dt))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "autotune: dt must be finite and positive");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    const size_t n = (size_t)w->n_all;
+    if (!w->d_snap)
+        CK(cudaMalloc(&w->d_snap, 6 * n * sizeof(float4)));
+    // snapshot the mutable state and the host-side step flags
+    float4 *bufs[6] = {w->dw.pos, w->dw.ang, w->dw.vel, w->dw.omg, w->dw.frc, w->dw.trq};
+    for (int i = 0; i < 6; ++i)
+        CK(cudaMemcpyAsync(w->d_snap + i * n, bufs[i], n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    const bool s_pending = w->pending, s_model = w->model_input, s_forces = w->forces_pending;
+    const float s_pdt = w->pending_dt;
+    const long long s_steps = w->steps_run;
+    struct Cfg
+    {
+        int warps, nbpsm, sbpsm;
+    };
+    const Cfg cands[] = {{4, 0, 0}, {8, 0, 0}, {4, 8, 0}, {8, 4, 0}, {4, 0, 4}, {8, 0, 2}};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    Cfg bestc = cands[0];
+    int rc = NANS_OK;
+    for (const Cfg &c : cands)
+    {
+        w->narrow_warps = c.warps;
+        w->narrow_bpsm = c.nbpsm;
+        w->solve_bpsm = c.sbpsm;
+        if ((rc = step_eager(w, dt, false)))
+            break;
+        cudaEventRecord(e0, st);
+        for (int k = 0; k < 2 && rc == NANS_OK; ++k)
+            rc = step_eager(w, dt, false);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best)
+        {
+            best = ms;
+            bestc = c;
+        }
+        for (int i = 0; i < 6; ++i)
+            cudaMemcpyAsync(bufs[i], w->d_snap + i * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+        w->pending = s_pending;
+        w->model_input = s_model;
+        w->forces_pending = s_forces;
+        w->pending_dt = s_pdt;
+        w->steps_run = s_steps;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    w->narrow_warps = bestc.warps;
+    w->narrow_bpsm = bestc.nbpsm;
+    w->solve_bpsm = bestc.sbpsm;
+    drop_graph(w);
+    CK(cudaStreamSynchronize(st));
+    CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), st));
+    return rc;
+}
+
+int nans_world_download(nans_world *w, nans_cube *cubes, nans_sphere *spheres, nans_cube *floors)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "download: null world");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "download: no scene uploaded");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    if (w->pending)
+    {
+        k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(w->dw, w->pending_dt, 0.0f,
+                                                                                           SW_APPLY_VEL);
+        w->pending = false;
+        w->model_input = false;
+    }
+    k_pack<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(
+        w->dw, w->d_rec_cube, w->d_rec_sphere, w->d_rec_floor, w->d_body_rec, w->d_size_moi, w->steps_run > 0);
+    CK(cudaGetLastError());
+    if (cubes && w->n_cubes)
+        CK(cudaMemcpyAsync(cubes, w->d_rec_cube, w->n_cubes * sizeof(nans_cube), cudaMemcpyDeviceToHost, st));
+    if (spheres && w->n_spheres)
+        CK(cudaMemcpyAsync(spheres, w->d_rec_sphere, w->n_spheres * sizeof(nans_sphere), cudaMemcpyDeviceToHost, st));
+    if (floors)
+        CK(cudaMemcpyAsync(floors, w->d_rec_floor, w->n_scenes * sizeof(nans_cube), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return NANS_OK;
+}
+
+int nans_world_set_state(nans_world *w, const nans_cube *cubes, const nans_sphere *spheres, uint32_t flags)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "set_state: null world");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "set_state: no scene uploaded");
+    if ((w->n_cubes && !cubes) || (w->n_spheres && !spheres))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "set_state: null body records");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    if (w->n_cubes)
+        CK(cudaMemcpyAsync(w->d_rec_cube, cubes, w->n_cubes * sizeof(nans_cube), cudaMemcpyHostToDevice, st));
+    if (w->n_spheres)
+        CK(cudaMemcpyAsync(w->d_rec_sphere, spheres, w->n_spheres * sizeof(nans_sphere), cudaMemcpyHostToDevice, st));
+    const int mode = (flags & NANS_UPLOAD_KEEP_MODEL) ? 2 : 0;
+    // floors keep their state: unpack only the dynamic bodies
+    DevWorld d = w->dw;
+    d.n_all = w->n_dyn;
+    if (w->n_dyn > 0)
+        k_unpack<<<(w->n_dyn + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(
+            d, w->d_rec_cube, w->d_rec_sphere, w->d_rec_floor, w->d_body_rec, mode, w->d_prm, w->d_model_in);
+    CK(cudaGetLastError());
+    w->pending = false;
+    w->model_input = (flags & NANS_UPLOAD_KEEP_MODEL) != 0;
+    w->forces_pending = true;
+    return NANS_OK;
+}
+
+int nans_get_pairs(nans_world *w, uint32_t scene, nans_contact_pair *out, uint32_t cap, uint32_t *count)
+{
+    if (!w || !count)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "get_pairs: null world or count");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "get_pairs: no scene uploaded");
+    if ((int)scene >= w->n_scenes)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "get_pairs: scene index out of range");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    if ((int)cap > w->pairs_out_cap)
+    {
+        if (w->d_pairs_out)
+            cudaFree(w->d_pairs_out);
+        w->d_pairs_out = nullptr;
+        CK(cudaMalloc(&w->d_pairs_out, (size_t)std::max<uint32_t>(cap, 1) * sizeof(nans_contact_pair)));
+        w->pairs_out_cap = (int)std::max<uint32_t>(cap, 1);
+    }
+    k_pairs_out<<<1, 256, 0, st>>>(w->dw, (int)scene, w->d_pairs_out, (int)cap, w->d_small);
+    CK(cudaGetLastError());
+    int n = 0;
+    CK(cudaMemcpyAsync(&n, w->d_small, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    *count = (uint32_t)n;
+    uint32_t m = std::min<uint32_t>((uint32_t)n, cap);
+    if (out && m)
+    {
+        CK(cudaMemcpyAsync(out, w->d_pairs_out, m * sizeof(nans_contact_pair), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+    }
+    return NANS_OK;
+}
+
+int nans_world_status(nans_world *w, uint32_t *bits)
+{
+    if (!w || !bits)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "status: null argument");
+    if (!w->uploaded)
+    {
+        *bits = 0;
+        return NANS_OK;
+    }
+    CK(cudaSetDevice(w->device));
+    unsigned s = 0;
+    CK(cudaMemcpyAsync(&s, w->dw.status, sizeof(unsigned), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    *bits = s;
+    return NANS_OK;
+}
+
+int nans_world_counts(nans_world *w, uint32_t *candidates, uint32_t *contacts)
+{
+    if (!w || !w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "counts: no scene uploaded");
+    CK(cudaSetDevice(w->device));
+    int nc = 0;
+    CK(cudaMemcpyAsync(&nc, w->dw.n_cand, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    if (candidates)
+        *candidates = (uint32_t)nc;
+    if (contacts)
+    {
+        std::vector<int> h(std::max(1, nc));
+        if (nc)
+            CK(cudaMemcpy(h.data(), w->dw.hit, nc * sizeof(int), cudaMemcpyDeviceToHost));
+        uint32_t t = 0;
+        for (int i = 0; i < nc; ++i)
+            t += h[i] ? 1u : 0u;
+        *contacts = t;
+    }
+    return NANS_OK;
+}
+
+void *nans_world_stream(nans_world *w) { return w ? (void *)w->stream : nullptr; }
+
+int nans_device_sincos(const float *x, float *s, float *c, uint32_t n)
+{
+    if (!x || !s || !c || n == 0)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "sincos: null argument or n == 0");
+    float *d = nullptr;
+    CK(cudaMalloc(&d, 3 * (size_t)n * sizeof(float)));
+    cudaError_t e = cudaMemcpy(d, x, n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+    {
+        k_sincos<<<(n + 255) / 256, 256>>>(d, d + n, d + 2 * (size_t)n, (int)n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+        e = cudaMemcpy(s, d + n, n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(c, d + 2 * (size_t)n, n * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess)
+        return fail(NANS_ERR_CUDA, std::string("sincos: ") + cudaGetErrorString(e));
+    return NANS_OK;
+}
+
+int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
+    uint32_t k = 4 + (w->cull_blocks > 0 ? 2u : 0u); // sweep, scan, [mask, write], narrow, solve
+    if (batched)
+        *batched = k;
+    if (plain)
+        *plain = k;
+    return NANS_OK;
+}
+
+} // extern "C"

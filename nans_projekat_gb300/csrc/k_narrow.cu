@@ -1,0 +1,545 @@
+// Narrowphase: GJK per candidate pair (one lane each), then EPA per hit (one warp each).
+//
+// GJK follows CheckCollision / EvolveSimplex (code/nans.cpp:571-769, 906-966): the search
+// direction is reset to normalize(PB - PA) on every call, Simplex[0] is the oldest point,
+// at most 65 calls, the degenerate-direction exit at |d| <= 1e-4 and the support test
+// dot(d, P) >= 0. The simplex lives in registers as four named slots.
+//
+// EPA follows ResolveCollision (code/nans.cpp:217-328, 771-904) with the polytope in
+// fixed-capacity shared-memory buffers instead of std::vector:
+//   * vertices are a pool (GJK tetrahedron + one support per iteration);
+//   * faces are an ordered list of vertex indices with their normal and distance; removing
+//     the visible faces is a stable compaction, new faces are appended in edge order -- the
+//     same order vector::erase / push_back produce;
+//   * horizon edges are pushed in the order of the visible faces, each push cancelling the
+//     FIRST stored edge that is its reverse (vertex equality compares P, code/nans.h:251-254).
+// A face's "recomputed" normal in the closest-face search and the removal test equals its
+// stored normal bit for bit (same operands, same operations, the flip is an exact negation),
+// so each face's distance |dot(N, A)| is computed once when the face is created.
+// The warp's lanes share the per-face loops; the sequential parts run redundantly.
+#include "nans_kernels.cuh"
+
+namespace nans
+{
+
+enum
+{
+    G_NOHIT = 0,
+    G_FOUND = 1,
+    G_EVOLVING = 2
+};
+
+// TripleCross (code/nans.cpp:564-569): (A x B) x C = B * dot(C, A) - A * dot(C, B)
+__device__ __forceinline__ v3 triple_cross(v3 a, v3 b, v3 c) { return (dot3(c, a) * b) - (dot3(c, b) * a); }
+
+__device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,
+                                   GV &s3)
+{
+    const v3 dir0 = normalize3(B.p - A.p);
+    int n = 0;
+    int res = G_EVOLVING;
+    for (int it = 0; it <= 64; ++it)
+    {
+        v3 dir = dir0;
+        if (n == 1)
+        {
+            dir = -1.0f * dir;
+        }
+        else if (n == 2)
+        {
+            // ClosestPointOnLine (code/nans.cpp:539-562)
+            v3 a = s0.p, b = s1.p;
+            v3 l = normalize3(b - a);
+            float ln = len3(l);
+            float v = dot3(-a, l) / ln;
+            float u = dot3(b, l) / ln;
+            v3 cp;
+            if (u <= 0.0f)
+                cp = b;
+            else if (v <= 0.0f)
+                cp = a;
+            else
+                cp = (u * a) + (v * b);
+            if (v <= 0.0f)
+                n = 1;
+            else if (u <= 0.0f)
+            {
+                s0 = s1;
+                n = 1;
+            }
+            dir = -cp;
+        }
+        else if (n == 3)
+        {
+            v3 a0 = -s0.p;
+            v3 e1 = s1.p - s0.p;
+            v3 e2 = s2.p - s0.p;
+            v3 tn = cross3(e1, e2);
+            v3 e1n = cross3(e1, tn);
+            v3 e2n = cross3(tn, e2);
+            if (dot3(e2n, a0) > 0.0f)
+            {
+                if (dot3(e2, a0) > 0.0f)
+                {
+                    dir = triple_cross(e2, a0, e2);
+                    s1 = s2;
+                    n = 2;
+                }
+                else if (dot3(e1, a0) > 0.0f)
+                {
+                    dir = triple_cross(e1, a0, e1);
+                    n = 2;
+                }
+                else
+                {
+                    dir = a0;
+                    n = 1;
+                }
+            }
+            else if (dot3(e1n, a0) > 0.0f)
+            {
+                if (dot3(e1, a0) > 0.0f)
+                {
+                    dir = triple_cross(e1, a0, e1);
+                    n = 2;
+                }
+                else
+                {
+                    dir = a0;
+                    n = 1;
+                }
+            }
+            else if (dot3(tn, a0) > 0.0f)
+            {
+                dir = tn;
+            }
+            else
+            {
+                dir = -tn;
+                GV t = s1;
+                s1 = s2;
+                s2 = t;
+            }
+        }
+        else if (n == 4)
+        {
+            v3 da = s0.p - s3.p;
+            v3 db = s1.p - s3.p;
+            v3 dc = s2.p - s3.p;
+            v3 d0 = -1.0f * s3.p;
+            v3 abd = cross3(da, db);
+            v3 bcd = cross3(db, dc);
+            v3 cad = cross3(dc, da);
+            if (dot3(abd, d0) > 0.0f)
+            {
+                s2 = s3;
+                n = 3;
+                dir = abd;
+            }
+            else if (dot3(bcd, d0) > 0.0f)
+            {
+                s0 = s1;
+                s1 = s2;
+                s2 = s3;
+                n = 3;
+                dir = bcd;
+            }
+            else if (dot3(cad, d0) > 0.0f)
+            {
+                s1 = s2;
+                s2 = s3;
+                n = 3;
+                dir = cad;
+            }
+            else
+                return G_FOUND;
+        }
+        if (len3(dir) <= 0.0001f)
+            return G_NOHIT;
+        GV nv = minkowski_support(verts, A, B, dir);
+        if (n == 0)
+            s0 = nv;
+        else if (n == 1)
+            s1 = nv;
+        else if (n == 2)
+            s2 = nv;
+        else
+            s3 = nv;
+        ++n;
+        res = (dot3(dir, nv.p) >= 0.0f) ? G_EVOLVING : G_NOHIT;
+        if (res != G_EVOLVING)
+            return res;
+    }
+    return G_NOHIT; // iteration cap reached while still evolving: no collision
+}
+
+struct EpaSmem
+{
+    float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
+    float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
+    float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
+    float fnx[kEpaMaxFaces], fny[kEpaMaxFaces], fnz[kEpaMaxFaces], fd[kEpaMaxFaces];
+    unsigned char fa[kEpaMaxFaces], fb[kEpaMaxFaces], fc[kEpaMaxFaces];
+    unsigned char ea[kEpaMaxEdges], eb[kEpaMaxEdges];
+    unsigned vis[(kEpaMaxFaces + 31) / 32];
+};
+
+__device__ __forceinline__ v3 pool_p(const EpaSmem &E, int i) { return mk3(E.px[i], E.py[i], E.pz[i]); }
+
+__device__ __forceinline__ void pool_put(EpaSmem &E, int i, const GV &g)
+{
+    E.px[i] = g.p.x;
+    E.py[i] = g.p.y;
+    E.pz[i] = g.p.z;
+    E.ax[i] = g.sa.x;
+    E.ay[i] = g.sa.y;
+    E.az[i] = g.sa.z;
+    E.bx[i] = g.sb.x;
+    E.by[i] = g.sb.y;
+    E.bz[i] = g.sb.z;
+}
+
+// PushTriangle (code/nans.cpp:292-322): N = normalize(cross(B-A, C-A)), flipped to face away
+// from the origin; the face's distance to the origin |dot(N, A)| is cached with it.
+__device__ __forceinline__ void face_put(EpaSmem &E, int f, int a, int b, int c)
+{
+    v3 pa = pool_p(E, a), pb = pool_p(E, b), pc = pool_p(E, c);
+    v3 n = normalize3(cross3(pb - pa, pc - pa));
+    if (dot3(pa, n) < 0.0f)
+        n = -1.0f * n;
+    E.fa[f] = (unsigned char)a;
+    E.fb[f] = (unsigned char)b;
+    E.fc[f] = (unsigned char)c;
+    E.fnx[f] = n.x;
+    E.fny[f] = n.y;
+    E.fnz[f] = n.z;
+    E.fd[f] = fabsf(dot3(n, pa));
+}
+
+// PushEdge (code/nans.cpp:232-266), warp-cooperative. Returns false on overflow.
+__device__ __forceinline__ bool push_edge(EpaSmem &E, int &ne, int u, int v, int lane)
+{
+    v3 pu = pool_p(E, u), pv = pool_p(E, v);
+    int found = -1;
+    for (int base = 0; base < ne; base += 32)
+    {
+        int e = base + lane;
+        bool m = false;
+        if (e < ne)
+            m = eq3(pool_p(E, E.ea[e]), pv) && eq3(pool_p(E, E.eb[e]), pu);
+        unsigned bal = __ballot_sync(0xffffffffu, m);
+        if (bal)
+        {
+            found = base + __ffs(bal) - 1;
+            break;
+        }
+    }
+    if (found >= 0)
+    {
+        // erase: shift the tail down by one (read everything first, then write)
+        unsigned char ta[(kEpaMaxEdges + 31) / 32], tb[(kEpaMaxEdges + 31) / 32];
+#pragma unroll
+        for (int r = 0; r < (kEpaMaxEdges + 31) / 32; ++r)
+        {
+            int e = found + 1 + lane + 32 * r;
+            ta[r] = (e < ne) ? E.ea[e] : 0;
+            tb[r] = (e < ne) ? E.eb[e] : 0;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < (kEpaMaxEdges + 31) / 32; ++r)
+        {
+            int e = found + 1 + lane + 32 * r;
+            if (e < ne)
+            {
+                E.ea[e - 1] = ta[r];
+                E.eb[e - 1] = tb[r];
+            }
+        }
+        __syncwarp();
+        --ne;
+        return true;
+    }
+    if (ne >= kEpaMaxEdges)
+        return false;
+    if (lane == 0)
+    {
+        E.ea[ne] = (unsigned char)u;
+        E.eb[ne] = (unsigned char)v;
+    }
+    __syncwarp();
+    ++ne;
+    return true;
+}
+
+// Returns 1 with the contact written, 0 for "no contact", and sets status bits on overflow.
+__device__ int epa_warp(const DevWorld &w, EpaSmem &E, const Shape &A, const Shape &B, const GV &s0, const GV &s1,
+                        const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n, int lane)
+{
+    if (lane == 0)
+    {
+        pool_put(E, 0, s0);
+        pool_put(E, 1, s1);
+        pool_put(E, 2, s2);
+        pool_put(E, 3, s3);
+    }
+    __syncwarp();
+    // ABC, ACD, ADB, BDC (code/nans.cpp:799-802)
+    if (lane == 0)
+        face_put(E, 0, 0, 1, 2);
+    else if (lane == 1)
+        face_put(E, 1, 0, 2, 3);
+    else if (lane == 2)
+        face_put(E, 2, 0, 3, 1);
+    else if (lane == 3)
+        face_put(E, 3, 1, 3, 2);
+    __syncwarp();
+    int nf = 4, nv = 4;
+    for (int it = 0; it <= 64; ++it)
+    {
+        if (nf == 0)
+        {
+            if (lane == 0)
+                atomicOr(w.status, (unsigned)ST_EPA_EMPTY);
+            return 0;
+        }
+        // closest face: CurrentDistance starts at face 0; strict '<' keeps the first minimum
+        int ci = 0;
+        float d0 = E.fd[0];
+        if (!isnan(d0))
+        {
+            float bd = d0;
+            int bi = 0;
+            for (int f = lane; f < nf; f += 32)
+            {
+                float d = E.fd[f];
+                if (d < bd || (d == bd && f < bi))
+                {
+                    bd = d;
+                    bi = f;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                float od = __shfl_xor_sync(0xffffffffu, bd, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (od < bd || (od == bd && oi < bi))
+                {
+                    bd = od;
+                    bi = oi;
+                }
+            }
+            ci = bi;
+        }
+        const float cur = E.fd[ci];
+        const v3 n = mk3(E.fnx[ci], E.fny[ci], E.fnz[ci]);
+        const GV ns = minkowski_support(w.verts, A, B, n);
+        if (dot3(n, ns.p) - cur < 0.001f)
+        {
+            // Barycentric (code/nans.cpp:771-785) of N*dist on the closest face
+            int ia = E.fa[ci], ib = E.fb[ci], ic = E.fc[ci];
+            v3 pa = pool_p(E, ia), pb = pool_p(E, ib), pc = pool_p(E, ic);
+            v3 p = cur * n;
+            v3 v0 = pb - pa, v1 = pc - pa, v2 = p - pa;
+            float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
+            float d20 = dot3(v2, v0), d21 = dot3(v2, v1);
+            float den = d00 * d11 - d01 * d01;
+            float bv = (d11 * d20 - d01 * d21) / den;
+            float bw = (d00 * d21 - d01 * d20) / den;
+            float bu = 1.0f - bv - bw;
+            if (fabsf(bu) > 1.0f || fabsf(bv) > 1.0f || fabsf(bw) > 1.0f)
+                return 0;
+            if (!isfinite(bu) || !isfinite(bv) || !isfinite(bw))
+                return 0;
+            v3 saa = mk3(E.ax[ia], E.ay[ia], E.az[ia]), sab = mk3(E.ax[ib], E.ay[ib], E.az[ib]),
+               sac = mk3(E.ax[ic], E.ay[ic], E.az[ic]);
+            v3 sba = mk3(E.bx[ia], E.by[ia], E.bz[ia]), sbb = mk3(E.bx[ib], E.by[ib], E.bz[ib]),
+               sbc = mk3(E.bx[ic], E.by[ic], E.bz[ic]);
+            out_pa = ((bu * saa) + (bv * sab)) + (bw * sac);
+            out_n = -1.0f * n;
+            out_pb = ((bu * sba) + (bv * sbb)) + (bw * sbc);
+            return 1;
+        }
+        // faces that see the new support point (code/nans.cpp:869-891)
+        const int nchunks = (nf + 31) >> 5;
+        for (int ch = 0; ch < nchunks; ++ch)
+        {
+            int f = ch * 32 + lane;
+            bool vis = false;
+            if (f < nf)
+            {
+                v3 fa = pool_p(E, E.fa[f]);
+                v3 fn = mk3(E.fnx[f], E.fny[f], E.fnz[f]);
+                vis = dot3(fn, ns.p - fa) > 0.0f;
+            }
+            unsigned bal = __ballot_sync(0xffffffffu, vis);
+            if (lane == 0)
+                E.vis[ch] = bal;
+        }
+        __syncwarp();
+        // horizon edges in face order
+        int ne = 0;
+        bool ok = true;
+        for (int ch = 0; ch < nchunks && ok; ++ch)
+        {
+            unsigned m = E.vis[ch];
+            while (m && ok)
+            {
+                int f = ch * 32 + __ffs(m) - 1;
+                m &= m - 1;
+                int a = E.fa[f], b = E.fb[f], c = E.fc[f];
+                ok = push_edge(E, ne, a, b, lane) && push_edge(E, ne, b, c, lane) && push_edge(E, ne, c, a, lane);
+            }
+        }
+        if (!ok)
+        {
+            if (lane == 0)
+                atomicOr(w.status, (unsigned)ST_EPA_EDGES);
+            return 0;
+        }
+        // stable removal of the visible faces
+        int keep = 0;
+        for (int ch = 0; ch < nchunks; ++ch)
+        {
+            int f = ch * 32 + lane;
+            unsigned vm = E.vis[ch];
+            bool stay = (f < nf) && !((vm >> lane) & 1u);
+            unsigned sm = __ballot_sync(0xffffffffu, stay);
+            int dst = keep + __popc(sm & ((1u << lane) - 1u));
+            float nx = 0.f, ny = 0.f, nz = 0.f, d = 0.f;
+            unsigned char a = 0, b = 0, c = 0;
+            if (stay)
+            {
+                nx = E.fnx[f];
+                ny = E.fny[f];
+                nz = E.fnz[f];
+                d = E.fd[f];
+                a = E.fa[f];
+                b = E.fb[f];
+                c = E.fc[f];
+            }
+            __syncwarp();
+            if (stay)
+            {
+                E.fnx[dst] = nx;
+                E.fny[dst] = ny;
+                E.fnz[dst] = nz;
+                E.fd[dst] = d;
+                E.fa[dst] = a;
+                E.fb[dst] = b;
+                E.fc[dst] = c;
+            }
+            __syncwarp();
+            keep += __popc(sm);
+        }
+        // the new support joins the vertex pool; new faces (S, e.A, e.B) in edge order
+        int sv = nv;
+        if (lane == 0)
+            pool_put(E, sv, ns);
+        ++nv;
+        __syncwarp();
+        if (keep + ne > kEpaMaxFaces)
+        {
+            if (lane == 0)
+                atomicOr(w.status, (unsigned)ST_EPA_FACES);
+            return 0;
+        }
+        for (int j = lane; j < ne; j += 32)
+            face_put(E, keep + j, sv, E.ea[j], E.eb[j]);
+        __syncwarp();
+        nf = keep + ne;
+    }
+    return 0;
+}
+
+__device__ __forceinline__ GV shfl_gv(const GV &g, int src)
+{
+    GV r;
+    r.p = mk3(__shfl_sync(0xffffffffu, g.p.x, src), __shfl_sync(0xffffffffu, g.p.y, src),
+              __shfl_sync(0xffffffffu, g.p.z, src));
+    r.sa = mk3(__shfl_sync(0xffffffffu, g.sa.x, src), __shfl_sync(0xffffffffu, g.sa.y, src),
+               __shfl_sync(0xffffffffu, g.sa.z, src));
+    r.sb = mk3(__shfl_sync(0xffffffffu, g.sb.x, src), __shfl_sync(0xffffffffu, g.sb.y, src),
+               __shfl_sync(0xffffffffu, g.sb.z, src));
+    return r;
+}
+
+// Persistent narrowphase: warps take 32 candidates at a time from a global queue.
+template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_narrow(DevWorld w)
+{
+    __shared__ EpaSmem epa[WARPS];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    EpaSmem &E = epa[wid];
+    const int n = *w.n_cand;
+    for (;;)
+    {
+        int base = 0;
+        if (lane == 0)
+            base = atomicAdd(w.work_counter, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const int c = base + lane;
+        const bool valid = c < n;
+        int res = G_NOHIT;
+        GV s0, s1, s2, s3;
+        int a = 0, b = 0;
+        if (valid)
+        {
+            a = w.cand_a[c];
+            b = w.cand_b[c];
+            int sc = w.cand_meta[c] >> 3;
+            if (c == 0 || (w.cand_meta[c - 1] >> 3) != sc)
+                w.cand_begin[sc] = c;
+            if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
+                w.cand_end[sc] = c + 1;
+            Shape A = load_shape(w, a), B = load_shape(w, b);
+            res = gjk(w.verts, A, B, s0, s1, s2, s3);
+            if (res != G_FOUND)
+                w.hit[c] = 0;
+        }
+        unsigned hits = __ballot_sync(0xffffffffu, valid && res == G_FOUND);
+        while (hits)
+        {
+            int src = __ffs(hits) - 1;
+            hits &= hits - 1;
+            GV t0 = shfl_gv(s0, src), t1 = shfl_gv(s1, src), t2 = shfl_gv(s2, src), t3 = shfl_gv(s3, src);
+            int ga = __shfl_sync(0xffffffffu, a, src), gb = __shfl_sync(0xffffffffu, b, src);
+            Shape A = load_shape(w, ga), B = load_shape(w, gb);
+            v3 pa, pb, nn;
+            int ok = epa_warp(w, E, A, B, t0, t1, t2, t3, pa, pb, nn, lane);
+            __syncwarp();
+            if (lane == 0)
+            {
+                int cc = base + src;
+                w.hit[cc] = ok;
+                if (ok)
+                {
+                    w.c_pa[cc] = f4(pa, 0.0f);
+                    w.c_pb[cc] = f4(pb, 0.0f);
+                    w.c_n[cc] = f4(nn, 0.0f);
+                }
+            }
+        }
+    }
+}
+
+int narrow_blocks_per_sm(int warps)
+{
+    int per = 0;
+    if (warps == 8)
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow<8>, 256, 0);
+    else
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow<4>, 128, 0);
+    return per;
+}
+
+void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
+{
+    if (warps == 8)
+        k_narrow<8><<<grid, 256, 0, st>>>(w);
+    else
+        k_narrow<4><<<grid, 128, 0, st>>>(w);
+}
+
+} // namespace nans

@@ -1,0 +1,353 @@
+// Sequential-impulse solver, one scene per block, scenes taken from a queue.
+//
+// The reference solves the contact list strictly in order (SolveConstraints,
+// code/nans.cpp:1538-1548), each contact reading and then updating the velocities of its
+// two bodies (Constraint, code/nans.cpp:1020-1329); the floor is never written
+// (:1280, :1311). A contact's result depends only on the current V/W of its two bodies, so
+// contacts that touch disjoint dynamic bodies commute exactly. Each contact gets a wave
+// number wave = 1 + max(last wave of body A, last wave of body B); contacts of one wave run
+// in parallel and waves run in order, which reproduces the sequential result bit for bit.
+//
+// Per scene: (1) compact the scene's hits in candidate order, (2) label waves (one thread,
+// shared memory), (3) counting-sort contacts by wave, (4) precompute everything that does
+// not depend on velocities (normal, tangents, lever arms, effective masses, the Baumgarte
+// term) in parallel, (5) per wave: the 'iterations'-step accumulate/clamp loop and the
+// impulse application, in the reference's operation order.
+#include "nans_kernels.cuh"
+
+namespace nans
+{
+
+constexpr int kSolveThreads = 256;
+constexpr int kWaveChunk = 1024;
+
+__device__ __forceinline__ int block_scan_excl(int v, int *sh, int *total)
+{
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        sh[wid] = x;
+    __syncthreads();
+    if (wid == 0)
+    {
+        int nw = blockDim.x >> 5;
+        int t = (lane < nw) ? sh[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o)
+                t += y;
+        }
+        if (lane < nw)
+            sh[lane] = t;
+    }
+    __syncthreads();
+    int pre = (wid > 0 ? sh[wid - 1] : 0) + x - v;
+    *total = sh[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return pre;
+}
+
+// Velocity-independent part of Constraint (code/nans.cpp:1023-1174).
+__device__ __forceinline__ void contact_constants(const DevWorld &w, int c, float dt, float4 *k)
+{
+    int a = w.cand_a[c], b = w.cand_b[c];
+    v3 n = normalize3(xyz(w.c_n[c]));
+    v3 pa = xyz(w.pos[a]), pb = xyz(w.pos[b]);
+    float4 pra = w.prm[a], prb = w.prm[b];
+    float invi1 = pra.w, invi2 = prb.w, invm1 = pra.z, invm2 = prb.z;
+    if (eq3(n, mk3(0.0f, 0.0f, 0.0f)))
+        n = normalize3(pb - pa);
+    v3 r1 = xyz(w.c_pa[c]) - pa;
+    v3 r2 = xyz(w.c_pb[c]) - pb;
+    v3 t1 = (n.x >= 0.57735f) ? mk3(n.y, -n.x, 0.0f) : mk3(0.0f, n.z, -n.y);
+    v3 t2 = cross3(n, t1);
+    float depth = dot3((pa + r1) - (pb + r2), n);
+    v3 rn1 = cross3(r1, n), rn2 = cross3(r2, n);
+    float jn = invm1 + invm2;
+    jn = jn + (invi1 * dot3(rn1, rn1) - invi2 * dot3(-rn2, -rn2));
+    jn = 1.0f / jn;
+    float bias0 = (-0.3f) / dt * depth;
+    v3 r1t1 = cross3(r1, t1), r2t1 = cross3(r2, t1), r1t2 = cross3(r1, t2), r2t2 = cross3(r2, t2);
+    float jt1 = invm1 + invm2;
+    jt1 = jt1 + (invi1 * dot3(r1t1, r1t1) - invi2 * dot3(-r2t1, -r2t1));
+    jt1 = 1.0f / jt1;
+    float jt2 = invm1 + invm2;
+    jt2 = jt2 + (invi1 * dot3(r1t2, r1t2) - invi2 * dot3(-r2t2, -r2t2));
+    jt2 = 1.0f / jt2;
+    k[0] = make_float4(n.x, n.y, n.z, jn);
+    k[1] = make_float4(t1.x, t1.y, t1.z, jt1);
+    k[2] = make_float4(t2.x, t2.y, t2.z, jt2);
+    k[3] = make_float4(rn1.x, rn1.y, rn1.z, bias0);
+    k[4] = make_float4(rn2.x, rn2.y, rn2.z, invm1);
+    k[5] = make_float4(r1t1.x, r1t1.y, r1t1.z, invm2);
+    k[6] = make_float4(r2t1.x, r2t1.y, r2t1.z, invi1);
+    k[7] = make_float4(r1t2.x, r1t2.y, r1t2.z, invi2);
+    k[8] = make_float4(r2t2.x, r2t2.y, r2t2.z, 0.0f);
+}
+
+// sqrt(2) * Cf * Sum in double, stored to float (code/nans.cpp:1199, 1214)
+__device__ __forceinline__ float friction_bound(float cf, float sum)
+{
+    return (float)(1.4142135623730951 * (double)cf * (double)sum);
+}
+
+// Velocity-dependent part of Constraint (code/nans.cpp:1149-1156, 1171-1328).
+__device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const float4 *k, float cr, float cf,
+                                              int iters)
+{
+    int a = w.cand_a[c], b = w.cand_b[c];
+    int type = w.cand_meta[c] & 7;
+    bool writes_b = !type_b_is_floor(type);
+    v3 n = xyz(k[0]), t1 = xyz(k[1]), t2 = xyz(k[2]);
+    float jn = k[0].w, jt1 = k[1].w, jt2 = k[2].w, bias0 = k[3].w;
+    float invm1 = k[4].w, invm2 = k[5].w, invi1 = k[6].w, invi2 = k[7].w;
+    v3 V1 = xyz(__ldcg(w.vel + a)), W1 = xyz(__ldcg(w.omg + a));
+    v3 V2 = xyz(__ldcg(w.vel + b)), W2 = xyz(__ldcg(w.omg + b));
+    float jdvn = dot3(((V1 + cross3(W1, n)) - V2) - cross3(W2, n), n);
+    float jdvt1 = dot3(((V1 + cross3(W1, t1)) - V2) - cross3(W2, t1), t1);
+    float jdvt2 = dot3(((V1 + cross3(W1, t2)) - V2) - cross3(W2, t2), t2);
+    float bias = bias0 + cr * jdvn;
+    float sn = 0.0f, st1 = 0.0f, st2 = 0.0f, dn = 0.0f, dt1 = 0.0f, dt2 = 0.0f;
+    for (int it = 0; it < iters; ++it)
+    {
+        float ln = (-jdvn + bias) * jn;
+        float old = sn;
+        sn = sn + ln;
+        if (sn < 0.0f)
+            sn = 0.0f;
+        dn = sn - old;
+        float lt1 = (-jdvt1) * jt1;
+        old = st1;
+        st1 = st1 + lt1;
+        float m1 = friction_bound(cf, sn);
+        if (st1 < -m1)
+            st1 = -m1;
+        if (st1 > m1)
+            st1 = m1;
+        dt1 = st1 - old;
+        float lt2 = (-jdvt2) * jt2;
+        old = st2;
+        st2 = st2 + lt2;
+        float m2 = friction_bound(cf, sn);
+        if (st2 < -m2)
+            st2 = -m2;
+        if (st2 > m2)
+            st2 = m2;
+        dt2 = st2 - old;
+    }
+    v3 li = dn * n, lt1 = dt1 * t1, lt2 = dt2 * t2;
+    v3 ai1 = dn * xyz(k[3]), ai2 = dn * xyz(k[4]);
+    v3 ai1t1 = dt1 * xyz(k[5]), ai2t1 = dt1 * xyz(k[6]);
+    v3 ai1t2 = dt2 * xyz(k[7]), ai2t2 = dt2 * xyz(k[8]);
+    V1 = V1 + invm1 * li;
+    W1 = W1 + invi1 * ai1;
+    V1 = V1 + invm1 * lt1;
+    W1 = W1 + invi1 * ai1t1;
+    V1 = V1 + invm1 * lt2;
+    W1 = W1 + invi1 * ai1t2;
+    __stcg(w.vel + a, f4(V1, 0.0f));
+    __stcg(w.omg + a, f4(W1, 0.0f));
+    if (writes_b)
+    {
+        V2 = V2 - invm2 * li;
+        W2 = W2 - invi2 * ai2;
+        V2 = V2 - invm2 * lt1;
+        W2 = W2 - invi2 * ai2t1;
+        V2 = V2 - invm2 * lt2;
+        W2 = W2 - invi2 * ai2t2;
+        __stcg(w.vel + b, f4(V2, 0.0f));
+        __stcg(w.omg + b, f4(W2, 0.0f));
+    }
+}
+
+// Dynamic shared memory: int last[max_scene_bodies] (wave of the last contact per body).
+__global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt)
+{
+    extern __shared__ int s_last[];
+    __shared__ int sh[32];
+    __shared__ int s_scene, s_maxw;
+    __shared__ int s_la[kWaveChunk], s_lb[kWaveChunk];
+    const int tid = threadIdx.x;
+    for (;;)
+    {
+        if (tid == 0)
+        {
+            int q = atomicAdd(w.work_counter + 1, 1);
+            s_scene = (q < w.n_scenes) ? w.sc_order[q] : -1;
+        }
+        __syncthreads();
+        const int s = s_scene;
+        if (s < 0)
+            break;
+        const int cb = w.cand_begin[s], ce = w.cand_end[s];
+        const int c0 = w.sc_cube0[s];
+        const int nb = w.sc_nc[s] + w.sc_ns[s];
+        // (1) ordered compaction of the scene's hits
+        int nh = 0;
+        for (int base = cb; base < ce; base += blockDim.x)
+        {
+            int i = base + tid;
+            int h = (i < ce) ? w.hit[i] : 0;
+            int tot;
+            int pre = block_scan_excl(h, sh, &tot);
+            if (h)
+                w.s_order[cb + nh + pre] = i;
+            nh += tot;
+        }
+        if (nh == 0)
+        {
+            __syncthreads();
+            continue;
+        }
+        // (2) wave labels
+        for (int i = tid; i < nb; i += blockDim.x)
+            s_last[i] = 0;
+        if (tid == 0)
+            s_maxw = 0;
+        __syncthreads();
+        for (int base = 0; base < nh; base += kWaveChunk)
+        {
+            int cnt = min(kWaveChunk, nh - base);
+            for (int i = tid; i < cnt; i += blockDim.x)
+            {
+                int c = w.s_order[cb + base + i];
+                int type = w.cand_meta[c] & 7;
+                s_la[i] = w.cand_a[c] - c0;
+                s_lb[i] = type_b_is_floor(type) ? -1 : w.cand_b[c] - c0;
+            }
+            __syncthreads();
+            if (tid == 0)
+            {
+                int maxw = s_maxw;
+                for (int i = 0; i < cnt; ++i)
+                {
+                    int la = s_la[i], lb = s_lb[i];
+                    int wv = s_last[la];
+                    if (lb >= 0)
+                        wv = max(wv, s_last[lb]);
+                    wv += 1;
+                    s_last[la] = wv;
+                    if (lb >= 0)
+                        s_last[lb] = wv;
+                    s_la[i] = wv;
+                    maxw = max(maxw, wv);
+                }
+                s_maxw = maxw;
+            }
+            __syncthreads();
+            for (int i = tid; i < cnt; i += blockDim.x)
+                w.s_wave[cb + base + i] = s_la[i];
+            __syncthreads();
+        }
+        const int maxw = s_maxw;
+        // (3) counting sort by wave: s_wcnt[cb + wave] (waves 1..maxw, maxw <= nh)
+        for (int i = tid; i <= maxw; i += blockDim.x)
+            w.s_wcnt[cb + i] = 0;
+        __syncthreads();
+        for (int i = tid; i < nh; i += blockDim.x)
+            atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i], 1);
+        __syncthreads();
+        {
+            int carry = 0;
+            for (int base = 0; base <= maxw; base += blockDim.x)
+            {
+                int i = base + tid;
+                int v = (i <= maxw) ? w.s_wcnt[cb + i] : 0;
+                int tot;
+                int pre = block_scan_excl(v, sh, &tot);
+                if (i <= maxw)
+                    w.s_wcnt[cb + i] = carry + pre;
+                carry += tot;
+                __syncthreads();
+            }
+        }
+        for (int i = tid; i < nh; i += blockDim.x)
+        {
+            int pos = atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i], 1);
+            w.s_perm[cb + pos] = w.s_order[cb + i];
+        }
+        // (4) velocity-independent constants
+        for (int i = tid; i < nh; i += blockDim.x)
+        {
+            int c = w.s_order[cb + i];
+            float4 k[9];
+            contact_constants(w, c, dt, k);
+#pragma unroll
+            for (int q = 0; q < 9; ++q)
+                w.s_k[(size_t)9 * c + q] = k[q];
+        }
+        __threadfence_block();
+        __syncthreads();
+        // (5) waves in order
+        const float cr = w.sc_cr[s], cf = w.sc_cf[s];
+        const int iters = w.sc_iters[s];
+        for (int wv = 1; wv <= maxw; ++wv)
+        {
+            int lo = __ldcg(w.s_wcnt + cb + wv - 1), hi = __ldcg(w.s_wcnt + cb + wv);
+            for (int i = lo + tid; i < hi; i += blockDim.x)
+            {
+                int c = __ldcg(w.s_perm + cb + i);
+                float4 k[9];
+#pragma unroll
+                for (int q = 0; q < 9; ++q)
+                    k[q] = __ldcg(w.s_k + (size_t)9 * c + q);
+                contact_apply(w, c, k, cr, cf, iters);
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Writes the contact list of one scene in the reference record layout (code/nans.h:338-372),
+// in list order. Single block.
+__global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count)
+{
+    __shared__ int sh[32];
+    const int cb = w.cand_begin[scene], ce = w.cand_end[scene];
+    const int c0 = w.sc_cube0[scene], s0 = c0 + w.sc_nc[scene];
+    int n = 0;
+    for (int base = cb; base < ce; base += blockDim.x)
+    {
+        int i = base + threadIdx.x;
+        int h = (i < ce) ? w.hit[i] : 0;
+        int tot;
+        int pre = block_scan_excl(h, sh, &tot);
+        int slot = n + pre;
+        if (h && slot < cap)
+        {
+            int type = w.cand_meta[i] & 7;
+            int a = w.cand_a[i], b = w.cand_b[i];
+            int ia = type_a_is_sphere(type) ? a - s0 : a - c0;
+            int ib = type_b_is_floor(type) ? ia : (type_b_is_sphere(type) ? b - s0 : b - c0);
+            float *r = out_rec + (size_t)slot * 24;
+            int *ri = reinterpret_cast<int *>(r);
+            for (int q = 0; q < 24; ++q)
+                r[q] = 0.0f;
+            ri[0] = type;
+            float4 pa = w.c_pa[i], pb = w.c_pb[i], nn = w.c_n[i];
+            r[7] = pa.x;
+            r[8] = pa.y;
+            r[9] = pa.z;
+            r[10] = pb.x;
+            r[11] = pb.y;
+            r[12] = pb.z;
+            r[13] = nn.x;
+            r[14] = nn.y;
+            r[15] = nn.z;
+            ri[22] = ia;
+            ri[23] = ib;
+        }
+        n += tot;
+    }
+    if (threadIdx.x == 0)
+        *count = n;
+}
+
+} // namespace nans

@@ -1,0 +1,232 @@
+"""ctypes binding of the C ABI (include/nans_gb300.h) and a small host-side World class that
+mirrors the reference's step interface: bodies go in as the reference's own records
+(cube / sphere, code/nans.h:303-336), the step runs on the GPU, and bodies and the contact
+list (contact_pair, code/nans.h:338-372) come back in the same layouts.
+
+There is no CPU fallback: importing works without a GPU, but every call needs the CUDA
+library and a device, and raises if either is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .types import CUBE_DTYPE, SPHERE_DTYPE, PAIR_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libnans_gb300.so")
+
+NANS_OK = 0
+ERRORS = {
+    1: "NANS_ERR_INVALID_ARGUMENT",
+    2: "NANS_ERR_CAPACITY",
+    3: "NANS_ERR_NAN_INPUT",
+    4: "NANS_ERR_CUDA",
+    5: "NANS_ERR_EPA_CAPACITY",
+    6: "NANS_ERR_NOT_UPLOADED",
+    7: "NANS_ERR_SCENE_TOO_LARGE",
+}
+UPLOAD_KEEP_MODEL = 1
+WORLD_ALL_PAIRS = 1
+
+# Every symbol include/nans_gb300.h declares.
+EXPORTS = (
+    "nans_world_create", "nans_world_destroy", "nans_world_upload", "nans_batch_upload", "nans_step",
+    "nans_batch_step", "nans_batch_autotune", "nans_world_download", "nans_world_set_state",
+    "nans_get_pairs", "nans_world_status", "nans_world_counts", "nans_world_stream",
+    "nans_launches_per_step", "nans_device_sincos", "nans_last_error",
+)
+
+
+class NansError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s: %s" % (ERRORS.get(code, str(code)), msg))
+        self.code = code
+
+
+class WorldDesc(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("flags", ctypes.c_uint32), ("max_candidates", ctypes.c_uint32)]
+
+
+class StepParams(ctypes.Structure):
+    _fields_ = [("cr", ctypes.c_float), ("cf", ctypes.c_float), ("iterations", ctypes.c_int32)]
+
+
+_LIB = None
+_P = ctypes.c_void_p
+_U = ctypes.c_uint32
+_F = ctypes.c_float
+
+
+def load(path=LIB_PATH):
+    """Loads the CUDA library (building it first if it is absent and nvcc is present)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(path):
+        from . import build as _build
+        _build.build()
+    L = ctypes.CDLL(path)
+    L.nans_last_error.restype = ctypes.c_char_p
+    L.nans_world_create.argtypes = [ctypes.POINTER(WorldDesc), ctypes.POINTER(_P)]
+    L.nans_world_destroy.argtypes = [_P]
+    L.nans_world_upload.argtypes = [_P, _P, _U, _P, _U, _P, _P, _U]
+    L.nans_batch_upload.argtypes = [_P, _U, _P, _P, _P, _P, _P, _P, _P, _P, _P, _U]
+    L.nans_step.argtypes = [_P, ctypes.POINTER(StepParams), _F, _U]
+    L.nans_batch_step.argtypes = [_P, _F, _U, _U]
+    L.nans_batch_autotune.argtypes = [_P, _F]
+    L.nans_world_download.argtypes = [_P, _P, _P, _P]
+    L.nans_world_set_state.argtypes = [_P, _P, _P, _U]
+    L.nans_get_pairs.argtypes = [_P, _U, _P, _U, ctypes.POINTER(_U)]
+    L.nans_world_status.argtypes = [_P, ctypes.POINTER(_U)]
+    L.nans_world_counts.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(_U)]
+    L.nans_world_stream.argtypes = [_P]
+    L.nans_world_stream.restype = _P
+    L.nans_launches_per_step.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(_U)]
+    L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
+    _LIB = L
+    return L
+
+
+def _check(rc):
+    if rc != NANS_OK:
+        raise NansError(rc, load().nans_last_error().decode())
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def device_sincos(x):
+    x = np.ascontiguousarray(x, np.float32)
+    s = np.zeros_like(x)
+    c = np.zeros_like(x)
+    _check(load().nans_device_sincos(_ptr(x), _ptr(s), _ptr(c), len(x)))
+    return s, c
+
+
+class World:
+    """A set of independent scenes on one GPU.
+
+    upload(scene)          one scene (the plain drop-in for one reference sdl_state)
+    upload_batch(scenes)   many scenes (the batched form)
+    step(dt, n, params)    the plain path: stage-by-stage launches, synchronised
+    batch_step(dt, n, g)   the batched path: persistent kernels replayed from a CUDA graph
+    """
+
+    def __init__(self, device=0, all_pairs=False, max_candidates=0):
+        self.lib = load()
+        d = WorldDesc(device, WORLD_ALL_PAIRS if all_pairs else 0, max_candidates)
+        h = _P()
+        _check(self.lib.nans_world_create(ctypes.byref(d), ctypes.byref(h)))
+        self.h = h
+        self.scenes = []
+        self._counts = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nans_world_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    # -- upload -------------------------------------------------------------------------
+    def upload(self, scene):
+        self.upload_batch([scene])
+
+    def upload_batch(self, scenes):
+        scenes = list(scenes)
+        self.scenes = scenes
+        ncs = np.array([len(s.cubes) for s in scenes], np.uint32)
+        nss = np.array([len(s.spheres) for s in scenes], np.uint32)
+        cubes = np.ascontiguousarray(np.concatenate([s.cubes for s in scenes])) if ncs.sum() else \
+            np.zeros(0, CUBE_DTYPE)
+        spheres = np.ascontiguousarray(np.concatenate([s.spheres for s in scenes])) if nss.sum() else \
+            np.zeros(0, SPHERE_DTYPE)
+        floors = np.ascontiguousarray(np.concatenate([s.floor for s in scenes]))
+        scale = np.ascontiguousarray(np.concatenate([s.scale_array() for s in scenes]) if ncs.sum() else
+                                     np.zeros((0, 3), np.float32), np.float32)
+        has_hull = any(s.hull_npts is not None for s in scenes)
+        npts = pts = None
+        if has_hull:
+            npts = np.ascontiguousarray(np.concatenate(
+                [s.hull_npts if s.hull_npts is not None else np.zeros(len(s.cubes), np.int32)
+                 for s in scenes]).astype(np.int32))
+            pl = [s.hull_pts for s in scenes if s.hull_pts is not None and len(s.hull_pts)]
+            pts = np.ascontiguousarray(np.concatenate(pl).astype(np.float32)) if pl else np.zeros((1, 3), np.float32)
+        params = (StepParams * len(scenes))()
+        for i, s in enumerate(scenes):
+            params[i].cr = s.constants.cr
+            params[i].cf = s.constants.cf
+            params[i].iterations = s.constants.iterations
+        keep = all(not s.rebuild_models for s in scenes)
+        if not keep and any(not s.rebuild_models for s in scenes):
+            raise ValueError("all scenes of a batch must agree on rebuild_models")
+        self._keep = (cubes, spheres, floors, scale, npts, pts, ncs, nss, params)
+        _check(self.lib.nans_batch_upload(
+            self.h, len(scenes), _ptr(ncs), _ptr(nss), _ptr(cubes), _ptr(spheres), _ptr(floors), _ptr(scale),
+            _ptr(npts), _ptr(pts), ctypes.cast(params, _P), UPLOAD_KEEP_MODEL if keep else 0))
+        self._ncubes = int(ncs.sum())
+        self._nspheres = int(nss.sum())
+        self._cube_off = np.concatenate([[0], np.cumsum(ncs)]).astype(np.int64)
+        self._sphere_off = np.concatenate([[0], np.cumsum(nss)]).astype(np.int64)
+
+    # -- stepping ----------------------------------------------------------------------
+    def step(self, dt, n=1, params=None):
+        p = None
+        if params is not None:
+            p = ctypes.byref(StepParams(params.cr, params.cf, params.iterations))
+        _check(self.lib.nans_step(self.h, p, dt, n))
+
+    def batch_step(self, dt, n=1, graph_steps=60):
+        _check(self.lib.nans_batch_step(self.h, dt, n, graph_steps))
+
+    def autotune(self, dt):
+        _check(self.lib.nans_batch_autotune(self.h, dt))
+
+    # -- readback ----------------------------------------------------------------------
+    def download(self):
+        """(cubes, spheres, floors) for all scenes, concatenated in upload order."""
+        cubes = np.zeros(self._ncubes, CUBE_DTYPE)
+        spheres = np.zeros(self._nspheres, SPHERE_DTYPE)
+        floors = np.zeros(len(self.scenes), CUBE_DTYPE)
+        _check(self.lib.nans_world_download(self.h, _ptr(cubes), _ptr(spheres), _ptr(floors)))
+        return cubes, spheres, floors
+
+    def scene_state(self, i, state=None):
+        cubes, spheres, floors = self.download() if state is None else state
+        return (cubes[self._cube_off[i]:self._cube_off[i + 1]],
+                spheres[self._sphere_off[i]:self._sphere_off[i + 1]], floors[i:i + 1])
+
+    def set_state(self, cubes, spheres, keep_model=False):
+        _check(self.lib.nans_world_set_state(self.h, _ptr(np.ascontiguousarray(cubes)),
+                                             _ptr(np.ascontiguousarray(spheres)),
+                                             UPLOAD_KEEP_MODEL if keep_model else 0))
+
+    def pairs(self, scene=0):
+        cnt = _U()
+        _check(self.lib.nans_get_pairs(self.h, scene, None, 0, ctypes.byref(cnt)))
+        out = np.zeros(cnt.value, PAIR_DTYPE)
+        if cnt.value:
+            _check(self.lib.nans_get_pairs(self.h, scene, _ptr(out), cnt.value, ctypes.byref(cnt)))
+        return out
+
+    def status(self):
+        s = _U()
+        _check(self.lib.nans_world_status(self.h, ctypes.byref(s)))
+        return s.value
+
+    def counts(self):
+        a, b = _U(), _U()
+        _check(self.lib.nans_world_counts(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def launches_per_step(self):
+        a, b = _U(), _U()
+        _check(self.lib.nans_launches_per_step(self.h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    @property
+    def stream(self):
+        return self.lib.nans_world_stream(self.h)

@@ -1,0 +1,123 @@
+"""Test infrastructure: ctypes binding of the oracle restatement (oracle/port/nans_oracle.cpp,
+built by ``make -C oracle port`` into oracle/_build/libnans_oracle.so).
+
+Only tests, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline leg may use this
+module, and only as the checker.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+from nans_projekat_gb300.types import CUBE_DTYPE, SPHERE_DTYPE, PAIR_DTYPE
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libnans_oracle.so")
+
+_P = ctypes.c_void_p
+_U = ctypes.c_uint32
+_F = ctypes.c_float
+_I = ctypes.c_int
+
+_LIB = None
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", HERE, "port"])
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = ctypes.CDLL(LIB_PATH)
+        L.nanso_create.argtypes = [_I]
+        L.nanso_create.restype = _P
+        L.nanso_destroy.argtypes = [_P]
+        L.nanso_num_scenes.argtypes = [_P]
+        L.nanso_num_scenes.restype = _I
+        L.nanso_add_scene.argtypes = [_P, _P, _U, _P, _U, _P, _P, _P, _P, _P, _F, _F, _I, _I]
+        L.nanso_add_scene.restype = _I
+        L.nanso_step.argtypes = [_P, _F, _I, _I]
+        L.nanso_stage.argtypes = [_P, _I, _F, _I]
+        L.nanso_step_range.argtypes = [_P, _I, _I, _F, _I, _I]
+        L.nanso_store.argtypes = [_P, _I, _P, _P, _P]
+        L.nanso_state_f64.argtypes = [_P, _I, _P]
+        L.nanso_pairs.argtypes = [_P, _I, _P, _U]
+        L.nanso_pairs.restype = _U
+        L.nanso_set_constants.argtypes = [_P, _I, _F, _F, _I]
+        L.nanso_sincosf.argtypes = [_P, _P, _P, _I]
+        _LIB = L
+    return _LIB
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+class OracleWorld:
+    """A set of independent scenes stepped by the oracle (FP32 or FP64)."""
+
+    def __init__(self, scenes, fp64=False):
+        self.lib = lib()
+        self.fp64 = bool(fp64)
+        self.h = self.lib.nanso_create(1 if fp64 else 0)
+        self.scenes = list(scenes)
+        self._keep = []
+        for sc in self.scenes:
+            cubes = np.ascontiguousarray(sc.cubes)
+            spheres = np.ascontiguousarray(sc.spheres)
+            floor = np.ascontiguousarray(sc.floor)
+            scale = None if sc.cube_scale is None else np.ascontiguousarray(sc.cube_scale, np.float32)
+            npts = None if sc.hull_npts is None else np.ascontiguousarray(sc.hull_npts, np.int32)
+            pts = None if sc.hull_pts is None else np.ascontiguousarray(sc.hull_pts, np.float32)
+            c = sc.constants
+            self.lib.nanso_add_scene(self.h, _ptr(cubes), len(cubes), _ptr(spheres), len(spheres),
+                                     _ptr(floor), _ptr(scale), None, _ptr(npts), _ptr(pts),
+                                     c.cr, c.cf, c.iterations, 1 if sc.rebuild_models else 0)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.nanso_destroy(self.h)
+            self.h = None
+
+    def step(self, dt, n=1, threads=1):
+        self.lib.nanso_step(self.h, dt, n, threads)
+
+    def stage(self, st, dt, threads=1):
+        self.lib.nanso_stage(self.h, st, dt, threads)
+
+    def step_range(self, lo, hi, dt, n=1, threads=1):
+        self.lib.nanso_step_range(self.h, lo, hi, dt, n, threads)
+
+    def state(self, i=0):
+        sc = self.scenes[i]
+        cubes = np.zeros(len(sc.cubes), CUBE_DTYPE)
+        spheres = np.zeros(len(sc.spheres), SPHERE_DTYPE)
+        floor = np.zeros(1, CUBE_DTYPE)
+        self.lib.nanso_store(self.h, i, _ptr(cubes), _ptr(spheres), _ptr(floor))
+        return cubes, spheres, floor
+
+    def state_f64(self, i=0):
+        """(n_bodies, 12) array: P, V, Angles, W for cubes then spheres."""
+        n = self.scenes[i].n_bodies
+        out = np.zeros((n, 12), np.float64)
+        self.lib.nanso_state_f64(self.h, i, _ptr(out))
+        return out
+
+    def pairs(self, i=0):
+        n = self.lib.nanso_pairs(self.h, i, None, 0)
+        out = np.zeros(n, PAIR_DTYPE)
+        if n:
+            self.lib.nanso_pairs(self.h, i, _ptr(out), n)
+        return out
+
+
+def sincos(x):
+    x = np.ascontiguousarray(x, np.float32)
+    s = np.zeros_like(x)
+    c = np.zeros_like(x)
+    lib().nanso_sincosf(_ptr(x), _ptr(s), _ptr(c), len(x))
+    return s, c

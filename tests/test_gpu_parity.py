@@ -1,0 +1,238 @@
+"""GPU parity tests: the CUDA step, called through the C ABI, against the oracle and the
+golden fixtures made from the reference. Parity is bit-exact (NaN matches NaN) for every
+body state, every contact list and every step."""
+import numpy as np
+import pytest
+
+from helpers import (GOLDEN_CASES, load_golden, step_digest, same_fields, first_difference,
+                     STATE_FIELDS, PAIR_FIELDS)
+from nans_projekat_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def nl():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for -m gpu tests")
+    from nans_projekat_gb300 import lib
+    lib.load()
+    return lib
+
+
+def test_device_sincos_matches_oracle(nl, oracle_lib):
+    from oracle.portbind import sincos
+    rng = np.random.default_rng(0)
+    x = np.concatenate([np.linspace(-720, 720, 100001), rng.uniform(-1e5, 1e5, 100000),
+                        np.array([0.0, -0.0, 1e-38, np.inf, -np.inf, np.nan])]).astype(np.float32)
+    s_h, c_h = sincos(x)
+    s_d, c_d = nl.device_sincos(x)
+    fin = np.isfinite(x)
+    assert s_h[fin].tobytes() == s_d[fin].tobytes()
+    assert c_h[fin].tobytes() == c_d[fin].tobytes()
+    assert np.all(np.isnan(s_d[~fin])) and np.all(np.isnan(c_d[~fin]))
+
+
+def _run_plain_digests(nl, scene, nsteps, all_pairs=False):
+    w = nl.World(all_pairs=all_pairs)
+    w.upload(scene)
+    dt = np.float32(scene.constants.dt)
+    out = []
+    for k in range(1, nsteps + 1):
+        w.step(dt, 1)
+        cubes, spheres, _ = w.download()
+        pairs = w.pairs(0)
+        out.append((step_digest(cubes, spheres, pairs), cubes, spheres, pairs))
+    assert w.status() == 0
+    w.close()
+    return out
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_plain_step_reproduces_reference_golden(nl, case):
+    scene, meta, digests, saved = load_golden(case)
+    res = _run_plain_digests(nl, scene, meta["nsteps"])
+    for k, (d, cubes, spheres, pairs) in enumerate(res, start=1):
+        if d != digests[k - 1]:
+            pytest.fail("%s: step %d differs from the reference" % (case, k))
+        if "cubes_%d" % k in saved:
+            ok, f = same_fields(saved["cubes_%d" % k], cubes, STATE_FIELDS + ("Vertices",))
+            assert ok, (f, first_difference(saved["cubes_%d" % k], cubes, STATE_FIELDS))
+            assert same_fields(saved["spheres_%d" % k], spheres, STATE_FIELDS)[0]
+            assert same_fields(saved["pairs_%d" % k], pairs, PAIR_FIELDS)[0]
+
+
+def test_demo_frames_model_and_vertices(nl):
+    """The reference frame's records after 300 frames, Model and Vertices included."""
+    scene, meta, digests, saved = load_golden("demo_frames")
+    w = nl.World()
+    w.upload(scene)
+    w.step(np.float32(meta["dt"]), 300)
+    cubes, spheres, _ = w.download()
+    assert same_fields(saved["cubes_300"], cubes, STATE_FIELDS + ("Vertices", "Model"))[0]
+    assert same_fields(saved["spheres_300"], spheres, STATE_FIELDS + ("Model",))[0]
+
+
+@pytest.mark.parametrize("seed", [41, 42])
+def test_cull_equals_all_pairs(nl, oracle_lib, seed):
+    """The conservative AABB cull yields exactly the reference's all-pairs result."""
+    rng = scenes.SplitMix64(seed)
+    sc = scenes.stack_scene_random(rng, 64)
+    a = _run_plain_digests(nl, sc, 40, all_pairs=False)
+    b = _run_plain_digests(nl, sc, 40, all_pairs=True)
+    assert [x[0] for x in a] == [x[0] for x in b]
+
+
+def _oracle_states(scenes_list, nsteps, dt, threads=8):
+    from oracle.portbind import OracleWorld
+    w = OracleWorld(scenes_list)
+    w.step(dt, nsteps, threads)
+    return w
+
+
+def test_batched_graph_path_matches_oracle(nl, oracle_lib):
+    batch = scenes.stack_batch(96, seed=5, lo=4, hi=96)
+    dt = np.float32(1 / 60)
+    nsteps = 50
+    w = nl.World()
+    w.upload_batch(batch)
+    w.batch_step(dt, nsteps, graph_steps=20)  # 1 eager + 2 graphs of 20 + 9 eager
+    state = w.download()
+    o = _oracle_states(batch, nsteps, dt)
+    for i, sc in enumerate(batch):
+        cubes, spheres, _ = w.scene_state(i, state)
+        oc, os_, _ = o.state(i)
+        assert same_fields(oc, cubes, STATE_FIELDS + ("Vertices",))[0], (i, first_difference(oc, cubes, STATE_FIELDS))
+        assert same_fields(os_, spheres, STATE_FIELDS)[0], i
+        assert same_fields(o.pairs(i), w.pairs(i), PAIR_FIELDS)[0], i
+    assert w.status() == 0
+
+
+def test_autotune_keeps_results(nl, oracle_lib):
+    batch = scenes.stack_batch(40, seed=6, lo=8, hi=64)
+    dt = np.float32(1 / 60)
+    w = nl.World()
+    w.upload_batch(batch)
+    w.autotune(dt)
+    w.batch_step(dt, 30, graph_steps=10)
+    state = w.download()
+    o = _oracle_states(batch, 30, dt)
+    for i in range(len(batch)):
+        assert same_fields(o.state(i)[0], w.scene_state(i, state)[0], STATE_FIELDS)[0], i
+
+
+def test_large_random_scene_matches_oracle(nl, oracle_lib):
+    """A scaled-down version of the 4,096-box + 512-sphere scene (same distributions)."""
+    sc = scenes.random_scene(1, n_boxes=700, n_spheres=90, extent=16.0)
+    dt = np.float32(1 / 60)
+    w = nl.World()
+    w.upload(sc)
+    w.step(dt, 40)
+    cubes, spheres, _ = w.download()
+    o = _oracle_states([sc], 40, dt)
+    oc, os_, _ = o.state(0)
+    assert same_fields(oc, cubes, STATE_FIELDS + ("Vertices",))[0], first_difference(oc, cubes, STATE_FIELDS)
+    assert same_fields(os_, spheres, STATE_FIELDS)[0]
+    assert same_fields(o.pairs(0), w.pairs(0), PAIR_FIELDS)[0]
+
+
+def test_hull_scenes_match_oracle(nl, oracle_lib):
+    """Convex hulls of 8-32 points (a shape the reference lacks) against the oracle's hull
+    support map with the same first-maximum rule."""
+    batch = scenes.mixed_batch(24, seed=8, lo=8, hi=48)
+    dt = np.float32(1 / 60)
+    w = nl.World()
+    w.upload_batch(batch)
+    w.batch_step(dt, 40, graph_steps=10)
+    state = w.download()
+    o = _oracle_states(batch, 40, dt)
+    for i in range(len(batch)):
+        cubes, spheres, _ = w.scene_state(i, state)
+        oc, os_, _ = o.state(i)
+        assert same_fields(oc, cubes, STATE_FIELDS)[0], (i, first_difference(oc, cubes, STATE_FIELDS))
+        assert same_fields(os_, spheres, STATE_FIELDS)[0], i
+
+
+def test_set_state_continues_exactly(nl):
+    sc = scenes.stack_scene(0)
+    dt = np.float32(1 / 60)
+    a = nl.World()
+    a.upload(sc)
+    a.step(dt, 30)
+    ca, sa, _ = a.download()
+    b = nl.World()
+    b.upload(sc)
+    b.step(dt, 10)
+    cb, sb, _ = b.download()
+    b.set_state(cb, sb, keep_model=True)
+    b.step(dt, 20)
+    cb, sb, _ = b.download()
+    assert same_fields(ca, cb, STATE_FIELDS + ("Vertices", "Model"))[0]
+    assert same_fields(sa, sb, STATE_FIELDS)[0]
+
+
+def test_error_codes(nl):
+    sc = scenes.stack_scene(0)
+    w = nl.World()
+    with pytest.raises(nl.NansError) as e:
+        w.step(np.float32(1 / 60), 1)
+    assert e.value.code == 6  # not uploaded
+    bad = scenes.stack_scene(0)
+    bad.cubes["Mass"][2] = np.nan
+    with pytest.raises(nl.NansError) as e:
+        w.upload(bad)
+    assert e.value.code == 3  # NaN input
+    bad = scenes.stack_scene(0)
+    bad.spheres["Radius"][0] = 0.0
+    with pytest.raises(nl.NansError) as e:
+        w.upload(bad)
+    assert e.value.code == 3
+    w.upload(sc)
+    for dt in (0.0, -1.0, np.inf, np.nan):
+        with pytest.raises(nl.NansError) as e:
+            w.step(np.float32(dt), 1)
+        assert e.value.code == 1
+    with pytest.raises(nl.NansError) as e:
+        w.pairs(5)
+    assert e.value.code == 1
+
+
+def test_candidate_capacity(nl, oracle_lib):
+    """The plain path grows its candidate buffers; the batched (graph) path reports
+    NANS_ERR_CAPACITY instead of dropping pairs."""
+    sc = scenes.stack_scene_random(scenes.SplitMix64(3), 80)
+    dt = np.float32(1 / 60)
+    w = nl.World(max_candidates=4)
+    w.upload(sc)
+    w.step(dt, 5)
+    o = _oracle_states([sc], 5, dt)
+    assert same_fields(o.state(0)[0], w.download()[0], STATE_FIELDS)[0]
+    w2 = nl.World(max_candidates=4)
+    w2.upload_batch([sc])
+    with pytest.raises(nl.NansError) as e:
+        w2.batch_step(dt, 3, graph_steps=2)
+    assert e.value.code == 2
+
+
+def test_full_size_batch_samples_match_oracle(nl, oracle_lib):
+    """16,384 uneven scenes (log-uniform 4..256 bodies) for 20 steps on the GPU; a sample of
+    scenes is replayed on the oracle (scenes are independent) and must match bit for bit."""
+    batch = scenes.stack_batch(16384, seed=2)
+    dt = np.float32(1 / 60)
+    w = nl.World()
+    w.upload_batch(batch)
+    w.batch_step(dt, 20, graph_steps=10)
+    assert w.status() == 0
+    state = w.download()
+    cubes_all, spheres_all, _ = state
+    assert np.all(np.isfinite(cubes_all["Position"]))
+    rng = np.random.default_rng(1)
+    pick = sorted(set(rng.integers(0, len(batch), 48).tolist()) | {int(np.argmax([s.n_bodies for s in batch]))})
+    o = _oracle_states([batch[i] for i in pick], 20, dt)
+    for j, i in enumerate(pick):
+        cubes, spheres, _ = w.scene_state(i, state)
+        oc, os_, _ = o.state(j)
+        assert same_fields(oc, cubes, STATE_FIELDS)[0], (i, first_difference(oc, cubes, STATE_FIELDS))
+        assert same_fields(os_, spheres, STATE_FIELDS)[0], i
+        assert same_fields(o.pairs(j), w.pairs(i), PAIR_FIELDS)[0], i
