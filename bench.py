@@ -1,0 +1,379 @@
+"""Benchmark of the physics step: body-steps/s on one GB300.
+
+Workload (default): 16,384 independent scenes whose body counts are log-uniform in [4, 256]
+(seeded stacks of boxes with half-extents U[0.25, 0.75] on a ground box plus one sphere
+projectile at U[5, 25] m/s), FP32, dt = 1/60, 10 impulse iterations, restitution 0.2,
+friction 0.5; the batched path replays a CUDA graph of 60 steps. A step is one full physics
+step over every scene. value = dynamic body-steps / device time of the timed steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N > 1) every rank steps its own shard of 16,384 scenes (weak scaling, no
+collective on the data path); the timed region is bracketed by barriers and the slowest
+rank's time is used.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s"
+UNIT = "body-steps/s"
+DT = np.float32(1.0 / 60.0)
+ALG_BYTES_SWEEP_BODY = 68 + 72     # read P,A,V,W,m,I,extents; write P,A,V,W,AABB
+ALG_BYTES_SWEEP_BOX_VERTS = 96     # world vertices written for the narrowphase
+ALG_BYTES_NARROW_CAND = 12 + 4 + 2 * (16 + 16) + 2 * 96  # pair, flag, 2 shapes, 2 vertex sets
+ALG_BYTES_NARROW_HIT = 36          # contact points and normal
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=600)
+    p.add_argument("--warmup", type=int, default=60)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--scenes", type=int, default=16384)
+    p.add_argument("--graph-steps", type=int, default=60)
+    p.add_argument("--e2e-steps", type=int, default=30)
+    p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-autotune", action="store_true")
+    return p.parse_args()
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws <= 1:
+        return None, 0, 1
+    import torch
+    import torch.distributed as dist
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    dist.init_process_group(backend)
+    return dist, rank, ws
+
+
+def max_over_ranks(dist, value, device=None):
+    """Maximum of a float over ranks (identity without a process group)."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(dist, value, device=None):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist, device=None):
+    if dist is not None:
+        if device is not None:
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+def make_workload(n_scenes, rank):
+    from nans_projekat_gb300 import scenes
+    return scenes.stack_batch(n_scenes, seed=2 + 1000 * rank)
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------------------
+# CPU baseline: the oracle's restatement of the reference step (or the reference itself
+# compiled headless, where that build is present), all host threads, bounded sample.
+# ---------------------------------------------------------------------------------------
+def cpu_reference_impl():
+    from oracle import refbind
+    try:
+        if refbind.ref_available("refbig"):
+            refbind.lib("refbig")
+            return "reference"
+    except OSError:
+        pass
+    return "port"
+
+
+def cpu_sample_rate(scenes_list, seconds, threads, kind):
+    """body-steps/s of the CPU implementation on a bounded sample of scenes."""
+    stride = max(1, len(scenes_list) // 512)
+    sample = scenes_list[::stride]
+    bodies = sum(s.n_bodies for s in sample)
+    if kind == "reference":
+        from concurrent.futures import ThreadPoolExecutor
+        from oracle.refbind import RefWorld
+        worlds = [RefWorld(s, "refbig") for s in sample]
+        pool = ThreadPoolExecutor(threads)
+
+        def run(n):
+            list(pool.map(lambda w: w.step(DT, n), worlds))
+    else:
+        from oracle.portbind import OracleWorld
+        ow = OracleWorld(sample)
+
+        def run(n):
+            ow.step(DT, n, threads)
+    t0 = time.perf_counter()
+    run(1)
+    t1 = time.perf_counter() - t0
+    n = max(1, min(200, int(seconds / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    run(n)
+    t = time.perf_counter() - t0
+    return {"value": bodies * n / t, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": "%d of the workload's scenes (every %dth, %d bodies) x %d steps, %.1f s" % (
+                len(sample), stride, bodies, n, t)}
+
+
+def run_reference_arm(args):
+    """--impl reference: the CPU implementation of the step, all host threads, each timed
+    step a bounded sample of the workload."""
+    dist, rank, ws = dist_init()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    kind = cpu_reference_impl()
+    batch = make_workload(args.scenes, 0)
+    # sample sized so one step takes ~0.1 s
+    probe = cpu_sample_rate(batch, 0.5, threads, kind)
+    per_step_bodies = max(64, int(probe["value"] * 0.1))
+    stride = max(1, int(sum(s.n_bodies for s in batch) / per_step_bodies))
+    sample = batch[::stride]
+    bodies = sum(s.n_bodies for s in sample)
+    if kind == "reference":
+        from concurrent.futures import ThreadPoolExecutor
+        from oracle.refbind import RefWorld
+        worlds = [RefWorld(s, "refbig") for s in sample]
+        pool = ThreadPoolExecutor(threads)
+
+        def step():
+            list(pool.map(lambda w: w.step(DT, 1), worlds))
+    else:
+        from oracle.portbind import OracleWorld
+        ow = OracleWorld(sample)
+
+        def step():
+            ow.step(DT, 1, threads)
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    t = time.perf_counter() - t0
+    value = bodies * args.steps / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": "stack_batch%d" % args.scenes, "scenes": args.scenes, "dt": float(DT),
+                   "iterations": 10, "sample_scenes_per_step": len(sample), "sample_bodies": bodies},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": "%d scenes (every %dth) per step, %d bodies" % (len(sample), stride, bodies)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+    dist, rank, ws = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    from nans_projekat_gb300 import lib
+    from nans_projekat_gb300.types import CUBE_DTYPE, SPHERE_DTYPE
+
+    batch = make_workload(args.scenes, rank)
+    w = lib.World(device=local)
+    w.upload_batch(batch)
+    bodies = w.n_bodies
+    if not args.no_autotune:
+        w.autotune(DT)
+    # warm-up (also runs the first, non-graph step and captures the graph)
+    w.batch_step(DT, args.warmup, args.graph_steps)
+    stream = torch.cuda.ExternalStream(w.stream, device=device)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    barrier(dist, device)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    w.batch_step(DT, args.steps, args.graph_steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist, device)
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    ms_max = max_over_ranks(dist, ms, device)
+    total_bodies = sum_over_ranks(dist, float(bodies), device)
+    value = total_bodies * args.steps / (ms_max / 1000.0)
+    n_cand, n_contacts = w.counts()
+
+    # per-stage device time from a live event-timed pass over the same world
+    prof_steps = 10
+    stage_ms = w.profile(DT, prof_steps) / prof_steps
+    names = ["k_sweep", "k_cull (3 kernels)", "k_narrow", "k_solve"]
+    dom = int(np.argmax(stage_ms))
+    peak, peak_kind = measured_peaks()
+    n_boxes = int(sum(len(s.cubes) for s in batch))
+    sweep_bytes = ALG_BYTES_SWEEP_BODY * bodies + ALG_BYTES_SWEEP_BOX_VERTS * n_boxes
+    narrow_bytes = ALG_BYTES_NARROW_CAND * n_cand + ALG_BYTES_NARROW_HIT * n_contacts
+    alg = {0: sweep_bytes, 2: narrow_bytes}
+    dom_bytes = alg.get(dom, narrow_bytes)
+    achieved = dom_bytes / (stage_ms[dom] / 1000.0) / 1e9
+    sweep_gbs = sweep_bytes / (stage_ms[0] / 1000.0) / 1e9
+
+    # end to end through the C ABI with pinned host buffers: set_state (H2D), one step,
+    # download (D2H), every step
+    cubes, spheres, floors = w.download()
+    pin_c = torch.empty(cubes.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(CUBE_DTYPE)
+    pin_s = torch.empty(max(1, spheres.nbytes), dtype=torch.uint8, pin_memory=True).numpy()[:spheres.nbytes]
+    pin_s = pin_s.view(SPHERE_DTYPE)
+    pin_c[:] = cubes
+    pin_s[:] = spheres
+    pin_f = np.zeros(len(floors), CUBE_DTYPE)
+    barrier(dist, device)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        w.set_state(pin_c, pin_s, keep_model=True)
+        w.batch_step(DT, 1, args.graph_steps)
+        w.lib.nans_world_download(w.h, pin_c.ctypes.data, pin_s.ctypes.data, pin_f.ctypes.data)
+    te2e = time.perf_counter() - t0
+    te2e = max_over_ranks(dist, te2e, device)
+    e2e_value = total_bodies * args.e2e_steps / te2e
+    rec_bytes = cubes.nbytes + spheres.nbytes
+    launches_batched, _ = w.launches_per_step()
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_sample_rate(batch, args.cpu_seconds, os.cpu_count() or 1, "port")
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {
+                "workload": "stack_batch%d" % args.scenes, "scenes_per_gpu": args.scenes,
+                "bodies_per_gpu": bodies, "body_counts": "log-uniform [4, 256]", "dt": float(DT),
+                "iterations": 10, "restitution": 0.2, "friction": 0.5, "graph_steps": args.graph_steps,
+                "path": "batched (persistent kernels, CUDA graph)",
+                "l2": "working set larger than L2 (%.0f MB of state, vertices and candidates)"
+                      % ((bodies * 64 + n_boxes * 96 + n_cand * 60) / 1e6),
+                "candidates_per_step": n_cand, "contacts_per_step": n_contacts,
+            },
+            "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "peak_source": peak_kind + " hbm_gbs",
+                         "bytes_per_launch": dom_bytes,
+                         "stage_ms": {n: float(x) for n, x in zip(names, stage_ms)},
+                         "sweep": {"achieved": sweep_gbs, "frac": sweep_gbs / peak,
+                                   "bytes_per_launch": sweep_bytes}},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(rec_bytes),
+                    "d2h_bytes_per_step": int(rec_bytes + pin_f.nbytes),
+                    "path": "nans_world_set_state + nans_batch_step(1) + nans_world_download, pinned host"},
+            "gpu_launches": int(launches_batched * args.steps),
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    w.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference_arm(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

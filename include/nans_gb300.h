@@ -183,6 +183,11 @@ int nans_world_counts(nans_world *world, uint32_t *candidates, uint32_t *contact
 /* The world's CUDA stream (a cudaStream_t), for event timing by the caller. */
 void *nans_world_stream(nans_world *world);
 
+/* Runs nsteps steps stage by stage with CUDA events on the world's stream between the
+ * stages and adds each stage's device time in milliseconds to stage_ms[0..3]:
+ * [0] integrate sweep, [1] pair cull (3 kernels), [2] narrowphase (GJK+EPA), [3] solver. */
+int nans_profile_steps(nans_world *world, float dt, uint32_t nsteps, float *stage_ms);
+
 /* Kernel launches per step on the batched path and on the plain path. */
 int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain);
 

@@ -799,13 +799,10 @@ int nans_world_set_state(nans_world *w, const nans_cube *cubes, const nans_spher
         CK(cudaMemcpyAsync(w->d_rec_cube, cubes, w->n_cubes * sizeof(nans_cube), cudaMemcpyHostToDevice, st));
     if (w->n_spheres)
         CK(cudaMemcpyAsync(w->d_rec_sphere, spheres, w->n_spheres * sizeof(nans_sphere), cudaMemcpyHostToDevice, st));
-    const int mode = (flags & NANS_UPLOAD_KEEP_MODEL) ? 2 : 0;
-    // floors keep their state: unpack only the dynamic bodies
-    DevWorld d = w->dw;
-    d.n_all = w->n_dyn;
-    if (w->n_dyn > 0)
-        k_unpack<<<(w->n_dyn + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(
-            d, w->d_rec_cube, w->d_rec_sphere, w->d_rec_floor, w->d_body_rec, mode, w->d_prm, w->d_model_in);
+    // floors keep their state; with KEEP_MODEL their input model is their rebuilt model
+    const int mode = (flags & NANS_UPLOAD_KEEP_MODEL) ? (2 | 4) : 0;
+    k_unpack<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(
+        w->dw, w->d_rec_cube, w->d_rec_sphere, w->d_rec_floor, w->d_body_rec, mode, w->d_prm, w->d_model_in);
     CK(cudaGetLastError());
     w->pending = false;
     w->model_input = (flags & NANS_UPLOAD_KEEP_MODEL) != 0;
@@ -909,6 +906,52 @@ int nans_device_sincos(const float *x, float *s, float *c, uint32_t n)
     if (e != cudaSuccess)
         return fail(NANS_ERR_CUDA, std::string("sincos: ") + cudaGetErrorString(e));
     return NANS_OK;
+}
+
+int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms)
+{
+    if (!w || !stage_ms)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "profile: null argument");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "profile: no scene uploaded");
+    if (!valid_dt(dt))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "profile: dt must be finite and positive");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    cudaEvent_t ev[5];
+    for (int i = 0; i < 5; ++i)
+        CK(cudaEventCreate(&ev[i]));
+    for (int i = 0; i < 4; ++i)
+        stage_ms[i] = 0.0f;
+    DevWorld &d = w->dw;
+    for (uint32_t k = 0; k < nsteps; ++k)
+    {
+        CK(cudaMemsetAsync(d.work_counter, 0, 2 * sizeof(int), st));
+        CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
+        CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
+        CK(cudaEventRecord(ev[0], st));
+        k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
+                                                                                           sweep_flags(w));
+        CK(cudaEventRecord(ev[1], st));
+        enqueue_cull(w);
+        CK(cudaEventRecord(ev[2], st));
+        launch_narrow(w->narrow_warps, narrow_grid(w), st, w->dw);
+        CK(cudaEventRecord(ev[3], st));
+        k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+        CK(cudaEventRecord(ev[4], st));
+        CK(cudaGetLastError());
+        after_step(w, dt);
+        CK(cudaEventSynchronize(ev[4]));
+        for (int i = 0; i < 4; ++i)
+        {
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
+            stage_ms[i] += ms;
+        }
+    }
+    for (int i = 0; i < 5; ++i)
+        cudaEventDestroy(ev[i]);
+    return check_status(w);
 }
 
 int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)

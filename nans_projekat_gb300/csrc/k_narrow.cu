@@ -465,9 +465,11 @@ __device__ __forceinline__ GV shfl_gv(const GV &g, int src)
 }
 
 // Persistent narrowphase: warps take 32 candidates at a time from a global queue.
+// Dynamic shared memory: one EpaSmem per warp.
 template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_narrow(DevWorld w)
 {
-    __shared__ EpaSmem epa[WARPS];
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    EpaSmem *epa = reinterpret_cast<EpaSmem *>(smem_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     EpaSmem &E = epa[wid];
     const int n = *w.n_cand;
@@ -524,22 +526,36 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_narrow(DevW
     }
 }
 
+static size_t narrow_smem(int warps) { return sizeof(EpaSmem) * (size_t)warps; }
+
+static void narrow_attrs()
+{
+    static bool done = false;
+    if (done)
+        return;
+    cudaFuncSetAttribute(k_narrow<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(4));
+    cudaFuncSetAttribute(k_narrow<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(8));
+    done = true;
+}
+
 int narrow_blocks_per_sm(int warps)
 {
+    narrow_attrs();
     int per = 0;
     if (warps == 8)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow<8>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow<8>, 256, narrow_smem(8));
     else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow<4>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow<4>, 128, narrow_smem(4));
     return per;
 }
 
 void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
 {
+    narrow_attrs();
     if (warps == 8)
-        k_narrow<8><<<grid, 256, 0, st>>>(w);
+        k_narrow<8><<<grid, 256, narrow_smem(8), st>>>(w);
     else
-        k_narrow<4><<<grid, 128, 0, st>>>(w);
+        k_narrow<4><<<grid, 128, narrow_smem(4), st>>>(w);
 }
 
 } // namespace nans

@@ -62,11 +62,12 @@ __device__ __forceinline__ m4 load_model_in(const float4 *mi, int b)
     return m;
 }
 
-// Writes hull vertices and returns their AABB.
+// Writes hull vertices and returns their AABB (NaN coordinates make it non-finite).
 __device__ __forceinline__ void write_vertices(const DevWorld &w, const m4 &model, int4 sh, v3 &lo, v3 &hi)
 {
     lo = mk3(FLT_MAX, FLT_MAX, FLT_MAX);
     hi = mk3(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+    bool finite = true;
     float *out = w.verts + sh.x;
     if (sh.z < 0)
     {
@@ -78,6 +79,7 @@ __device__ __forceinline__ void write_vertices(const DevWorld &w, const m4 &mode
             v[3 * k] = p.x;
             v[3 * k + 1] = p.y;
             v[3 * k + 2] = p.z;
+            finite = finite && isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
             lo = mk3(fminf(lo.x, p.x), fminf(lo.y, p.y), fminf(lo.z, p.z));
             hi = mk3(fmaxf(hi.x, p.x), fmaxf(hi.y, p.y), fmaxf(hi.z, p.z));
         }
@@ -95,18 +97,33 @@ __device__ __forceinline__ void write_vertices(const DevWorld &w, const m4 &mode
             out[3 * k] = p.x;
             out[3 * k + 1] = p.y;
             out[3 * k + 2] = p.z;
+            finite = finite && isfinite(p.x) && isfinite(p.y) && isfinite(p.z);
             lo = mk3(fminf(lo.x, p.x), fminf(lo.y, p.y), fminf(lo.z, p.z));
             hi = mk3(fmaxf(hi.x, p.x), fmaxf(hi.y, p.y), fmaxf(hi.z, p.z));
         }
     }
+    if (!finite)
+        lo.x = __int_as_float(0x7fc00000); // marks the box unbounded in store_box
 }
 
-// Inflates an AABB so that the cull keeps every pair whose supports could meet under
-// float rounding: 1e-4 of the larger coordinate magnitude plus 1e-5 m.
+// Stores the AABB the pair cull tests, inflated so that the cull keeps every pair whose
+// supports could meet under float rounding: 1e-4 of the larger coordinate magnitude plus
+// 1e-5 m. A body with a non-finite coordinate, or one beyond 1e6 m, gets an unbounded box:
+// the reference's support map returns (0,0,0) when no vertex beats -FLT_MAX (all dot
+// products NaN), so such a body can "touch" any shape that contains the origin, and only
+// running GJK on its pairs reproduces that.
 __device__ __forceinline__ void store_box(const DevWorld &w, int b, v3 lo, v3 hi)
 {
     float mag = fmaxf(fmaxf(fmaxf(fabsf(lo.x), fabsf(hi.x)), fmaxf(fabsf(lo.y), fabsf(hi.y))),
                       fmaxf(fabsf(lo.z), fabsf(hi.z)));
+    bool bounded = isfinite(lo.x) && isfinite(lo.y) && isfinite(lo.z) && isfinite(hi.x) && isfinite(hi.y) &&
+                   isfinite(hi.z) && mag <= 1e6f;
+    if (!bounded)
+    {
+        w.box_lo[b] = make_float4(-INFINITY, -INFINITY, -INFINITY, 0.0f);
+        w.box_hi[b] = make_float4(INFINITY, INFINITY, INFINITY, 0.0f);
+        return;
+    }
     float m = 1e-4f * mag + 1e-5f;
     w.box_lo[b] = make_float4(lo.x - m, lo.y - m, lo.z - m, 0.0f);
     w.box_hi[b] = make_float4(hi.x + m, hi.y + m, hi.z + m, 0.0f);
@@ -204,12 +221,21 @@ __device__ __forceinline__ float4 rd3(const float *r, int o, float w4) { return 
 // Unpacks records into the state. rec_cube/rec_sphere are indexed by the body's rank
 // among cubes / spheres in upload order; floors follow the cubes in rec_floor.
 // mode bit 0: also unpack masses/MOI into prm (static data); bit 1: keep Model as input.
+// mode bit 2: floors keep their state and get Model = rebuild(Position, Angles, scale) as input
+// model (the state update of nans_world_set_state carries no floor records).
 __global__ void k_unpack(DevWorld w, const float *rec_cube, const float *rec_sphere, const float *rec_floor,
                          const int *body_rec, int mode, float4 *prm_out, float4 *model_out)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
     if (b >= w.n_all)
         return;
+    if (b >= w.n_dyn && (mode & 4))
+    {
+        m4 m = model_of(xyz(w.pos[b]), xyz(w.ang[b]), xyz(w.scl[b]));
+        for (int j = 0; j < 4; ++j)
+            model_out[4 * b + j] = make_float4(m.c[j][0], m.c[j][1], m.c[j][2], m.c[j][3]);
+        return;
+    }
     const float *r;
     bool sphere = false;
     if (b >= w.n_dyn)

@@ -19,11 +19,14 @@ constexpr int kPairsPerThread = 32;
 constexpr int kPairsPerBlock = kCullThreads * kPairsPerThread;
 
 // EPA shared-memory capacities per warp. Vertices: the GJK tetrahedron plus one support per
-// EPA iteration (at most 65, code/nans.cpp:804). Faces grow by at most two per iteration on a
-// convex polytope (4 + 2*65 = 134); the buffers leave headroom and report overflow.
+// EPA iteration (at most 65, code/nans.cpp:804). Faces grow by two per iteration on a convex
+// polytope, but the reference's polytope is not always convex (supports can repeat a vertex,
+// visible sets can be non-manifold) and runs of all 65 iterations are common; measured on the
+// 16,384-scene workload the face list reached ~200 and the horizon ~10 edges. The buffers hold
+// 512 faces and 128 edges and report overflow (NANS_ERR_EPA_CAPACITY) instead of dropping data.
 constexpr int kEpaMaxVerts = 72;
-constexpr int kEpaMaxFaces = 192;
-constexpr int kEpaMaxEdges = 96;
+constexpr int kEpaMaxFaces = 512;
+constexpr int kEpaMaxEdges = 128;
 
 __global__ void k_sweep(DevWorld w, float pending_dt, float dt, int flags);
 __global__ void k_unpack(DevWorld w, const float *rec_cube, const float *rec_sphere, const float *rec_floor,

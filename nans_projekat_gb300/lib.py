@@ -34,7 +34,7 @@ EXPORTS = (
     "nans_world_create", "nans_world_destroy", "nans_world_upload", "nans_batch_upload", "nans_step",
     "nans_batch_step", "nans_batch_autotune", "nans_world_download", "nans_world_set_state",
     "nans_get_pairs", "nans_world_status", "nans_world_counts", "nans_world_stream",
-    "nans_launches_per_step", "nans_device_sincos", "nans_last_error",
+    "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps",
 )
 
 
@@ -84,6 +84,7 @@ def load(path=LIB_PATH):
     L.nans_world_stream.restype = _P
     L.nans_launches_per_step.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(_U)]
     L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
+    L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
     _LIB = L
     return L
 
@@ -226,6 +227,16 @@ class World:
         a, b = _U(), _U()
         _check(self.lib.nans_launches_per_step(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def profile(self, dt, n):
+        """Device milliseconds per stage summed over n steps: sweep, cull, narrowphase, solver."""
+        ms = np.zeros(4, np.float32)
+        _check(self.lib.nans_profile_steps(self.h, dt, n, _ptr(ms)))
+        return ms
+
+    @property
+    def n_bodies(self):
+        return self._ncubes + self._nspheres
 
     @property
     def stream(self):

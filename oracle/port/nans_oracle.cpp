@@ -506,8 +506,21 @@ template <class T> static void barycentric(V3<T> p, V3<T> a, V3<T> b, V3<T> c, T
 
 template <class T> static bool finite(T x) { return !(std::isnan(x) || std::isinf(x)); }
 
+// EPA size statistics (max faces, max horizon edges, max iterations), for sizing the
+// device's shared-memory buffers.
+static std::atomic<int> g_epa_max_faces(0), g_epa_max_edges(0), g_epa_max_iters(0);
+static std::atomic<long long> g_epa_calls(0);
+static void atomic_max(std::atomic<int> &a, int v)
+{
+    int cur = a.load();
+    while (v > cur && !a.compare_exchange_weak(cur, v))
+    {
+    }
+}
+
 template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>> &S, Contact<T> &out)
 {
+    g_epa_calls.fetch_add(1);
     std::vector<Face<T>> F;
     std::vector<Edge<T>> E;
     F.reserve(64);
@@ -521,6 +534,8 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
         // (code/nans.cpp:807); the oracle reports no contact instead.
         if (F.empty())
             return false;
+        atomic_max(g_epa_max_faces, (int)F.size());
+        atomic_max(g_epa_max_iters, it);
         T cur = std::fabs(dot(F[0].n, F[0].a.P));
         size_t ci = 0;
         for (size_t i = 0; i < F.size(); ++i)
@@ -564,6 +579,7 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             }
             ++i;
         }
+        atomic_max(g_epa_max_edges, (int)E.size());
         for (size_t i = 0; i < E.size(); ++i)
             push_face(F, ns, E[i].a, E[i].b);
         E.clear();
@@ -1062,6 +1078,23 @@ void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
         w->sd[scene].k = Consts{cr, cf, iters};
     else
         w->sf[scene].k = Consts{cr, cf, iters};
+}
+
+// EPA size statistics since the last reset: out[0] max faces, [1] max edges,
+// [2] max iteration index, [3] EPA calls.
+void nanso_epa_stats(long long *out, int reset)
+{
+    out[0] = g_epa_max_faces.load();
+    out[1] = g_epa_max_edges.load();
+    out[2] = g_epa_max_iters.load();
+    out[3] = g_epa_calls.load();
+    if (reset)
+    {
+        g_epa_max_faces = 0;
+        g_epa_max_edges = 0;
+        g_epa_max_iters = 0;
+        g_epa_calls = 0;
+    }
 }
 
 // Project sincos, exported so tests can compare it with the device copy.

@@ -49,6 +49,7 @@ def lib():
         L.nanso_pairs.restype = _U
         L.nanso_set_constants.argtypes = [_P, _I, _F, _F, _I]
         L.nanso_sincosf.argtypes = [_P, _P, _P, _I]
+        L.nanso_epa_stats.argtypes = [_P, _I]
         _LIB = L
     return _LIB
 
@@ -121,3 +122,9 @@ def sincos(x):
     c = np.zeros_like(x)
     lib().nanso_sincosf(_ptr(x), _ptr(s), _ptr(c), len(x))
     return s, c
+
+
+def epa_stats(reset=True):
+    out = np.zeros(4, np.int64)
+    lib().nanso_epa_stats(_ptr(out), 1 if reset else 0)
+    return dict(max_faces=int(out[0]), max_edges=int(out[1]), max_iter=int(out[2]), calls=int(out[3]))

@@ -85,11 +85,35 @@ def load_golden(name):
     return scene, meta, [str(d) for d in z["digests"]], saved
 
 
-def aabb_margin_boxes(vertices):
-    """Inflated AABBs exactly as the device sweep computes them (float32)."""
-    v = np.asarray(vertices, np.float32)
-    lo = v.min(axis=-2)
-    hi = v.max(axis=-2)
+def _inflate(lo, hi, finite):
     mag = np.maximum(np.abs(lo), np.abs(hi)).max(axis=-1)
     m = (np.float32(1e-4) * mag + np.float32(1e-5)).astype(np.float32)
-    return lo - m[..., None], hi + m[..., None]
+    lo = (lo - m[..., None]).astype(np.float32)
+    hi = (hi + m[..., None]).astype(np.float32)
+    unbounded = ~finite | ~(mag <= np.float32(1e6))
+    lo[unbounded] = -np.inf
+    hi[unbounded] = np.inf
+    return lo, hi
+
+
+def aabb_margin_boxes(vertices):
+    """Cull boxes of hulls exactly as the device sweep computes them (float32)."""
+    v = np.asarray(vertices, np.float32)
+    finite = np.isfinite(v).all(axis=(-1, -2))
+    fv = np.where(np.isfinite(v), v, np.float32(0))
+    lo = fv.min(axis=-2)
+    hi = fv.max(axis=-2)
+    lo = np.where(np.isnan(lo), np.float32(0), lo).astype(np.float32)
+    hi = np.where(np.isnan(hi), np.float32(0), hi).astype(np.float32)
+    return _inflate(lo, hi, finite)
+
+
+def aabb_margin_spheres(position, radius):
+    p = np.asarray(position, np.float32)
+    r = np.asarray(radius, np.float32)[:, None]
+    with np.errstate(invalid="ignore", over="ignore"):
+        lo = (p - r).astype(np.float32)
+        hi = (p + r).astype(np.float32)
+        finite = np.isfinite(lo).all(axis=-1) & np.isfinite(hi).all(axis=-1)
+    return _inflate(np.where(np.isfinite(lo), lo, 0).astype(np.float32),
+                    np.where(np.isfinite(hi), hi, 0).astype(np.float32), finite)
