@@ -5,7 +5,7 @@
 // render code's Model rebuild, as six kernels:
 //   k_sweep        IntegrateVelocities(prev) + rebuild + IntegrateForces + vertices + AABB
 //   k_cull_mask / k_scan_blocks / k_cull_write   ordered candidate pairs
-//   k_narrow       GJK + EPA                      (DetectCollisions)
+//   k_narrow / k_narrow_big   GJK + EPA           (DetectCollisions)
 //   k_solve        sequential impulses by waves   (SolveConstraints)
 // The last step's IntegrateVelocities is folded into the next step's sweep, or applied by
 // nans_world_download.
@@ -346,7 +346,10 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.pair_mask, (size_t)((pair_acc + 31) / 32))) ||
         (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.n_cand, 1)) ||
         (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
-        (rc = dalloc(w, L, &d.work_counter, 2)) || (rc = dalloc(w, L, &d.status, 1)) ||
+        (rc = dalloc(w, L, &d.work_counter, 4)) || (rc = dalloc(w, L, &d.status, 1)) ||
+        (rc = dalloc(w, L, &d.ovf_cand, kEpaOverflowCap)) ||
+        (rc = dalloc(w, L, &d.ovf_simplex, (size_t)12 * kEpaOverflowCap)) ||
+        (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes() * kEpaArenaWarps)) ||
         (rc = dalloc(w, L, &w->d_rec_cube, (size_t)61 * tc)) || (rc = dalloc(w, L, &w->d_rec_sphere, (size_t)37 * ts)) ||
         (rc = dalloc(w, L, &w->d_rec_floor, (size_t)61 * S)) || (rc = dalloc(w, L, &w->d_small, 2)) ||
         (rc = dalloc(w, L, &d.s_last, 1)))
@@ -365,6 +368,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.scl = w->d_scl;
     d.prm = w->d_prm;
     d.model_in = w->d_model_in;
+    d.ovf_cap = kEpaOverflowCap;
+    d.epa_arena_warps = kEpaArenaWarps;
     cudaStream_t st = w->stream;
     CK(cudaMemcpyAsync(p_cube0, sc_cube0.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_nc, sc_nc.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -456,7 +461,7 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
 {
     cudaStream_t st = w->stream;
     DevWorld &d = w->dw;
-    CK(cudaMemsetAsync(d.work_counter, 0, 2 * sizeof(int), st));
+    CK(cudaMemsetAsync(d.work_counter, 0, 4 * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
     k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
@@ -533,7 +538,7 @@ int ensure_graph(nans_world *w, float dt, int gsteps)
     DevWorld &d = w->dw;
     for (int i = 0; i < gsteps; ++i)
     {
-        cudaMemsetAsync(d.work_counter, 0, 2 * sizeof(int), st);
+        cudaMemsetAsync(d.work_counter, 0, 4 * sizeof(int), st);
         cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st);
         cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st);
         k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, dt, dt,
@@ -926,7 +931,7 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
     DevWorld &d = w->dw;
     for (uint32_t k = 0; k < nsteps; ++k)
     {
-        CK(cudaMemsetAsync(d.work_counter, 0, 2 * sizeof(int), st));
+        CK(cudaMemsetAsync(d.work_counter, 0, 4 * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
         CK(cudaEventRecord(ev[0], st));
@@ -958,7 +963,8 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
 {
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
-    uint32_t k = 4 + (w->cull_blocks > 0 ? 2u : 0u); // sweep, scan, [mask, write], narrow, solve
+    // sweep, [mask, write], scan, narrow, narrow_big, solve
+    uint32_t k = 5 + (w->cull_blocks > 0 ? 2u : 0u);
     if (batched)
         *batched = k;
     if (plain)

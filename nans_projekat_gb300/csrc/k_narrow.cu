@@ -173,20 +173,34 @@ __device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Sha
     return G_NOHIT; // iteration cap reached while still evolving: no collision
 }
 
-struct EpaSmem
+// Polytope storage of one EPA. The vertex pool holds the GJK tetrahedron plus one support per
+// iteration; faces are an ordered list (vertex indices, normal, cached distance); edges are
+// the current horizon. FMAX / EMAX bound faces and edges.
+template <int FMAX, int EMAX> struct EpaBuf
 {
+    static constexpr int kFaces = FMAX;
+    static constexpr int kEdges = EMAX;
     float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
     float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
     float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
-    float fnx[kEpaMaxFaces], fny[kEpaMaxFaces], fnz[kEpaMaxFaces], fd[kEpaMaxFaces];
-    unsigned char fa[kEpaMaxFaces], fb[kEpaMaxFaces], fc[kEpaMaxFaces];
-    unsigned char ea[kEpaMaxEdges], eb[kEpaMaxEdges];
-    unsigned vis[(kEpaMaxFaces + 31) / 32];
+    float fnx[FMAX], fny[FMAX], fnz[FMAX], fd[FMAX];
+    unsigned char fa[FMAX], fb[FMAX], fc[FMAX];
+    unsigned char ea[EMAX], eb[EMAX];
+    unsigned vis[FMAX / 32];
+};
+using EpaFast = EpaBuf<kEpaFastFaces, kEpaFastEdges>; // shared memory, one per warp
+using EpaBig = EpaBuf<kEpaBigFaces, kEpaBigEdges>;    // global memory, one per slow-path warp
+
+enum
+{
+    EPA_NONE = 0,
+    EPA_CONTACT = 1,
+    EPA_OVERFLOW = -1
 };
 
-__device__ __forceinline__ v3 pool_p(const EpaSmem &E, int i) { return mk3(E.px[i], E.py[i], E.pz[i]); }
+template <class B> __device__ __forceinline__ v3 pool_p(const B &E, int i) { return mk3(E.px[i], E.py[i], E.pz[i]); }
 
-__device__ __forceinline__ void pool_put(EpaSmem &E, int i, const GV &g)
+template <class B> __device__ __forceinline__ void pool_put(B &E, int i, const GV &g)
 {
     E.px[i] = g.p.x;
     E.py[i] = g.p.y;
@@ -201,7 +215,7 @@ __device__ __forceinline__ void pool_put(EpaSmem &E, int i, const GV &g)
 
 // PushTriangle (code/nans.cpp:292-322): N = normalize(cross(B-A, C-A)), flipped to face away
 // from the origin; the face's distance to the origin |dot(N, A)| is cached with it.
-__device__ __forceinline__ void face_put(EpaSmem &E, int f, int a, int b, int c)
+template <class B> __device__ __forceinline__ void face_put(B &E, int f, int a, int b, int c)
 {
     v3 pa = pool_p(E, a), pb = pool_p(E, b), pc = pool_p(E, c);
     v3 n = normalize3(cross3(pb - pa, pc - pa));
@@ -216,8 +230,9 @@ __device__ __forceinline__ void face_put(EpaSmem &E, int f, int a, int b, int c)
     E.fd[f] = fabsf(dot3(n, pa));
 }
 
-// PushEdge (code/nans.cpp:232-266), warp-cooperative. Returns false on overflow.
-__device__ __forceinline__ bool push_edge(EpaSmem &E, int &ne, int u, int v, int lane)
+// PushEdge (code/nans.cpp:232-266), warp-cooperative: cancels the first stored edge that is the
+// reverse of (u, v) (vertex equality compares P), else appends. Returns false on overflow.
+template <class B> __device__ __forceinline__ bool push_edge(B &E, int &ne, int u, int v, int lane)
 {
     v3 pu = pool_p(E, u), pv = pool_p(E, v);
     int found = -1;
@@ -236,31 +251,28 @@ __device__ __forceinline__ bool push_edge(EpaSmem &E, int &ne, int u, int v, int
     }
     if (found >= 0)
     {
-        // erase: shift the tail down by one (read everything first, then write)
-        unsigned char ta[(kEpaMaxEdges + 31) / 32], tb[(kEpaMaxEdges + 31) / 32];
-#pragma unroll
-        for (int r = 0; r < (kEpaMaxEdges + 31) / 32; ++r)
+        // erase: shift the tail down by one, chunk by chunk (each chunk read before written)
+        for (int base = found + 1; base < ne; base += 32)
         {
-            int e = found + 1 + lane + 32 * r;
-            ta[r] = (e < ne) ? E.ea[e] : 0;
-            tb[r] = (e < ne) ? E.eb[e] : 0;
-        }
-        __syncwarp();
-#pragma unroll
-        for (int r = 0; r < (kEpaMaxEdges + 31) / 32; ++r)
-        {
-            int e = found + 1 + lane + 32 * r;
+            int e = base + lane;
+            unsigned char ta = 0, tb = 0;
             if (e < ne)
             {
-                E.ea[e - 1] = ta[r];
-                E.eb[e - 1] = tb[r];
+                ta = E.ea[e];
+                tb = E.eb[e];
             }
+            __syncwarp();
+            if (e < ne)
+            {
+                E.ea[e - 1] = ta;
+                E.eb[e - 1] = tb;
+            }
+            __syncwarp();
         }
-        __syncwarp();
         --ne;
         return true;
     }
-    if (ne >= kEpaMaxEdges)
+    if (ne >= B::kEdges)
         return false;
     if (lane == 0)
     {
@@ -272,9 +284,11 @@ __device__ __forceinline__ bool push_edge(EpaSmem &E, int &ne, int u, int v, int
     return true;
 }
 
-// Returns 1 with the contact written, 0 for "no contact", and sets status bits on overflow.
-__device__ int epa_warp(const DevWorld &w, EpaSmem &E, const Shape &A, const Shape &B, const GV &s0, const GV &s1,
-                        const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n, int lane)
+// ResolveCollision (code/nans.cpp:787-904) on one warp. Returns EPA_CONTACT with the contact
+// written, EPA_NONE, or EPA_OVERFLOW when the polytope outgrows B.
+template <class B>
+__device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs, const GV &s0, const GV &s1,
+                       const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n, int lane)
 {
     if (lane == 0)
     {
@@ -301,7 +315,7 @@ __device__ int epa_warp(const DevWorld &w, EpaSmem &E, const Shape &A, const Sha
         {
             if (lane == 0)
                 atomicOr(w.status, (unsigned)ST_EPA_EMPTY);
-            return 0;
+            return EPA_NONE;
         }
         // closest face: CurrentDistance starts at face 0; strict '<' keeps the first minimum
         int ci = 0;
@@ -333,7 +347,7 @@ __device__ int epa_warp(const DevWorld &w, EpaSmem &E, const Shape &A, const Sha
         }
         const float cur = E.fd[ci];
         const v3 n = mk3(E.fnx[ci], E.fny[ci], E.fnz[ci]);
-        const GV ns = minkowski_support(w.verts, A, B, n);
+        const GV ns = minkowski_support(w.verts, A, Bs, n);
         if (dot3(n, ns.p) - cur < 0.001f)
         {
             // Barycentric (code/nans.cpp:771-785) of N*dist on the closest face
@@ -348,9 +362,9 @@ __device__ int epa_warp(const DevWorld &w, EpaSmem &E, const Shape &A, const Sha
             float bw = (d00 * d21 - d01 * d20) / den;
             float bu = 1.0f - bv - bw;
             if (fabsf(bu) > 1.0f || fabsf(bv) > 1.0f || fabsf(bw) > 1.0f)
-                return 0;
+                return EPA_NONE;
             if (!isfinite(bu) || !isfinite(bv) || !isfinite(bw))
-                return 0;
+                return EPA_NONE;
             v3 saa = mk3(E.ax[ia], E.ay[ia], E.az[ia]), sab = mk3(E.ax[ib], E.ay[ib], E.az[ib]),
                sac = mk3(E.ax[ic], E.ay[ic], E.az[ic]);
             v3 sba = mk3(E.bx[ia], E.by[ia], E.bz[ia]), sbb = mk3(E.bx[ib], E.by[ib], E.bz[ib]),
@@ -358,7 +372,7 @@ __device__ int epa_warp(const DevWorld &w, EpaSmem &E, const Shape &A, const Sha
             out_pa = ((bu * saa) + (bv * sab)) + (bw * sac);
             out_n = -1.0f * n;
             out_pb = ((bu * sba) + (bv * sbb)) + (bw * sbc);
-            return 1;
+            return EPA_CONTACT;
         }
         // faces that see the new support point (code/nans.cpp:869-891)
         const int nchunks = (nf + 31) >> 5;
@@ -392,11 +406,7 @@ __device__ int epa_warp(const DevWorld &w, EpaSmem &E, const Shape &A, const Sha
             }
         }
         if (!ok)
-        {
-            if (lane == 0)
-                atomicOr(w.status, (unsigned)ST_EPA_EDGES);
-            return 0;
-        }
+            return EPA_OVERFLOW;
         // stable removal of the visible faces
         int keep = 0;
         for (int ch = 0; ch < nchunks; ++ch)
@@ -432,24 +442,20 @@ __device__ int epa_warp(const DevWorld &w, EpaSmem &E, const Shape &A, const Sha
             __syncwarp();
             keep += __popc(sm);
         }
+        if (keep + ne > B::kFaces)
+            return EPA_OVERFLOW;
         // the new support joins the vertex pool; new faces (S, e.A, e.B) in edge order
         int sv = nv;
         if (lane == 0)
             pool_put(E, sv, ns);
         ++nv;
         __syncwarp();
-        if (keep + ne > kEpaMaxFaces)
-        {
-            if (lane == 0)
-                atomicOr(w.status, (unsigned)ST_EPA_FACES);
-            return 0;
-        }
         for (int j = lane; j < ne; j += 32)
             face_put(E, keep + j, sv, E.ea[j], E.eb[j]);
         __syncwarp();
         nf = keep + ne;
     }
-    return 0;
+    return EPA_NONE;
 }
 
 __device__ __forceinline__ GV shfl_gv(const GV &g, int src)
@@ -465,13 +471,26 @@ __device__ __forceinline__ GV shfl_gv(const GV &g, int src)
 }
 
 // Persistent narrowphase: warps take 32 candidates at a time from a global queue.
-// Dynamic shared memory: one EpaSmem per warp.
+__device__ __forceinline__ void write_result(const DevWorld &w, int cc, int res, v3 pa, v3 pb, v3 nn)
+{
+    w.hit[cc] = (res == EPA_CONTACT) ? 1 : 0;
+    if (res == EPA_CONTACT)
+    {
+        w.c_pa[cc] = f4(pa, 0.0f);
+        w.c_pb[cc] = f4(pb, 0.0f);
+        w.c_n[cc] = f4(nn, 0.0f);
+    }
+}
+
+// Persistent narrowphase: warps take 32 candidates at a time from a global queue. EPAs that
+// outgrow the shared-memory buffers are queued, with their GJK simplex, for k_narrow_big.
+// Dynamic shared memory: one EpaFast per warp.
 template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_narrow(DevWorld w)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    EpaSmem *epa = reinterpret_cast<EpaSmem *>(smem_raw);
+    EpaFast *epa = reinterpret_cast<EpaFast *>(smem_raw);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    EpaSmem &E = epa[wid];
+    EpaFast &E = epa[wid];
     const int n = *w.n_cand;
     for (;;)
     {
@@ -509,24 +528,78 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_narrow(DevW
             int ga = __shfl_sync(0xffffffffu, a, src), gb = __shfl_sync(0xffffffffu, b, src);
             Shape A = load_shape(w, ga), B = load_shape(w, gb);
             v3 pa, pb, nn;
-            int ok = epa_warp(w, E, A, B, t0, t1, t2, t3, pa, pb, nn, lane);
+            int r = epa_run(w, E, A, B, t0, t1, t2, t3, pa, pb, nn, lane);
             __syncwarp();
             if (lane == 0)
             {
                 int cc = base + src;
-                w.hit[cc] = ok;
-                if (ok)
+                if (r == EPA_OVERFLOW)
                 {
-                    w.c_pa[cc] = f4(pa, 0.0f);
-                    w.c_pb[cc] = f4(pb, 0.0f);
-                    w.c_n[cc] = f4(nn, 0.0f);
+                    int q = atomicAdd(w.work_counter + 3, 1);
+                    w.hit[cc] = 0;
+                    if (q < w.ovf_cap)
+                    {
+                        w.ovf_cand[q] = cc;
+                        const GV *g[4] = {&t0, &t1, &t2, &t3};
+                        for (int k = 0; k < 4; ++k)
+                        {
+                            w.ovf_simplex[(size_t)12 * q + 3 * k] = f4(g[k]->p, 0.0f);
+                            w.ovf_simplex[(size_t)12 * q + 3 * k + 1] = f4(g[k]->sa, 0.0f);
+                            w.ovf_simplex[(size_t)12 * q + 3 * k + 2] = f4(g[k]->sb, 0.0f);
+                        }
+                    }
+                    else
+                        atomicOr(w.status, (unsigned)ST_EPA_FACES);
                 }
+                else
+                    write_result(w, cc, r, pa, pb, nn);
             }
         }
     }
 }
 
-static size_t narrow_smem(int warps) { return sizeof(EpaSmem) * (size_t)warps; }
+// Slow path: one warp per queued EPA, polytope in a per-warp global-memory arena.
+__global__ void __launch_bounds__(128) k_narrow_big(DevWorld w)
+{
+    const int lane = threadIdx.x & 31;
+    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    EpaBig &E = reinterpret_cast<EpaBig *>(w.epa_arena)[gwarp];
+    const int n = min(w.work_counter[3], w.ovf_cap);
+    for (;;)
+    {
+        int q = 0;
+        if (lane == 0)
+            q = atomicAdd(w.work_counter + 2, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= n)
+            break;
+        const int cc = w.ovf_cand[q];
+        GV t[4];
+        for (int k = 0; k < 4; ++k)
+        {
+            t[k].p = xyz(w.ovf_simplex[(size_t)12 * q + 3 * k]);
+            t[k].sa = xyz(w.ovf_simplex[(size_t)12 * q + 3 * k + 1]);
+            t[k].sb = xyz(w.ovf_simplex[(size_t)12 * q + 3 * k + 2]);
+        }
+        Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
+        v3 pa, pb, nn;
+        int r = epa_run(w, E, A, B, t[0], t[1], t[2], t[3], pa, pb, nn, lane);
+        __syncwarp();
+        if (lane == 0)
+        {
+            if (r == EPA_OVERFLOW)
+            {
+                atomicOr(w.status, (unsigned)ST_EPA_FACES);
+                r = EPA_NONE;
+            }
+            write_result(w, cc, r, pa, pb, nn);
+        }
+    }
+}
+
+size_t epa_big_bytes() { return sizeof(EpaBig); }
+
+static size_t narrow_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }
 
 static void narrow_attrs()
 {
@@ -556,6 +629,7 @@ void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
         k_narrow<8><<<grid, 256, narrow_smem(8), st>>>(w);
     else
         k_narrow<4><<<grid, 128, narrow_smem(4), st>>>(w);
+    k_narrow_big<<<w.epa_arena_warps / 4, 128, 0, st>>>(w);
 }
 
 } // namespace nans

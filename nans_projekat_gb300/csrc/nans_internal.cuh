@@ -79,7 +79,13 @@ struct DevWorld
     // narrowphase output, per candidate
     int *hit;
     float4 *c_pa, *c_pb, *c_n;
-    int *work_counter;                  // persistent-kernel work queue heads
+    int *work_counter;                  // [0] narrowphase, [1] solver, [2] slow EPA queue heads,
+                                        // [3] slow EPA queue length
+    int ovf_cap;                        // slow EPA queue capacity
+    int *ovf_cand;                      // queued candidate index
+    float4 *ovf_simplex;                // queued GJK simplex: 4 x (P, SupA, SupB)
+    unsigned char *epa_arena;           // slow-path polytope buffers, one per warp
+    int epa_arena_warps;
     // solver scratch, per candidate slot
     int *s_order, *s_wave, *s_perm, *s_wcnt;
     float4 *s_k;                        // 9 float4 of per-contact constants

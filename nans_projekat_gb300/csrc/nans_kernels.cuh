@@ -18,15 +18,21 @@ constexpr int kCullThreads = 256;
 constexpr int kPairsPerThread = 32;
 constexpr int kPairsPerBlock = kCullThreads * kPairsPerThread;
 
-// EPA shared-memory capacities per warp. Vertices: the GJK tetrahedron plus one support per
-// EPA iteration (at most 65, code/nans.cpp:804). Faces grow by two per iteration on a convex
-// polytope, but the reference's polytope is not always convex (supports can repeat a vertex,
-// visible sets can be non-manifold) and runs of all 65 iterations are common; measured on the
-// 16,384-scene workload the face list reached ~200 and the horizon ~10 edges. The buffers hold
-// 512 faces and 128 edges and report overflow (NANS_ERR_EPA_CAPACITY) instead of dropping data.
+// EPA capacities. Vertices: the GJK tetrahedron plus one support per EPA iteration (at most
+// 65, code/nans.cpp:804). Faces grow by two per iteration on a convex polytope, but the
+// reference's polytope is not always convex (supports can repeat a vertex and visible sets
+// can be non-manifold), so its face list can grow much faster: on the 16,384-scene stack
+// workload ~4 EPAs in a million exceed 128 faces and the largest seen held 12,494 faces and
+// 4,104 horizon edges. The fast path keeps 128 faces / 32 edges per warp in shared memory;
+// an EPA that outgrows it is rerun by k_narrow_big with 32,768 faces / 16,384 edges per warp
+// in global memory. Beyond that the step reports NANS_ERR_EPA_CAPACITY.
 constexpr int kEpaMaxVerts = 72;
-constexpr int kEpaMaxFaces = 512;
-constexpr int kEpaMaxEdges = 128;
+constexpr int kEpaFastFaces = 128;
+constexpr int kEpaFastEdges = 32;
+constexpr int kEpaBigFaces = 32768;
+constexpr int kEpaBigEdges = 16384;
+constexpr int kEpaArenaWarps = 256;   // slow-path warps (each with its own arena)
+constexpr int kEpaOverflowCap = 65536; // queued EPAs per step
 
 __global__ void k_sweep(DevWorld w, float pending_dt, float dt, int flags);
 __global__ void k_unpack(DevWorld w, const float *rec_cube, const float *rec_sphere, const float *rec_floor,
@@ -41,6 +47,7 @@ __global__ void k_scan_blocks(DevWorld w, int nblocks);
 __global__ void k_cull_write(DevWorld w);
 
 int narrow_blocks_per_sm(int warps);
+size_t epa_big_bytes();
 void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w);
 __global__ void k_solve(DevWorld w, float dt);
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);

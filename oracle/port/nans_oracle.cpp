@@ -510,6 +510,7 @@ template <class T> static bool finite(T x) { return !(std::isnan(x) || std::isin
 // device's shared-memory buffers.
 static std::atomic<int> g_epa_max_faces(0), g_epa_max_edges(0), g_epa_max_iters(0);
 static std::atomic<long long> g_epa_calls(0);
+static std::atomic<long long> g_epa_big[4]; // EPAs whose face list exceeded 128, 256, 1024, 4096
 static void atomic_max(std::atomic<int> &a, int v)
 {
     int cur = a.load();
@@ -521,6 +522,17 @@ static void atomic_max(std::atomic<int> &a, int v)
 template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>> &S, Contact<T> &out)
 {
     g_epa_calls.fetch_add(1);
+    struct BigCount
+    {
+        size_t peak = 0;
+        ~BigCount()
+        {
+            if (peak > 128) g_epa_big[0].fetch_add(1);
+            if (peak > 256) g_epa_big[1].fetch_add(1);
+            if (peak > 1024) g_epa_big[2].fetch_add(1);
+            if (peak > 4096) g_epa_big[3].fetch_add(1);
+        }
+    } big;
     std::vector<Face<T>> F;
     std::vector<Edge<T>> E;
     F.reserve(64);
@@ -535,6 +547,7 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
         if (F.empty())
             return false;
         atomic_max(g_epa_max_faces, (int)F.size());
+        big.peak = std::max(big.peak, F.size());
         atomic_max(g_epa_max_iters, it);
         T cur = std::fabs(dot(F[0].n, F[0].a.P));
         size_t ci = 0;
@@ -1081,15 +1094,20 @@ void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
 }
 
 // EPA size statistics since the last reset: out[0] max faces, [1] max edges,
-// [2] max iteration index, [3] EPA calls.
+// [2] max iteration index, [3] EPA calls, [4..7] EPAs whose face list exceeded
+// 128, 256, 1024, 4096 faces.
 void nanso_epa_stats(long long *out, int reset)
 {
     out[0] = g_epa_max_faces.load();
     out[1] = g_epa_max_edges.load();
     out[2] = g_epa_max_iters.load();
     out[3] = g_epa_calls.load();
+    for (int i = 0; i < 4; ++i)
+        out[4 + i] = g_epa_big[i].load();
     if (reset)
     {
+        for (int i = 0; i < 4; ++i)
+            g_epa_big[i] = 0;
         g_epa_max_faces = 0;
         g_epa_max_edges = 0;
         g_epa_max_iters = 0;
