@@ -392,6 +392,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         CK(cudaMemcpyAsync(w->d_rec_sphere, spheres, ts * sizeof(nans_sphere), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(w->d_rec_floor, floors, S * sizeof(nans_cube), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
+    CK(cudaMemsetAsync(d.epa_arena, 0, epa_big_bytes() * kEpaArenaWarps, st));
     CK(cudaMemsetAsync(d.n_cand, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, S * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, S * sizeof(int), st));

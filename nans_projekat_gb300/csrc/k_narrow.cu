@@ -176,10 +176,22 @@ __device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Sha
 // Polytope storage of one EPA. The vertex pool holds the GJK tetrahedron plus one support per
 // iteration; faces are an ordered list (vertex indices, normal, cached distance); edges are
 // the current horizon. FMAX / EMAX bound faces and edges.
-template <int FMAX, int EMAX> struct EpaBuf
+template <int FMAX, int EMAX, bool HASH> struct EpaBuf;
+
+// Slot of the horizon hash table: FIFO (head, tail) of live edges whose directed key is
+// (canonical P of the first vertex, canonical P of the second); valid while gen matches.
+struct HSlot
+{
+    unsigned key[6];
+    int head, tail;
+    unsigned gen;
+};
+
+template <int FMAX, int EMAX> struct EpaBuf<FMAX, EMAX, false>
 {
     static constexpr int kFaces = FMAX;
     static constexpr int kEdges = EMAX;
+    static constexpr bool kHash = false;
     float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
     float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
     float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
@@ -188,8 +200,28 @@ template <int FMAX, int EMAX> struct EpaBuf
     unsigned char ea[EMAX], eb[EMAX];
     unsigned vis[FMAX / 32];
 };
-using EpaFast = EpaBuf<kEpaFastFaces, kEpaFastEdges>; // shared memory, one per warp
-using EpaBig = EpaBuf<kEpaBigFaces, kEpaBigEdges>;    // global memory, one per slow-path warp
+
+template <int FMAX, int EMAX> struct EpaBuf<FMAX, EMAX, true>
+{
+    static constexpr int kFaces = FMAX;
+    static constexpr int kEdges = EMAX;
+    static constexpr bool kHash = true;
+    static constexpr int kSlots = 2 * EMAX; // load factor <= 1/2
+    float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
+    float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
+    float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
+    float fnx[FMAX], fny[FMAX], fnz[FMAX], fd[FMAX];
+    unsigned char fa[FMAX], fb[FMAX], fc[FMAX];
+    unsigned char ea[EMAX], eb[EMAX];
+    unsigned vis[FMAX / 32];
+    int enext[EMAX];
+    unsigned char ealive[EMAX];
+    unsigned gen;
+    HSlot slot[kSlots];
+};
+
+using EpaFast = EpaBuf<kEpaFastFaces, kEpaFastEdges, false>; // shared memory, one per warp
+using EpaBig = EpaBuf<kEpaBigFaces, kEpaBigEdges, true>;     // global memory, one per slow-path warp
 
 enum
 {
@@ -284,6 +316,116 @@ template <class B> __device__ __forceinline__ bool push_edge(B &E, int &ne, int 
     return true;
 }
 
+// Canonical bits of a coordinate for vertex equality: -0 and +0 compare equal.
+__device__ __forceinline__ unsigned canon_bits(float x)
+{
+    unsigned b = __float_as_uint(x);
+    return (b == 0x80000000u) ? 0u : b;
+}
+
+// Horizon for large polytopes, run by one lane: the same result as PushEdge in push order
+// (each push cancels the first live stored edge that is its reverse, else is appended), in
+// O(1) per push. Live edges with equal directed keys form FIFO queues, so "first live reverse
+// edge" is the head of the reverse key's queue. A vertex with a NaN coordinate equals nothing,
+// so its edges are appended without a key.
+template <class B> __device__ int horizon_hash(B &E, int nchunks)
+{
+    E.gen = E.gen + 1u;
+    const unsigned gen = E.gen;
+    int ne = 0;
+    for (int ch = 0; ch < nchunks; ++ch)
+    {
+        unsigned m = E.vis[ch];
+        while (m)
+        {
+            int f = ch * 32 + __ffs(m) - 1;
+            m &= m - 1;
+            int vv[4] = {E.fa[f], E.fb[f], E.fc[f], E.fa[f]};
+            for (int k = 0; k < 3; ++k)
+            {
+                int u = vv[k], v = vv[k + 1];
+                v3 pu = pool_p(E, u), pv = pool_p(E, v);
+                bool nan = isnan(pu.x) || isnan(pu.y) || isnan(pu.z) || isnan(pv.x) || isnan(pv.y) || isnan(pv.z);
+                unsigned ku[3] = {canon_bits(pu.x), canon_bits(pu.y), canon_bits(pu.z)};
+                unsigned kv[3] = {canon_bits(pv.x), canon_bits(pv.y), canon_bits(pv.z)};
+                if (!nan)
+                {
+                    // look up the reverse key (v, u)
+                    unsigned h = 2166136261u;
+                    for (int q = 0; q < 3; ++q)
+                        h = (h ^ kv[q]) * 16777619u;
+                    for (int q = 0; q < 3; ++q)
+                        h = (h ^ ku[q]) * 16777619u;
+                    int found = -1;
+                    for (int probe = 0; probe < B::kSlots; ++probe)
+                    {
+                        HSlot &sl = E.slot[(h + probe) & (B::kSlots - 1)];
+                        if (sl.gen != gen)
+                            break;
+                        if (sl.key[0] == kv[0] && sl.key[1] == kv[1] && sl.key[2] == kv[2] && sl.key[3] == ku[0] &&
+                            sl.key[4] == ku[1] && sl.key[5] == ku[2])
+                        {
+                            found = (int)((h + probe) & (B::kSlots - 1));
+                            break;
+                        }
+                    }
+                    if (found >= 0 && E.slot[found].head >= 0)
+                    {
+                        HSlot &sl = E.slot[found];
+                        int e = sl.head;
+                        E.ealive[e] = 0;
+                        sl.head = E.enext[e];
+                        if (sl.head < 0)
+                            sl.tail = -1;
+                        continue;
+                    }
+                }
+                if (ne >= B::kEdges)
+                    return -1;
+                int e = ne++;
+                E.ea[e] = (unsigned char)u;
+                E.eb[e] = (unsigned char)v;
+                E.ealive[e] = 1;
+                E.enext[e] = -1;
+                if (nan)
+                    continue;
+                unsigned h = 2166136261u;
+                for (int q = 0; q < 3; ++q)
+                    h = (h ^ ku[q]) * 16777619u;
+                for (int q = 0; q < 3; ++q)
+                    h = (h ^ kv[q]) * 16777619u;
+                for (int probe = 0; probe < B::kSlots; ++probe)
+                {
+                    HSlot &sl = E.slot[(h + probe) & (B::kSlots - 1)];
+                    if (sl.gen != gen)
+                    {
+                        sl.gen = gen;
+                        sl.key[0] = ku[0];
+                        sl.key[1] = ku[1];
+                        sl.key[2] = ku[2];
+                        sl.key[3] = kv[0];
+                        sl.key[4] = kv[1];
+                        sl.key[5] = kv[2];
+                        sl.head = sl.tail = e;
+                        break;
+                    }
+                    if (sl.key[0] == ku[0] && sl.key[1] == ku[1] && sl.key[2] == ku[2] && sl.key[3] == kv[0] &&
+                        sl.key[4] == kv[1] && sl.key[5] == kv[2])
+                    {
+                        if (sl.tail >= 0)
+                            E.enext[sl.tail] = e;
+                        else
+                            sl.head = e;
+                        sl.tail = e;
+                        break;
+                    }
+                }
+            }
+        }
+    }
+    return ne;
+}
+
 // ResolveCollision (code/nans.cpp:787-904) on one warp. Returns EPA_CONTACT with the contact
 // written, EPA_NONE, or EPA_OVERFLOW when the polytope outgrows B.
 template <class B>
@@ -309,18 +451,18 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         face_put(E, 3, 1, 3, 2);
     __syncwarp();
     int nf = 4, nv = 4;
+    // When every face is removed and the horizon cancels out, the reference reads Triangle[0]
+    // of the empty vector (code/nans.cpp:807, 824); with libstdc++ that slot still holds the
+    // face erased last, the last face of the list before removal. It is kept at index 0.
+    bool stale = false;
     for (int it = 0; it <= 64; ++it)
     {
-        if (nf == 0)
-        {
-            if (lane == 0)
-                atomicOr(w.status, (unsigned)ST_EPA_EMPTY);
+        if (nf == 0 && !stale)
             return EPA_NONE;
-        }
         // closest face: CurrentDistance starts at face 0; strict '<' keeps the first minimum
         int ci = 0;
         float d0 = E.fd[0];
-        if (!isnan(d0))
+        if (nf > 0 && !isnan(d0))
         {
             float bd = d0;
             int bi = 0;
@@ -374,6 +516,8 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
             out_pb = ((bu * sba) + (bv * sbb)) + (bw * sbc);
             return EPA_CONTACT;
         }
+        if (nf == 0)
+            return EPA_NONE; // the stale read repeats identically until the iteration cap
         // faces that see the new support point (code/nans.cpp:869-891)
         const int nchunks = (nf + 31) >> 5;
         for (int ch = 0; ch < nchunks; ++ch)
@@ -393,20 +537,57 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         __syncwarp();
         // horizon edges in face order
         int ne = 0;
-        bool ok = true;
-        for (int ch = 0; ch < nchunks && ok; ++ch)
+        if constexpr (B::kHash)
         {
-            unsigned m = E.vis[ch];
-            while (m && ok)
+            if (lane == 0)
+                ne = horizon_hash(E, nchunks);
+            ne = __shfl_sync(0xffffffffu, ne, 0);
+            __syncwarp();
+            if (ne < 0)
+                return EPA_OVERFLOW;
+            // keep the live edges in push order
+            int live = 0;
+            for (int base = 0; base < ne; base += 32)
             {
-                int f = ch * 32 + __ffs(m) - 1;
-                m &= m - 1;
-                int a = E.fa[f], b = E.fb[f], c = E.fc[f];
-                ok = push_edge(E, ne, a, b, lane) && push_edge(E, ne, b, c, lane) && push_edge(E, ne, c, a, lane);
+                int e = base + lane;
+                bool al = (e < ne) && E.ealive[e];
+                unsigned bal = __ballot_sync(0xffffffffu, al);
+                int dst = live + __popc(bal & ((1u << lane) - 1u));
+                unsigned char ta = 0, tb = 0;
+                if (al)
+                {
+                    ta = E.ea[e];
+                    tb = E.eb[e];
+                }
+                __syncwarp();
+                if (al)
+                {
+                    E.ea[dst] = ta;
+                    E.eb[dst] = tb;
+                }
+                __syncwarp();
+                live += __popc(bal);
             }
+            ne = live;
         }
-        if (!ok)
-            return EPA_OVERFLOW;
+        else
+        {
+            bool ok = true;
+            for (int ch = 0; ch < nchunks && ok; ++ch)
+            {
+                unsigned m = E.vis[ch];
+                while (m && ok)
+                {
+                    int f = ch * 32 + __ffs(m) - 1;
+                    m &= m - 1;
+                    int a = E.fa[f], b = E.fb[f], c = E.fc[f];
+                    ok = push_edge(E, ne, a, b, lane) && push_edge(E, ne, b, c, lane) &&
+                         push_edge(E, ne, c, a, lane);
+                }
+            }
+            if (!ok)
+                return EPA_OVERFLOW;
+        }
         // stable removal of the visible faces
         int keep = 0;
         for (int ch = 0; ch < nchunks; ++ch)
@@ -444,6 +625,24 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         }
         if (keep + ne > B::kFaces)
             return EPA_OVERFLOW;
+        if (keep == 0 && ne == 0)
+        {
+            // every face removed: slot 0 keeps the last face of the list (still intact, the
+            // compaction wrote nothing)
+            if (lane == 0)
+            {
+                int l = nf - 1;
+                E.fa[0] = E.fa[l];
+                E.fb[0] = E.fb[l];
+                E.fc[0] = E.fc[l];
+                E.fnx[0] = E.fnx[l];
+                E.fny[0] = E.fny[l];
+                E.fnz[0] = E.fnz[l];
+                E.fd[0] = E.fd[l];
+            }
+            __syncwarp();
+            stale = true;
+        }
         // the new support joins the vertex pool; new faces (S, e.A, e.B) in edge order
         int sv = nv;
         if (lane == 0)

@@ -19,6 +19,9 @@
 #include <thread>
 #include <atomic>
 #include <algorithm>
+#include <string>
+#include <cstdio>
+#include <cstdlib>
 
 #include "nans_trig.h"  // the project sincos (oracle/shim/glm/nans_trig.h)
 
@@ -511,6 +514,8 @@ template <class T> static bool finite(T x) { return !(std::isnan(x) || std::isin
 static std::atomic<int> g_epa_max_faces(0), g_epa_max_edges(0), g_epa_max_iters(0);
 static std::atomic<long long> g_epa_calls(0);
 static std::atomic<long long> g_epa_big[4]; // EPAs whose face list exceeded 128, 256, 1024, 4096
+static std::atomic<long long> g_epa_big_nan0(0); // of those above 128: face 0 had a NaN distance
+static std::atomic<long long> g_epa_stale(0);     // EPAs that read the emptied face list
 static void atomic_max(std::atomic<int> &a, int v)
 {
     int cur = a.load();
@@ -540,13 +545,40 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
     push_face(F, S[0], S[2], S[3]);
     push_face(F, S[0], S[3], S[1]);
     push_face(F, S[1], S[3], S[2]);
+#ifdef NANS_EPA_TRACE
+    std::vector<std::string> trace;
+#endif
+    // When every face was removed and the horizon cancelled out, the reference reads
+    // Triangle[0] of an empty vector (code/nans.cpp:807, 824). With libstdc++ that slot
+    // still holds the face erased last (erase shifts trivially copyable elements down and
+    // leaves the old slot contents), which is the last face of the list before removal.
+    // `stale` models exactly that read.
+    bool has_stale = false;
+    Face<T> stale{};
     for (int it = 0; it <= 64; ++it)
     {
-        // An empty face list would make the reference read a destroyed element
-        // (code/nans.cpp:807); the oracle reports no contact instead.
         if (F.empty())
-            return false;
+        {
+            if (!has_stale)
+                return false;
+            T cur = std::fabs(dot(stale.n, stale.a.P));
+            Vx<T> ns = support(p, stale.n);
+            if (!(dot(stale.n, ns.P) - cur < K<T>::epa_tol()))
+                return false; // every remaining iteration repeats this one
+            T u, v, w;
+            barycentric(mul(cur, stale.n), stale.a.P, stale.b.P, stale.c.P, &u, &v, &w);
+            if (std::fabs(u) > T(1) || std::fabs(v) > T(1) || std::fabs(w) > T(1))
+                return false;
+            if (!finite(u) || !finite(v) || !finite(w))
+                return false;
+            out.pa = add(add(mul(u, stale.a.SupA), mul(v, stale.b.SupA)), mul(w, stale.c.SupA));
+            out.n = mul(T(-1), stale.n);
+            out.pb = add(add(mul(u, stale.a.SupB), mul(v, stale.b.SupB)), mul(w, stale.c.SupB));
+            return true;
+        }
         atomic_max(g_epa_max_faces, (int)F.size());
+        if (F.size() > 128 && big.peak <= 128 && std::isnan(std::fabs(dot(F[0].n, F[0].a.P))))
+            g_epa_big_nan0.fetch_add(1);
         big.peak = std::max(big.peak, F.size());
         atomic_max(g_epa_max_iters, it);
         T cur = std::fabs(dot(F[0].n, F[0].a.P));
@@ -563,6 +595,35 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
         }
         Face<T> cf = F[ci];
         Vx<T> ns = support(p, cf.n);
+#ifdef NANS_EPA_TRACE
+        {
+            int nanf = 0, vis = 0, dup = 0;
+            for (auto &f : F)
+            {
+                if (std::isnan(std::fabs(dot(f.n, f.a.P))))
+                    ++nanf;
+                if (dot(f.n, sub(ns.P, f.a.P)) > T(0))
+                    ++vis;
+            }
+            for (auto &f : F)
+                if (eq(f.a.P, ns.P) || eq(f.b.P, ns.P) || eq(f.c.P, ns.P))
+                {
+                    dup = 1;
+                    break;
+                }
+            char buf[256];
+            snprintf(buf, sizeof(buf), "it %d faces %zu nan %d visible %d closest %zu cur %.9g gap %.9g dupS %d",
+                     it, F.size(), nanf, vis, ci, (double)cur, (double)(dot(cf.n, ns.P) - cur), dup);
+            trace.push_back(buf);
+            if (F.size() > 600)
+            {
+                for (auto &l : trace)
+                    fprintf(stderr, "%s\n", l.c_str());
+                fprintf(stderr, "----\n");
+                abort();
+            }
+        }
+#endif
         if (dot(cf.n, ns.P) - cur < K<T>::epa_tol())
         {
             T u, v, w;
@@ -576,6 +637,7 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             out.pb = add(add(mul(u, cf.a.SupB), mul(v, cf.b.SupB)), mul(w, cf.c.SupB));
             return true;
         }
+        const Face<T> last_face = F.back();
         for (size_t i = 0; i < F.size();)
         {
             V3<T> tmp = sub(ns.P, F[i].a.P);
@@ -593,6 +655,12 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             ++i;
         }
         atomic_max(g_epa_max_edges, (int)E.size());
+        if (F.empty() && E.empty())
+        {
+            g_epa_stale.fetch_add(1);
+            has_stale = true;
+            stale = last_face;
+        }
         for (size_t i = 0; i < E.size(); ++i)
             push_face(F, ns, E[i].a, E[i].b);
         E.clear();
@@ -1095,7 +1163,8 @@ void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
 
 // EPA size statistics since the last reset: out[0] max faces, [1] max edges,
 // [2] max iteration index, [3] EPA calls, [4..7] EPAs whose face list exceeded
-// 128, 256, 1024, 4096 faces.
+// 128, 256, 1024, 4096 faces, [8] of those above 128 with a NaN face 0, [9] EPAs whose
+// face list emptied.
 void nanso_epa_stats(long long *out, int reset)
 {
     out[0] = g_epa_max_faces.load();
@@ -1104,8 +1173,12 @@ void nanso_epa_stats(long long *out, int reset)
     out[3] = g_epa_calls.load();
     for (int i = 0; i < 4; ++i)
         out[4 + i] = g_epa_big[i].load();
+    out[8] = g_epa_big_nan0.load();
+    out[9] = g_epa_stale.load();
     if (reset)
     {
+        g_epa_stale = 0;
+        g_epa_big_nan0 = 0;
         for (int i = 0; i < 4; ++i)
             g_epa_big[i] = 0;
         g_epa_max_faces = 0;

@@ -89,6 +89,14 @@ def main():
               {1, 100}, "refbig")
     run_world("random_dense16", scenes.random_scene(6, n_boxes=12, n_spheres=4, extent=3.0), 200,
               {1, 200}, "ref16")
+    # Scenes of the 16,384-scene stack workload (seed 2) that hit the reference's rare EPA paths:
+    # an EPA that empties its face list (scenes 6663, 5642) and EPAs whose face list outgrows
+    # 128 faces (scenes 3029, 7755, 6880).
+    batch = scenes.stack_batch(16384, seed=2)
+    for idx in (6663, 5642):
+        run_world("stack_emptied_%d" % idx, batch[idx], 20, {20}, "refbig")
+    for idx in (3029, 7755, 6880):
+        run_world("stack_bigepa_%d" % idx, batch[idx], 30, {30}, "refbig")
 
 
 if __name__ == "__main__":
