@@ -293,6 +293,7 @@ def run_ours(args):
     total_bodies = sum_over_ranks(dist, float(bodies), device)
     value = total_bodies * args.steps / (ms_max / 1000.0)
     n_cand, n_contacts = w.counts()
+    epa = w.epa_stats()
 
     # per-stage device time from a live event-timed pass over the same world
     prof_steps = 10
@@ -346,6 +347,8 @@ def run_ours(args):
                 "l2": "working set larger than L2 (%.0f MB of state, vertices and candidates)"
                       % ((bodies * 64 + n_boxes * 96 + n_cand * 60) / 1e6),
                 "candidates_per_step": n_cand, "contacts_per_step": n_contacts,
+                "large_epa": {"slow_path_epas": epa["slow_epas"], "max_faces": epa["max_faces"],
+                              "max_horizon_edges": epa["max_edges"], "beyond_capacity": epa["overflows"]},
             },
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": None,

@@ -97,7 +97,7 @@ typedef struct nans_contact_pair
 #define NANS_ERR_CAPACITY 2         /* more candidate pairs than the world's capacity */
 #define NANS_ERR_NAN_INPUT 3        /* non-finite or non-positive mass / MOI / size input */
 #define NANS_ERR_CUDA 4             /* a CUDA runtime call failed (see nans_last_error) */
-#define NANS_ERR_EPA_CAPACITY 5     /* an EPA polytope outgrew its shared-memory buffers */
+#define NANS_ERR_EPA_CAPACITY 5     /* an EPA polytope outgrew its buffers (strict worlds) */
 #define NANS_ERR_NOT_UPLOADED 6     /* the world holds no scene yet */
 #define NANS_ERR_SCENE_TOO_LARGE 7  /* a scene has more bodies than the solver supports */
 
@@ -111,6 +111,11 @@ typedef struct nans_contact_pair
 /* World flags */
 #define NANS_WORLD_ALL_PAIRS 1u    /* run GJK on every pair (the reference's all-pairs
                                       loop); default: conservative AABB cull first */
+#define NANS_WORLD_STRICT_EPA 2u   /* an EPA polytope beyond the large-polytope buffers
+                                      (2,097,152 faces) fails the step with
+                                      NANS_ERR_EPA_CAPACITY; default: that pair gets no
+                                      contact (the reference's result for every EPA that does
+                                      not converge) and the event is counted */
 
 typedef struct nans_world_desc
 {
@@ -179,6 +184,12 @@ int nans_world_status(nans_world *world, uint32_t *status_bits);
 
 /* Counts of the last step: candidate pairs after the cull and contacts. */
 int nans_world_counts(nans_world *world, uint32_t *candidates, uint32_t *contacts);
+
+/* Large-polytope EPA statistics since upload (or the last reset): out[0] largest face list
+ * and out[1] largest horizon seen by the large-polytope path, out[2] EPAs that took that path,
+ * out[3] candidate index + 1 and out[4] scene + 1 of the last EPA that outgrew it (0 if none),
+ * out[5] EPAs that outgrew it. out holds 6 entries. */
+int nans_world_epa_stats(nans_world *world, uint32_t *out, int reset);
 
 /* The world's CUDA stream (a cudaStream_t), for event timing by the caller. */
 void *nans_world_stream(nans_world *world);

@@ -349,7 +349,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.work_counter, 4)) || (rc = dalloc(w, L, &d.status, 1)) ||
         (rc = dalloc(w, L, &d.ovf_cand, kEpaOverflowCap)) ||
         (rc = dalloc(w, L, &d.ovf_simplex, (size_t)12 * kEpaOverflowCap)) ||
-        (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes() * kEpaArenaWarps)) ||
+        (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes() * (size_t)kEpaArenaWarps)) ||
+        (rc = dalloc(w, L, &d.epa_stats, 8)) ||
         (rc = dalloc(w, L, &w->d_rec_cube, (size_t)61 * tc)) || (rc = dalloc(w, L, &w->d_rec_sphere, (size_t)37 * ts)) ||
         (rc = dalloc(w, L, &w->d_rec_floor, (size_t)61 * S)) || (rc = dalloc(w, L, &w->d_small, 2)) ||
         (rc = dalloc(w, L, &d.s_last, 1)))
@@ -392,7 +393,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         CK(cudaMemcpyAsync(w->d_rec_sphere, spheres, ts * sizeof(nans_sphere), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(w->d_rec_floor, floors, S * sizeof(nans_cube), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
-    CK(cudaMemsetAsync(d.epa_arena, 0, epa_big_bytes() * kEpaArenaWarps, st));
+    CK(cudaMemsetAsync(d.epa_arena, 0, epa_big_bytes() * (size_t)kEpaArenaWarps, st));
+    CK(cudaMemsetAsync(d.epa_stats, 0, 8 * sizeof(unsigned), st));
     CK(cudaMemsetAsync(d.n_cand, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, S * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, S * sizeof(int), st));
@@ -508,8 +510,8 @@ int check_status(nans_world *w)
     CK(cudaStreamSynchronize(w->stream));
     if (status & ST_CANDIDATES)
         return fail(NANS_ERR_CAPACITY, "step: more candidate pairs than the world's capacity");
-    if (status & (ST_EPA_FACES | ST_EPA_EDGES))
-        return fail(NANS_ERR_EPA_CAPACITY, "step: an EPA polytope outgrew its shared-memory buffers");
+    if ((status & (ST_EPA_FACES | ST_EPA_EDGES)) && (w->flags & NANS_WORLD_STRICT_EPA))
+        return fail(NANS_ERR_EPA_CAPACITY, "step: an EPA polytope outgrew the large-polytope buffers");
     return NANS_OK;
 }
 
@@ -891,6 +893,20 @@ int nans_world_counts(nans_world *w, uint32_t *candidates, uint32_t *contacts)
 }
 
 void *nans_world_stream(nans_world *w) { return w ? (void *)w->stream : nullptr; }
+
+int nans_world_epa_stats(nans_world *w, uint32_t *out, int reset)
+{
+    if (!w || !out)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "epa_stats: null argument");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "epa_stats: no scene uploaded");
+    CK(cudaSetDevice(w->device));
+    CK(cudaMemcpyAsync(out, w->dw.epa_stats, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    if (reset)
+        CK(cudaMemsetAsync(w->dw.epa_stats, 0, 8 * sizeof(unsigned), w->stream));
+    CK(cudaStreamSynchronize(w->stream));
+    return NANS_OK;
+}
 
 int nans_device_sincos(const float *x, float *s, float *c, uint32_t n)
 {

@@ -623,6 +623,14 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
             __syncwarp();
             keep += __popc(sm);
         }
+        if constexpr (B::kHash)
+        {
+            if (lane == 0)
+            {
+                atomicMax(w.epa_stats + 0, (unsigned)(keep + ne));
+                atomicMax(w.epa_stats + 1, (unsigned)ne);
+            }
+        }
         if (keep + ne > B::kFaces)
             return EPA_OVERFLOW;
         if (keep == 0 && ne == 0)
@@ -762,7 +770,7 @@ __global__ void __launch_bounds__(128) k_narrow_big(DevWorld w)
 {
     const int lane = threadIdx.x & 31;
     const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    EpaBig &E = reinterpret_cast<EpaBig *>(w.epa_arena)[gwarp];
+    EpaBig &E = *reinterpret_cast<EpaBig *>(w.epa_arena + (size_t)gwarp * sizeof(EpaBig));
     const int n = min(w.work_counter[3], w.ovf_cap);
     for (;;)
     {
@@ -786,9 +794,15 @@ __global__ void __launch_bounds__(128) k_narrow_big(DevWorld w)
         __syncwarp();
         if (lane == 0)
         {
+            atomicAdd(w.epa_stats + 2, 1u);
             if (r == EPA_OVERFLOW)
             {
+                // Beyond the arena the pair gets no contact, which is what the reference
+                // returns for every EPA that does not converge within its 65 iterations.
                 atomicOr(w.status, (unsigned)ST_EPA_FACES);
+                atomicAdd(w.epa_stats + 5, 1u);
+                w.epa_stats[3] = (unsigned)cc + 1u;
+                w.epa_stats[4] = (unsigned)(w.cand_meta[cc] >> 3) + 1u;
                 r = EPA_NONE;
             }
             write_result(w, cc, r, pa, pb, nn);

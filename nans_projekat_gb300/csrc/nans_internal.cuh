@@ -38,7 +38,7 @@ enum PairType
 // device status bits (or'ed into DevWorld::status)
 enum StatusBits
 {
-    ST_EPA_FACES = 1u << 0,      // EPA face buffer full
+    ST_EPA_FACES = 1u << 0,      // an EPA outgrew the large-polytope buffers (pair: no contact)
     ST_EPA_EDGES = 1u << 1,      // EPA horizon edge buffer full
     ST_CANDIDATES = 1u << 2,     // candidate capacity exceeded
     ST_EPA_EMPTY = 1u << 3,      // EPA face list emptied (reference would read a stale face)
@@ -86,6 +86,9 @@ struct DevWorld
     float4 *ovf_simplex;                // queued GJK simplex: 4 x (P, SupA, SupB)
     unsigned char *epa_arena;           // slow-path polytope buffers, one per warp
     int epa_arena_warps;
+    unsigned *epa_stats;                // [0] max faces, [1] max horizon edges, [2] slow-path EPAs,
+                                        // [3] overflowing candidate + 1, [4] its scene + 1,
+                                        // [5] EPAs that outgrew the slow path
     // solver scratch, per candidate slot
     int *s_order, *s_wave, *s_perm, *s_wcnt;
     float4 *s_k;                        // 9 float4 of per-contact constants

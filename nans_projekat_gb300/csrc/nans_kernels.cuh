@@ -22,18 +22,19 @@ constexpr int kPairsPerBlock = kCullThreads * kPairsPerThread;
 // 65, code/nans.cpp:804). Faces grow by two per iteration on a convex polytope, but the
 // reference's polytope is not always convex: with bodies flung to large coordinates the
 // supports repeat existing vertices, faces degenerate (NaN normals, never removed) and the
-// list keeps growing for all 65 iterations. On the 16,384-scene stack workload ~4 EPAs in a
-// million exceed 128 faces and the largest seen in 130 steps held 12,494 faces and 4,104
-// horizon edges. The fast path keeps 128 faces / 32 edges per warp in shared memory; an EPA
-// that outgrows it is rerun by k_narrow_big in a per-warp global-memory arena with 262,144
-// faces, 65,536 edges and an O(1)-per-push horizon. Beyond that the step reports
-// NANS_ERR_EPA_CAPACITY.
+// list keeps growing, at times geometrically, for all 65 iterations. On the 16,384-scene
+// stack workload ~4 EPAs in a million exceed 128 faces; the largest met so far (scene 10198,
+// step 135) reaches 485,688 faces and a 139,111-edge horizon, which the reference's own
+// algorithm needs 334 s of one CPU core to finish. The fast path keeps 128 faces / 32 edges per
+// warp in shared memory; an EPA that outgrows it is rerun by k_narrow_big in a per-warp
+// global-memory arena (2,097,152 faces, 524,288 edges, an O(1)-per-push horizon). Beyond that
+// the step reports NANS_ERR_EPA_CAPACITY.
 constexpr int kEpaMaxVerts = 72;
 constexpr int kEpaFastFaces = 128;
 constexpr int kEpaFastEdges = 32;
-constexpr int kEpaBigFaces = 262144;
-constexpr int kEpaBigEdges = 65536;
-constexpr int kEpaArenaWarps = 32;     // slow-path warps (each with its own arena)
+constexpr int kEpaBigFaces = 1 << 21;
+constexpr int kEpaBigEdges = 1 << 19;
+constexpr int kEpaArenaWarps = 16;     // slow-path warps (each with its own ~78 MB arena)
 constexpr int kEpaOverflowCap = 65536; // queued EPAs per step
 
 __global__ void k_sweep(DevWorld w, float pending_dt, float dt, int flags);

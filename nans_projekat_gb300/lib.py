@@ -28,6 +28,7 @@ ERRORS = {
 }
 UPLOAD_KEEP_MODEL = 1
 WORLD_ALL_PAIRS = 1
+WORLD_STRICT_EPA = 2
 
 # Every symbol include/nans_gb300.h declares.
 EXPORTS = (
@@ -35,6 +36,7 @@ EXPORTS = (
     "nans_batch_step", "nans_batch_autotune", "nans_world_download", "nans_world_set_state",
     "nans_get_pairs", "nans_world_status", "nans_world_counts", "nans_world_stream",
     "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps",
+    "nans_world_epa_stats",
 )
 
 
@@ -85,6 +87,7 @@ def load(path=LIB_PATH):
     L.nans_launches_per_step.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(_U)]
     L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
     L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
+    L.nans_world_epa_stats.argtypes = [_P, _P, ctypes.c_int]
     _LIB = L
     return L
 
@@ -115,9 +118,10 @@ class World:
     batch_step(dt, n, g)   the batched path: persistent kernels replayed from a CUDA graph
     """
 
-    def __init__(self, device=0, all_pairs=False, max_candidates=0):
+    def __init__(self, device=0, all_pairs=False, max_candidates=0, strict_epa=False):
         self.lib = load()
-        d = WorldDesc(device, WORLD_ALL_PAIRS if all_pairs else 0, max_candidates)
+        flags = (WORLD_ALL_PAIRS if all_pairs else 0) | (WORLD_STRICT_EPA if strict_epa else 0)
+        d = WorldDesc(device, flags, max_candidates)
         h = _P()
         _check(self.lib.nans_world_create(ctypes.byref(d), ctypes.byref(h)))
         self.h = h
@@ -233,6 +237,13 @@ class World:
         ms = np.zeros(4, np.float32)
         _check(self.lib.nans_profile_steps(self.h, dt, n, _ptr(ms)))
         return ms
+
+    def epa_stats(self, reset=False):
+        out = np.zeros(6, np.uint32)
+        _check(self.lib.nans_world_epa_stats(self.h, _ptr(out), 1 if reset else 0))
+        return dict(max_faces=int(out[0]), max_edges=int(out[1]), slow_epas=int(out[2]),
+                    overflow_candidate=int(out[3]) - 1, overflow_scene=int(out[4]) - 1,
+                    overflows=int(out[5]))
 
     @property
     def n_bodies(self):

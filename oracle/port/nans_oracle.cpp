@@ -516,6 +516,7 @@ static std::atomic<long long> g_epa_calls(0);
 static std::atomic<long long> g_epa_big[4]; // EPAs whose face list exceeded 128, 256, 1024, 4096
 static std::atomic<long long> g_epa_big_nan0(0); // of those above 128: face 0 had a NaN distance
 static std::atomic<long long> g_epa_stale(0);     // EPAs that read the emptied face list
+static std::atomic<long long> g_epa_big_contact(0); // EPAs above 1024 faces that returned a contact
 static void atomic_max(std::atomic<int> &a, int v)
 {
     int cur = a.load();
@@ -530,8 +531,10 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
     struct BigCount
     {
         size_t peak = 0;
+        bool contact = false;
         ~BigCount()
         {
+            if (peak > 1024 && contact) g_epa_big_contact.fetch_add(1);
             if (peak > 128) g_epa_big[0].fetch_add(1);
             if (peak > 256) g_epa_big[1].fetch_add(1);
             if (peak > 1024) g_epa_big[2].fetch_add(1);
@@ -635,6 +638,7 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             out.pa = add(add(mul(u, cf.a.SupA), mul(v, cf.b.SupA)), mul(w, cf.c.SupA));
             out.n = mul(T(-1), cf.n);
             out.pb = add(add(mul(u, cf.a.SupB), mul(v, cf.b.SupB)), mul(w, cf.c.SupB));
+            big.contact = true;
             return true;
         }
         const Face<T> last_face = F.back();
@@ -1164,7 +1168,7 @@ void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
 // EPA size statistics since the last reset: out[0] max faces, [1] max edges,
 // [2] max iteration index, [3] EPA calls, [4..7] EPAs whose face list exceeded
 // 128, 256, 1024, 4096 faces, [8] of those above 128 with a NaN face 0, [9] EPAs whose
-// face list emptied.
+// face list emptied, [10] EPAs above 1024 faces that returned a contact.
 void nanso_epa_stats(long long *out, int reset)
 {
     out[0] = g_epa_max_faces.load();
@@ -1175,8 +1179,10 @@ void nanso_epa_stats(long long *out, int reset)
         out[4 + i] = g_epa_big[i].load();
     out[8] = g_epa_big_nan0.load();
     out[9] = g_epa_stale.load();
+    out[10] = g_epa_big_contact.load();
     if (reset)
     {
+        g_epa_big_contact = 0;
         g_epa_stale = 0;
         g_epa_big_nan0 = 0;
         for (int i = 0; i < 4; ++i)
