@@ -35,6 +35,14 @@ ALG_BYTES_NARROW_CAND = 12 + 4 + 2 * (16 + 16) + 2 * 96  # pair, flag, 2 shapes,
 ALG_BYTES_NARROW_HIT = 36          # contact points and normal
 
 
+def _jsonable(o):
+    if isinstance(o, (np.floating,)):
+        return float(o)
+    if isinstance(o, (np.integer,)):
+        return int(o)
+    raise TypeError(type(o).__name__)
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -252,7 +260,7 @@ def run_reference_arm(args):
                          "sample": "%d scenes (every %dth) per step, %d bodies" % (len(sample), stride, bodies)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line))
+    print(json.dumps(line, default=_jsonable))
 
 
 def run_ours(args):
@@ -364,7 +372,7 @@ def run_ours(args):
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
-        print(json.dumps(line))
+        print(json.dumps(line, default=_jsonable))
     w.close()
     if dist is not None:
         dist.destroy_process_group()
