@@ -205,6 +205,34 @@ int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain
 /* The project sine/cosine used by the Model rebuild, evaluated on the device (n values). */
 int nans_device_sincos(const float *x, float *s, float *c, uint32_t n);
 
+/* ---- allocation-free solve -------------------------------------------------------- */
+
+/* No counterpart in the reference: an extra entry point for callers that must not allocate
+ * GPU memory after start-up -- a host that, like the reference's own platform layer, owns all
+ * memory and hands it to the simulation library each frame, an engine whose GPU memory belongs
+ * to the application's pool, or a real-time loop that forbids allocation once running. The
+ * nans_world_* calls allocate with cudaMalloc; this one allocates nothing.
+ *
+ * It runs the sequential-impulse solve of one scene's contact list (the world's solver:
+ * SolveConstraints, code/nans.cpp:1538-1548, with contacts touching disjoint bodies run in
+ * parallel waves; results are bit-identical) on device buffers the caller owns:
+ *   bodies [0, ncubes) are cubes, [ncubes, nbodies) spheres; d_position, d_velocity and
+ *   d_angular_velocity hold nbodies x 3 floats, d_mass and d_moi nbodies floats; velocities
+ *   are updated in place. floor (host) holds Position[3], V[3], W[3], Mass, MOI of the static
+ *   ground; d_pairs holds npairs contact records as nans_get_pairs returns them.
+ * Scratch lives in one fixed device array inside the library (about 2.7 MB on every GPU that
+ * loads it, kept until the process exits): at most 16,384 bodies and 16,384 contacts per call,
+ * larger requests fail with NANS_ERR_INVALID_ARGUMENT. Every call shares that array, so calls
+ * whose kernels overlap on the GPU race; serialise them. The first call on a device looks up
+ * the array's device address (once per device, with that device current); make that first
+ * call before any stream capture. The call is synchronous on `stream` (a cudaStream_t, NULL for
+ * the default stream). A contact naming a body outside the scene is skipped and reported as
+ * NANS_ERR_INVALID_ARGUMENT. */
+int nans_solve_contacts_static(uint32_t nbodies, uint32_t ncubes, const float *d_position, const float *d_mass,
+                               const float *d_moi, float *d_velocity, float *d_angular_velocity, const float *floor,
+                               const nans_contact_pair *d_pairs, uint32_t npairs, float cr, float cf,
+                               int32_t iterations, float dt, void *stream);
+
 /* Description of the last failure on the calling thread ("" if none). */
 const char *nans_last_error(void);
 

@@ -44,6 +44,13 @@ int fail(int code, const std::string &msg)
     } while (0)
 
 constexpr int kSolveThreadsHost = 256;
+} // namespace
+
+// Lets other translation units of the library report through nans_last_error().
+void nans::set_last_error(const char *msg) { g_err = msg; }
+
+namespace
+{
 constexpr int kSweepThreads = 256;
 constexpr size_t kSolveSmemMax = 200 * 1024;
 } // namespace

@@ -5,6 +5,8 @@
 namespace nans
 {
 
+void set_last_error(const char *msg);
+
 // k_sweep flags
 enum SweepFlags
 {

@@ -36,7 +36,7 @@ EXPORTS = (
     "nans_batch_step", "nans_batch_autotune", "nans_world_download", "nans_world_set_state",
     "nans_get_pairs", "nans_world_status", "nans_world_counts", "nans_world_stream",
     "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps",
-    "nans_world_epa_stats",
+    "nans_world_epa_stats", "nans_solve_contacts_static",
 )
 
 
@@ -88,6 +88,8 @@ def load(path=LIB_PATH):
     L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
     L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
     L.nans_world_epa_stats.argtypes = [_P, _P, ctypes.c_int]
+    L.nans_solve_contacts_static.argtypes = [_U, _U, _P, _P, _P, _P, _P, _P, _P, _U, _F, _F, ctypes.c_int32,
+                                             _F, _P]
     _LIB = L
     return L
 
@@ -252,3 +254,12 @@ class World:
     @property
     def stream(self):
         return self.lib.nans_world_stream(self.h)
+
+
+def solve_contacts_static(nbodies, ncubes, d_position, d_mass, d_moi, d_velocity, d_angular_velocity, floor,
+                          d_pairs, npairs, cr, cf, iterations, dt, stream=None):
+    """Allocation-free contact solve on caller-owned device buffers (raw device addresses)."""
+    floor = np.ascontiguousarray(floor, np.float32)
+    _check(load().nans_solve_contacts_static(nbodies, ncubes, d_position, d_mass, d_moi, d_velocity,
+                                             d_angular_velocity, _ptr(floor), d_pairs, npairs, cr, cf,
+                                             iterations, dt, stream))
