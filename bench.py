@@ -306,7 +306,7 @@ def run_ours(args):
     # per-stage device time from a live event-timed pass over the same world
     prof_steps = 10
     stage_ms = w.profile(DT, prof_steps) / prof_steps
-    names = ["k_sweep", "k_cull (3 kernels)", "k_narrow", "k_solve"]
+    names = ["k_sweep", "k_cull (3 kernels)", "k_narrow", "k_narrow_big", "k_solve"]
     dom = int(np.argmax(stage_ms))
     peak, peak_kind = measured_peaks()
     n_boxes = int(sum(len(s.cubes) for s in batch))

@@ -195,8 +195,9 @@ int nans_world_epa_stats(nans_world *world, uint32_t *out, int reset);
 void *nans_world_stream(nans_world *world);
 
 /* Runs nsteps steps stage by stage with CUDA events on the world's stream between the
- * stages and adds each stage's device time in milliseconds to stage_ms[0..3]:
- * [0] integrate sweep, [1] pair cull (3 kernels), [2] narrowphase (GJK+EPA), [3] solver. */
+ * stages and adds each stage's device time in milliseconds to stage_ms[0..4]:
+ * [0] integrate sweep, [1] pair cull (3 kernels), [2] narrowphase (GJK + shared-memory EPA),
+ * [3] large-polytope EPA, [4] solver. */
 int nans_profile_steps(nans_world *world, float dt, uint32_t nsteps, float *stage_ms);
 
 /* Kernel launches per step on the batched path and on the plain path. */

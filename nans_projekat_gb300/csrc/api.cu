@@ -353,9 +353,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.pair_mask, (size_t)((pair_acc + 31) / 32))) ||
         (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.n_cand, 1)) ||
         (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
-        (rc = dalloc(w, L, &d.work_counter, 4)) || (rc = dalloc(w, L, &d.status, 1)) ||
-        (rc = dalloc(w, L, &d.ovf_cand, kEpaOverflowCap)) ||
-        (rc = dalloc(w, L, &d.ovf_simplex, (size_t)12 * kEpaOverflowCap)) ||
+        (rc = dalloc(w, L, &d.work_counter, 8)) || (rc = dalloc(w, L, &d.status, 1)) ||
+        (rc = dalloc(w, L, &d.ovf_cand, kEpaOverflowCap)) || (rc = dalloc(w, L, &d.med_cand, kEpaMediumCap)) ||
         (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes() * (size_t)kEpaArenaWarps)) ||
         (rc = dalloc(w, L, &d.epa_stats, 8)) ||
         (rc = dalloc(w, L, &w->d_rec_cube, (size_t)61 * tc)) || (rc = dalloc(w, L, &w->d_rec_sphere, (size_t)37 * ts)) ||
@@ -377,6 +376,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.prm = w->d_prm;
     d.model_in = w->d_model_in;
     d.ovf_cap = kEpaOverflowCap;
+    d.med_cap = kEpaMediumCap;
+    d.medium_blocks = 2 * w->sm_count;
     d.epa_arena_warps = kEpaArenaWarps;
     cudaStream_t st = w->stream;
     CK(cudaMemcpyAsync(p_cube0, sc_cube0.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -471,7 +472,7 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
 {
     cudaStream_t st = w->stream;
     DevWorld &d = w->dw;
-    CK(cudaMemsetAsync(d.work_counter, 0, 4 * sizeof(int), st));
+    CK(cudaMemsetAsync(d.work_counter, 0, 8 * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
     k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
@@ -548,7 +549,7 @@ int ensure_graph(nans_world *w, float dt, int gsteps)
     DevWorld &d = w->dw;
     for (int i = 0; i < gsteps; ++i)
     {
-        cudaMemsetAsync(d.work_counter, 0, 4 * sizeof(int), st);
+        cudaMemsetAsync(d.work_counter, 0, 8 * sizeof(int), st);
         cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st);
         cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st);
         k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, dt, dt,
@@ -947,15 +948,15 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         return fail(NANS_ERR_INVALID_ARGUMENT, "profile: dt must be finite and positive");
     CK(cudaSetDevice(w->device));
     cudaStream_t st = w->stream;
-    cudaEvent_t ev[5];
-    for (int i = 0; i < 5; ++i)
+    cudaEvent_t ev[6];
+    for (int i = 0; i < 6; ++i)
         CK(cudaEventCreate(&ev[i]));
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < 5; ++i)
         stage_ms[i] = 0.0f;
     DevWorld &d = w->dw;
     for (uint32_t k = 0; k < nsteps; ++k)
     {
-        CK(cudaMemsetAsync(d.work_counter, 0, 4 * sizeof(int), st));
+        CK(cudaMemsetAsync(d.work_counter, 0, 8 * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
         CK(cudaEventRecord(ev[0], st));
@@ -964,21 +965,23 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[1], st));
         enqueue_cull(w);
         CK(cudaEventRecord(ev[2], st));
-        launch_narrow(w->narrow_warps, narrow_grid(w), st, w->dw);
+        launch_narrow_fast(w->narrow_warps, narrow_grid(w), st, w->dw);
         CK(cudaEventRecord(ev[3], st));
-        k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+        launch_narrow_big(st, w->dw);
         CK(cudaEventRecord(ev[4], st));
+        k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+        CK(cudaEventRecord(ev[5], st));
         CK(cudaGetLastError());
         after_step(w, dt);
-        CK(cudaEventSynchronize(ev[4]));
-        for (int i = 0; i < 4; ++i)
+        CK(cudaEventSynchronize(ev[5]));
+        for (int i = 0; i < 5; ++i)
         {
             float ms = 0.0f;
             CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
             stage_ms[i] += ms;
         }
     }
-    for (int i = 0; i < 5; ++i)
+    for (int i = 0; i < 6; ++i)
         cudaEventDestroy(ev[i]);
     return check_status(w);
 }

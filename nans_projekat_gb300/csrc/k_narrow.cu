@@ -665,19 +665,6 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
     return EPA_NONE;
 }
 
-__device__ __forceinline__ GV shfl_gv(const GV &g, int src)
-{
-    GV r;
-    r.p = mk3(__shfl_sync(0xffffffffu, g.p.x, src), __shfl_sync(0xffffffffu, g.p.y, src),
-              __shfl_sync(0xffffffffu, g.p.z, src));
-    r.sa = mk3(__shfl_sync(0xffffffffu, g.sa.x, src), __shfl_sync(0xffffffffu, g.sa.y, src),
-               __shfl_sync(0xffffffffu, g.sa.z, src));
-    r.sb = mk3(__shfl_sync(0xffffffffu, g.sb.x, src), __shfl_sync(0xffffffffu, g.sb.y, src),
-               __shfl_sync(0xffffffffu, g.sb.z, src));
-    return r;
-}
-
-// Persistent narrowphase: warps take 32 candidates at a time from a global queue.
 __device__ __forceinline__ void write_result(const DevWorld &w, int cc, int res, v3 pa, v3 pb, v3 nn)
 {
     w.hit[cc] = (res == EPA_CONTACT) ? 1 : 0;
@@ -689,15 +676,223 @@ __device__ __forceinline__ void write_result(const DevWorld &w, int cc, int res,
     }
 }
 
-// Persistent narrowphase: warps take 32 candidates at a time from a global queue. EPAs that
-// outgrow the shared-memory buffers are queued, with their GJK simplex, for k_narrow_big.
-// Dynamic shared memory: one EpaFast per warp.
-template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_narrow(DevWorld w)
+// Queues a candidate whose EPA outgrew the current tier: the warp tier (capacity med_cap),
+// then the large-polytope tier (capacity ovf_cap). The next tier reruns GJK (deterministic,
+// so it sees the same simplex) and EPA from scratch.
+__device__ __forceinline__ void escalate(const DevWorld &w, int c, bool to_big)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    EpaFast *epa = reinterpret_cast<EpaFast *>(smem_raw);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    EpaFast &E = epa[wid];
+    w.hit[c] = 0;
+    if (!to_big)
+    {
+        int q = atomicAdd(w.work_counter + 5, 1);
+        if (q < w.med_cap)
+        {
+            w.med_cand[q] = c;
+            return;
+        }
+    }
+    int q = atomicAdd(w.work_counter + 3, 1);
+    if (q < w.ovf_cap)
+        w.ovf_cand[q] = c;
+    else
+        atomicOr(w.status, (unsigned)ST_EPA_FACES);
+}
+
+// ------------------------------------------------------------------------------------
+// Tier 1: one thread per candidate pair, GJK then EPA on a small per-thread polytope.
+// Positions of the polytope's vertices, its faces and the horizon live in shared memory in
+// field-major layout ([slot][thread], so a warp touches 32 consecutive words); the support
+// points SupA/SupB, read only for the final contact point, live in thread-local arrays.
+// 12 vertices (8 EPA iterations) and 20 faces hold ~99.7% of the EPAs of the stack workload.
+// ------------------------------------------------------------------------------------
+constexpr int kTinyThreads = 64;
+constexpr int kTinyV = 12;
+constexpr int kTinyF = 20;
+constexpr int kTinyE = 12;
+
+struct TinySmem
+{
+    float px[kTinyV][kTinyThreads], py[kTinyV][kTinyThreads], pz[kTinyV][kTinyThreads];
+    float fnx[kTinyF][kTinyThreads], fny[kTinyF][kTinyThreads], fnz[kTinyF][kTinyThreads];
+    float fd[kTinyF][kTinyThreads];
+    unsigned fidx[kTinyF][kTinyThreads]; // a | b << 8 | c << 16
+    unsigned short edge[kTinyE][kTinyThreads]; // a | b << 8
+};
+
+struct TinyLocal
+{
+    float sa[kTinyV][3], sb[kTinyV][3];
+};
+
+__device__ __forceinline__ v3 tiny_p(const TinySmem &S, int t, int i) { return mk3(S.px[i][t], S.py[i][t], S.pz[i][t]); }
+
+__device__ __forceinline__ void tiny_put(TinySmem &S, TinyLocal &L, int t, int i, const GV &g)
+{
+    S.px[i][t] = g.p.x;
+    S.py[i][t] = g.p.y;
+    S.pz[i][t] = g.p.z;
+    L.sa[i][0] = g.sa.x;
+    L.sa[i][1] = g.sa.y;
+    L.sa[i][2] = g.sa.z;
+    L.sb[i][0] = g.sb.x;
+    L.sb[i][1] = g.sb.y;
+    L.sb[i][2] = g.sb.z;
+}
+
+// PushTriangle (code/nans.cpp:292-322) with the face distance cached.
+__device__ __forceinline__ void tiny_face(TinySmem &S, int t, int f, int a, int b, int c)
+{
+    v3 pa = tiny_p(S, t, a), pb = tiny_p(S, t, b), pc = tiny_p(S, t, c);
+    v3 n = normalize3(cross3(pb - pa, pc - pa));
+    if (dot3(pa, n) < 0.0f)
+        n = -1.0f * n;
+    S.fidx[f][t] = (unsigned)a | ((unsigned)b << 8) | ((unsigned)c << 16);
+    S.fnx[f][t] = n.x;
+    S.fny[f][t] = n.y;
+    S.fnz[f][t] = n.z;
+    S.fd[f][t] = fabsf(dot3(n, pa));
+}
+
+// PushEdge (code/nans.cpp:232-266), sequential. Returns false on overflow.
+__device__ __forceinline__ bool tiny_edge(TinySmem &S, int t, int &ne, int u, int v)
+{
+    v3 pu = tiny_p(S, t, u), pv = tiny_p(S, t, v);
+    for (int e = 0; e < ne; ++e)
+    {
+        unsigned ed = S.edge[e][t];
+        if (eq3(tiny_p(S, t, ed & 0xffu), pv) && eq3(tiny_p(S, t, ed >> 8), pu))
+        {
+            for (int k = e + 1; k < ne; ++k)
+                S.edge[k - 1][t] = S.edge[k][t];
+            --ne;
+            return true;
+        }
+    }
+    if (ne >= kTinyE)
+        return false;
+    S.edge[ne][t] = (unsigned short)(u | (v << 8));
+    ++ne;
+    return true;
+}
+
+// ResolveCollision (code/nans.cpp:787-904) by one thread; same results as epa_run.
+__device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, const Shape &B, const GV &s0,
+                        const GV &s1, const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n)
+{
+    TinyLocal L;
+    tiny_put(S, L, t, 0, s0);
+    tiny_put(S, L, t, 1, s1);
+    tiny_put(S, L, t, 2, s2);
+    tiny_put(S, L, t, 3, s3);
+    tiny_face(S, t, 0, 0, 1, 2);
+    tiny_face(S, t, 1, 0, 2, 3);
+    tiny_face(S, t, 2, 0, 3, 1);
+    tiny_face(S, t, 3, 1, 3, 2);
+    int nf = 4, nv = 4;
+    bool stale = false;
+    for (int it = 0; it <= 64; ++it)
+    {
+        if (nf == 0 && !stale)
+            return EPA_NONE;
+        int ci = 0;
+        float cur = S.fd[0][t];
+        if (nf > 0 && !isnan(cur))
+            for (int f = 1; f < nf; ++f)
+            {
+                float d = S.fd[f][t];
+                if (d < cur)
+                {
+                    cur = d;
+                    ci = f;
+                }
+            }
+        const v3 n = mk3(S.fnx[ci][t], S.fny[ci][t], S.fnz[ci][t]);
+        const GV ns = minkowski_support(w.verts, A, B, n);
+        if (dot3(n, ns.p) - cur < 0.001f)
+        {
+            unsigned fi = S.fidx[ci][t];
+            int ia = fi & 0xffu, ib = (fi >> 8) & 0xffu, ic = fi >> 16;
+            v3 pa = tiny_p(S, t, ia), pb = tiny_p(S, t, ib), pc = tiny_p(S, t, ic);
+            v3 p = cur * n;
+            v3 v0 = pb - pa, v1 = pc - pa, v2 = p - pa;
+            float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
+            float d20 = dot3(v2, v0), d21 = dot3(v2, v1);
+            float den = d00 * d11 - d01 * d01;
+            float bv = (d11 * d20 - d01 * d21) / den;
+            float bw = (d00 * d21 - d01 * d20) / den;
+            float bu = 1.0f - bv - bw;
+            if (fabsf(bu) > 1.0f || fabsf(bv) > 1.0f || fabsf(bw) > 1.0f)
+                return EPA_NONE;
+            if (!isfinite(bu) || !isfinite(bv) || !isfinite(bw))
+                return EPA_NONE;
+            v3 saa = mk3(L.sa[ia][0], L.sa[ia][1], L.sa[ia][2]), sab = mk3(L.sa[ib][0], L.sa[ib][1], L.sa[ib][2]),
+               sac = mk3(L.sa[ic][0], L.sa[ic][1], L.sa[ic][2]);
+            v3 sba = mk3(L.sb[ia][0], L.sb[ia][1], L.sb[ia][2]), sbb = mk3(L.sb[ib][0], L.sb[ib][1], L.sb[ib][2]),
+               sbc = mk3(L.sb[ic][0], L.sb[ic][1], L.sb[ic][2]);
+            out_pa = ((bu * saa) + (bv * sab)) + (bw * sac);
+            out_n = -1.0f * n;
+            out_pb = ((bu * sba) + (bv * sbb)) + (bw * sbc);
+            return EPA_CONTACT;
+        }
+        if (nf == 0)
+            return EPA_NONE; // the stale read repeats identically until the iteration cap
+        // visible faces -> horizon edges, the others compacted in place (code/nans.cpp:869-891)
+        int ne = 0, keep = 0;
+        for (int f = 0; f < nf; ++f)
+        {
+            unsigned fi = S.fidx[f][t];
+            v3 fa = tiny_p(S, t, fi & 0xffu);
+            v3 fn = mk3(S.fnx[f][t], S.fny[f][t], S.fnz[f][t]);
+            if (dot3(fn, ns.p - fa) > 0.0f)
+            {
+                int a = fi & 0xffu, b = (fi >> 8) & 0xffu, c = fi >> 16;
+                if (!(tiny_edge(S, t, ne, a, b) && tiny_edge(S, t, ne, b, c) && tiny_edge(S, t, ne, c, a)))
+                    return EPA_OVERFLOW;
+            }
+            else
+            {
+                if (keep != f)
+                {
+                    S.fidx[keep][t] = fi;
+                    S.fnx[keep][t] = fn.x;
+                    S.fny[keep][t] = fn.y;
+                    S.fnz[keep][t] = fn.z;
+                    S.fd[keep][t] = S.fd[f][t];
+                }
+                ++keep;
+            }
+        }
+        if (keep + ne > kTinyF || nv >= kTinyV)
+            return EPA_OVERFLOW;
+        if (keep == 0 && ne == 0)
+        {
+            // every face removed: slot 0 keeps the last face of the list (nothing was moved)
+            int l = nf - 1;
+            S.fidx[0][t] = S.fidx[l][t];
+            S.fnx[0][t] = S.fnx[l][t];
+            S.fny[0][t] = S.fny[l][t];
+            S.fnz[0][t] = S.fnz[l][t];
+            S.fd[0][t] = S.fd[l][t];
+            stale = true;
+        }
+        int sv = nv++;
+        tiny_put(S, L, t, sv, ns);
+        for (int j = 0; j < ne; ++j)
+        {
+            unsigned ed = S.edge[j][t];
+            tiny_face(S, t, keep + j, sv, ed & 0xffu, ed >> 8);
+        }
+        nf = keep + ne;
+    }
+    return EPA_NONE;
+}
+
+// Persistent: warps take 32 candidates at a time from a global queue; each lane runs GJK and,
+// on a hit, EPA; EPAs that outgrow the per-thread polytope are queued for the warp tier.
+__global__ void __launch_bounds__(kTinyThreads) k_narrow_tiny(DevWorld w)
+{
+    __shared__ TinySmem S;
+    const int lane = threadIdx.x & 31, t = threadIdx.x;
     const int n = *w.n_cand;
     for (;;)
     {
@@ -708,64 +903,65 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_narrow(DevW
         if (base >= n)
             break;
         const int c = base + lane;
-        const bool valid = c < n;
-        int res = G_NOHIT;
+        if (c >= n)
+            continue;
+        const int a = w.cand_a[c], b = w.cand_b[c];
+        const int sc = w.cand_meta[c] >> 3;
+        if (c == 0 || (w.cand_meta[c - 1] >> 3) != sc)
+            w.cand_begin[sc] = c;
+        if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
+            w.cand_end[sc] = c + 1;
+        const Shape A = load_shape(w, a), B = load_shape(w, b);
         GV s0, s1, s2, s3;
-        int a = 0, b = 0;
-        if (valid)
+        if (gjk(w.verts, A, B, s0, s1, s2, s3) != G_FOUND)
         {
-            a = w.cand_a[c];
-            b = w.cand_b[c];
-            int sc = w.cand_meta[c] >> 3;
-            if (c == 0 || (w.cand_meta[c - 1] >> 3) != sc)
-                w.cand_begin[sc] = c;
-            if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
-                w.cand_end[sc] = c + 1;
-            Shape A = load_shape(w, a), B = load_shape(w, b);
-            res = gjk(w.verts, A, B, s0, s1, s2, s3);
-            if (res != G_FOUND)
-                w.hit[c] = 0;
+            w.hit[c] = 0;
+            continue;
         }
-        unsigned hits = __ballot_sync(0xffffffffu, valid && res == G_FOUND);
-        while (hits)
+        v3 pa, pb, nn;
+        int r = epa_tiny(w, S, t, A, B, s0, s1, s2, s3, pa, pb, nn);
+        if (r == EPA_OVERFLOW)
+            escalate(w, c, false);
+        else
+            write_result(w, c, r, pa, pb, nn);
+    }
+}
+
+// Tier 2: one warp per queued candidate, polytope of up to 128 faces in shared memory.
+// Dynamic shared memory: one EpaFast per warp.
+template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(DevWorld w)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    EpaFast *epa = reinterpret_cast<EpaFast *>(smem_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    EpaFast &E = epa[wid];
+    const int n = min(w.work_counter[5], w.med_cap);
+    for (;;)
+    {
+        int q = 0;
+        if (lane == 0)
+            q = atomicAdd(w.work_counter + 6, 1);
+        q = __shfl_sync(0xffffffffu, q, 0);
+        if (q >= n)
+            break;
+        const int cc = w.med_cand[q];
+        const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
+        GV s0, s1, s2, s3;
+        gjk(w.verts, A, B, s0, s1, s2, s3); // every lane: same inputs, same simplex
+        v3 pa, pb, nn;
+        int r = epa_run(w, E, A, B, s0, s1, s2, s3, pa, pb, nn, lane);
+        __syncwarp();
+        if (lane == 0)
         {
-            int src = __ffs(hits) - 1;
-            hits &= hits - 1;
-            GV t0 = shfl_gv(s0, src), t1 = shfl_gv(s1, src), t2 = shfl_gv(s2, src), t3 = shfl_gv(s3, src);
-            int ga = __shfl_sync(0xffffffffu, a, src), gb = __shfl_sync(0xffffffffu, b, src);
-            Shape A = load_shape(w, ga), B = load_shape(w, gb);
-            v3 pa, pb, nn;
-            int r = epa_run(w, E, A, B, t0, t1, t2, t3, pa, pb, nn, lane);
-            __syncwarp();
-            if (lane == 0)
-            {
-                int cc = base + src;
-                if (r == EPA_OVERFLOW)
-                {
-                    int q = atomicAdd(w.work_counter + 3, 1);
-                    w.hit[cc] = 0;
-                    if (q < w.ovf_cap)
-                    {
-                        w.ovf_cand[q] = cc;
-                        const GV *g[4] = {&t0, &t1, &t2, &t3};
-                        for (int k = 0; k < 4; ++k)
-                        {
-                            w.ovf_simplex[(size_t)12 * q + 3 * k] = f4(g[k]->p, 0.0f);
-                            w.ovf_simplex[(size_t)12 * q + 3 * k + 1] = f4(g[k]->sa, 0.0f);
-                            w.ovf_simplex[(size_t)12 * q + 3 * k + 2] = f4(g[k]->sb, 0.0f);
-                        }
-                    }
-                    else
-                        atomicOr(w.status, (unsigned)ST_EPA_FACES);
-                }
-                else
-                    write_result(w, cc, r, pa, pb, nn);
-            }
+            if (r == EPA_OVERFLOW)
+                escalate(w, cc, true);
+            else
+                write_result(w, cc, r, pa, pb, nn);
         }
     }
 }
 
-// Slow path: one warp per queued EPA, polytope in a per-warp global-memory arena.
+// Tier 3: one warp per queued candidate, polytope in a per-warp global-memory arena.
 __global__ void __launch_bounds__(128) k_narrow_big(DevWorld w)
 {
     const int lane = threadIdx.x & 31;
@@ -781,16 +977,11 @@ __global__ void __launch_bounds__(128) k_narrow_big(DevWorld w)
         if (q >= n)
             break;
         const int cc = w.ovf_cand[q];
-        GV t[4];
-        for (int k = 0; k < 4; ++k)
-        {
-            t[k].p = xyz(w.ovf_simplex[(size_t)12 * q + 3 * k]);
-            t[k].sa = xyz(w.ovf_simplex[(size_t)12 * q + 3 * k + 1]);
-            t[k].sb = xyz(w.ovf_simplex[(size_t)12 * q + 3 * k + 2]);
-        }
-        Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
+        const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
+        GV s0, s1, s2, s3;
+        gjk(w.verts, A, B, s0, s1, s2, s3);
         v3 pa, pb, nn;
-        int r = epa_run(w, E, A, B, t[0], t[1], t[2], t[3], pa, pb, nn, lane);
+        int r = epa_run(w, E, A, B, s0, s1, s2, s3, pa, pb, nn, lane);
         __syncwarp();
         if (lane == 0)
         {
@@ -812,37 +1003,39 @@ __global__ void __launch_bounds__(128) k_narrow_big(DevWorld w)
 
 size_t epa_big_bytes() { return sizeof(EpaBig); }
 
-static size_t narrow_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }
+static size_t medium_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }
 
 static void narrow_attrs()
 {
     static bool done = false;
     if (done)
         return;
-    cudaFuncSetAttribute(k_narrow<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(4));
-    cudaFuncSetAttribute(k_narrow<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)narrow_smem(8));
+    cudaFuncSetAttribute(k_epa_medium<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)medium_smem(4));
     done = true;
 }
 
 int narrow_blocks_per_sm(int warps)
 {
-    narrow_attrs();
+    (void)warps;
     int per = 0;
-    if (warps == 8)
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow<8>, 256, narrow_smem(8));
-    else
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow<4>, 128, narrow_smem(4));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow_tiny, kTinyThreads, 0);
     return per;
 }
 
+void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
+{
+    (void)warps;
+    narrow_attrs();
+    k_narrow_tiny<<<grid, kTinyThreads, 0, st>>>(w);
+    k_epa_medium<4><<<w.medium_blocks, 128, medium_smem(4), st>>>(w);
+}
+
+void launch_narrow_big(cudaStream_t st, const DevWorld &w) { k_narrow_big<<<w.epa_arena_warps / 4, 128, 0, st>>>(w); }
+
 void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
 {
-    narrow_attrs();
-    if (warps == 8)
-        k_narrow<8><<<grid, 256, narrow_smem(8), st>>>(w);
-    else
-        k_narrow<4><<<grid, 128, narrow_smem(4), st>>>(w);
-    k_narrow_big<<<w.epa_arena_warps / 4, 128, 0, st>>>(w);
+    launch_narrow_fast(warps, grid, st, w);
+    launch_narrow_big(st, w);
 }
 
 } // namespace nans

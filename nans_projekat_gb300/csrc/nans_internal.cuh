@@ -79,11 +79,14 @@ struct DevWorld
     // narrowphase output, per candidate
     int *hit;
     float4 *c_pa, *c_pb, *c_n;
-    int *work_counter;                  // [0] narrowphase, [1] solver, [2] slow EPA queue heads,
-                                        // [3] slow EPA queue length
-    int ovf_cap;                        // slow EPA queue capacity
-    int *ovf_cand;                      // queued candidate index
-    float4 *ovf_simplex;                // queued GJK simplex: 4 x (P, SupA, SupB)
+    int *work_counter;                  // [0] narrowphase head, [1] solver head, [2] large-EPA
+                                        // head, [3] large-EPA queue length, [5] warp-EPA queue
+                                        // length, [6] warp-EPA head
+    int med_cap;                        // warp-EPA queue capacity
+    int *med_cand;                      // candidates queued for the warp tier
+    int medium_blocks;                  // warp-tier grid
+    int ovf_cap;                        // large-EPA queue capacity
+    int *ovf_cand;                      // candidates queued for the large-polytope tier
     unsigned char *epa_arena;           // slow-path polytope buffers, one per warp
     int epa_arena_warps;
     unsigned *epa_stats;                // [0] max faces, [1] max horizon edges, [2] slow-path EPAs,

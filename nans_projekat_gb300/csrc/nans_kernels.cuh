@@ -37,7 +37,8 @@ constexpr int kEpaFastEdges = 32;
 constexpr int kEpaBigFaces = 1 << 21;
 constexpr int kEpaBigEdges = 1 << 19;
 constexpr int kEpaArenaWarps = 16;     // slow-path warps (each with its own ~78 MB arena)
-constexpr int kEpaOverflowCap = 65536; // queued EPAs per step
+constexpr int kEpaOverflowCap = 65536; // large-polytope EPAs queued per step
+constexpr int kEpaMediumCap = 1 << 20;  // warp-tier EPAs queued per step
 
 __global__ void k_sweep(DevWorld w, float pending_dt, float dt, int flags);
 __global__ void k_unpack(DevWorld w, const float *rec_cube, const float *rec_sphere, const float *rec_floor,
@@ -54,6 +55,8 @@ __global__ void k_cull_write(DevWorld w);
 int narrow_blocks_per_sm(int warps);
 size_t epa_big_bytes();
 void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w);
+void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w);
+void launch_narrow_big(cudaStream_t st, const DevWorld &w);
 __global__ void k_solve(DevWorld w, float dt);
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);
 

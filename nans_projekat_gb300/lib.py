@@ -235,8 +235,9 @@ class World:
         return a.value, b.value
 
     def profile(self, dt, n):
-        """Device milliseconds per stage summed over n steps: sweep, cull, narrowphase, solver."""
-        ms = np.zeros(4, np.float32)
+        """Device milliseconds per stage summed over n steps: sweep, cull, narrowphase,
+        large-polytope EPA, solver."""
+        ms = np.zeros(5, np.float32)
         _check(self.lib.nans_profile_steps(self.h, dt, n, _ptr(ms)))
         return ms
 

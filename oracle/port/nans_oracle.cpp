@@ -517,6 +517,8 @@ static std::atomic<long long> g_epa_big[4]; // EPAs whose face list exceeded 128
 static std::atomic<long long> g_epa_big_nan0(0); // of those above 128: face 0 had a NaN distance
 static std::atomic<long long> g_epa_stale(0);     // EPAs that read the emptied face list
 static std::atomic<long long> g_epa_big_contact(0); // EPAs above 1024 faces that returned a contact
+static std::atomic<long long> g_epa_iter_hist[5];  // EPAs ending after 1-4, 5-8, 9-16, 17-64, 65 iterations
+static std::atomic<long long> g_gjk_iters(0), g_gjk_calls(0);
 static void atomic_max(std::atomic<int> &a, int v)
 {
     int cur = a.load();
@@ -532,8 +534,11 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
     {
         size_t peak = 0;
         bool contact = false;
+        int iters = 65;
         ~BigCount()
         {
+            int b = iters <= 4 ? 0 : iters <= 8 ? 1 : iters <= 16 ? 2 : iters <= 64 ? 3 : 4;
+            g_epa_iter_hist[b].fetch_add(1);
             if (peak > 1024 && contact) g_epa_big_contact.fetch_add(1);
             if (peak > 128) g_epa_big[0].fetch_add(1);
             if (peak > 256) g_epa_big[1].fetch_add(1);
@@ -584,6 +589,7 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             g_epa_big_nan0.fetch_add(1);
         big.peak = std::max(big.peak, F.size());
         atomic_max(g_epa_max_iters, it);
+        big.iters = it + 1;
         T cur = std::fabs(dot(F[0].n, F[0].a.P));
         size_t ci = 0;
         for (size_t i = 0; i < F.size(); ++i)
@@ -677,8 +683,11 @@ template <class T> static bool check_collision(const PairCtx<T> &p, Contact<T> &
     std::vector<Vx<T>> S;
     S.reserve(8);
     int r = Evolving;
-    for (int it = 0; r == Evolving && it <= 64; ++it)
+    int it = 0;
+    for (; r == Evolving && it <= 64; ++it)
         r = evolve(p, S);
+    g_gjk_iters.fetch_add(it);
+    g_gjk_calls.fetch_add(1);
     if (r == Found)
         return epa(p, S, c);
     return false;
@@ -1168,7 +1177,8 @@ void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
 // EPA size statistics since the last reset: out[0] max faces, [1] max edges,
 // [2] max iteration index, [3] EPA calls, [4..7] EPAs whose face list exceeded
 // 128, 256, 1024, 4096 faces, [8] of those above 128 with a NaN face 0, [9] EPAs whose
-// face list emptied, [10] EPAs above 1024 faces that returned a contact.
+// face list emptied, [10] EPAs above 1024 faces that returned a contact, [11..15] EPAs that
+// ended after 1-4, 5-8, 9-16, 17-64, 65 iterations, [16] GJK evolve calls, [17] GJK runs.
 void nanso_epa_stats(long long *out, int reset)
 {
     out[0] = g_epa_max_faces.load();
@@ -1180,9 +1190,17 @@ void nanso_epa_stats(long long *out, int reset)
     out[8] = g_epa_big_nan0.load();
     out[9] = g_epa_stale.load();
     out[10] = g_epa_big_contact.load();
+    for (int i = 0; i < 5; ++i)
+        out[11 + i] = g_epa_iter_hist[i].load();
+    out[16] = g_gjk_iters.load();
+    out[17] = g_gjk_calls.load();
     if (reset)
     {
         g_epa_big_contact = 0;
+        for (int i = 0; i < 5; ++i)
+            g_epa_iter_hist[i] = 0;
+        g_gjk_iters = 0;
+        g_gjk_calls = 0;
         g_epa_stale = 0;
         g_epa_big_nan0 = 0;
         for (int i = 0; i < 4; ++i)
