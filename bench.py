@@ -306,13 +306,13 @@ def run_ours(args):
     # per-stage device time from a live event-timed pass over the same world
     prof_steps = 10
     stage_ms = w.profile(DT, prof_steps) / prof_steps
-    names = ["k_sweep", "k_cull (3 kernels)", "k_narrow", "k_narrow_big", "k_solve"]
+    names = ["k_sweep", "k_cull (3 kernels)", "k_narrow_tiny", "k_epa_medium", "k_narrow_big", "k_solve"]
     dom = int(np.argmax(stage_ms))
     peak, peak_kind = measured_peaks()
     n_boxes = int(sum(len(s.cubes) for s in batch))
     sweep_bytes = ALG_BYTES_SWEEP_BODY * bodies + ALG_BYTES_SWEEP_BOX_VERTS * n_boxes
     narrow_bytes = ALG_BYTES_NARROW_CAND * n_cand + ALG_BYTES_NARROW_HIT * n_contacts
-    alg = {0: sweep_bytes, 2: narrow_bytes}
+    alg = {0: sweep_bytes, 2: narrow_bytes, 3: narrow_bytes, 4: narrow_bytes}
     dom_bytes = alg.get(dom, narrow_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1000.0) / 1e9
     sweep_gbs = sweep_bytes / (stage_ms[0] / 1000.0) / 1e9
@@ -356,7 +356,8 @@ def run_ours(args):
                       % ((bodies * 64 + n_boxes * 96 + n_cand * 60) / 1e6),
                 "candidates_per_step": n_cand, "contacts_per_step": n_contacts,
                 "large_epa": {"slow_path_epas": epa["slow_epas"], "max_faces": epa["max_faces"],
-                              "max_horizon_edges": epa["max_edges"], "beyond_capacity": epa["overflows"]},
+                              "max_horizon_edges": epa["max_edges"], "beyond_capacity": epa["overflows"],
+                              "warp_tier_epas": epa["warp_tier"]},
             },
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": None,

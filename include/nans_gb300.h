@@ -188,16 +188,17 @@ int nans_world_counts(nans_world *world, uint32_t *candidates, uint32_t *contact
 /* Large-polytope EPA statistics since upload (or the last reset): out[0] largest face list
  * and out[1] largest horizon seen by the large-polytope path, out[2] EPAs that took that path,
  * out[3] candidate index + 1 and out[4] scene + 1 of the last EPA that outgrew it (0 if none),
- * out[5] EPAs that outgrew it. out holds 6 entries. */
+ * out[5] EPAs that outgrew it, out[6] EPAs escalated from the per-thread tier to the warp
+ * tier. out holds 7 entries. */
 int nans_world_epa_stats(nans_world *world, uint32_t *out, int reset);
 
 /* The world's CUDA stream (a cudaStream_t), for event timing by the caller. */
 void *nans_world_stream(nans_world *world);
 
 /* Runs nsteps steps stage by stage with CUDA events on the world's stream between the
- * stages and adds each stage's device time in milliseconds to stage_ms[0..4]:
- * [0] integrate sweep, [1] pair cull (3 kernels), [2] narrowphase (GJK + shared-memory EPA),
- * [3] large-polytope EPA, [4] solver. */
+ * stages and adds each stage's device time in milliseconds to stage_ms[0..5]:
+ * [0] integrate sweep, [1] pair cull (3 kernels), [2] narrowphase (GJK + per-thread EPA),
+ * [3] warp-tier EPA, [4] large-polytope EPA, [5] solver. */
 int nans_profile_steps(nans_world *world, float dt, uint32_t nsteps, float *stage_ms);
 
 /* Kernel launches per step on the batched path and on the plain path. */

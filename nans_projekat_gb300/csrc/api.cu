@@ -168,7 +168,7 @@ int alloc_candidates(nans_world *w, int cap)
         (rc = dalloc(w, L, &d.c_pa, cap)) || (rc = dalloc(w, L, &d.c_pb, cap)) || (rc = dalloc(w, L, &d.c_n, cap)) ||
         (rc = dalloc(w, L, &d.s_order, cap)) || (rc = dalloc(w, L, &d.s_wave, cap)) ||
         (rc = dalloc(w, L, &d.s_perm, cap)) || (rc = dalloc(w, L, &d.s_wcnt, (size_t)cap + 1)) ||
-        (rc = dalloc(w, L, &d.s_k, (size_t)9 * cap)))
+        (rc = dalloc(w, L, &d.s_k, (size_t)9 * cap)) || (rc = dalloc(w, L, &d.long_cand, cap)))
         return rc;
     return NANS_OK;
 }
@@ -909,7 +909,7 @@ int nans_world_epa_stats(nans_world *w, uint32_t *out, int reset)
     if (!w->uploaded)
         return fail(NANS_ERR_NOT_UPLOADED, "epa_stats: no scene uploaded");
     CK(cudaSetDevice(w->device));
-    CK(cudaMemcpyAsync(out, w->dw.epa_stats, 6 * sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaMemcpyAsync(out, w->dw.epa_stats, 7 * sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
     if (reset)
         CK(cudaMemsetAsync(w->dw.epa_stats, 0, 8 * sizeof(unsigned), w->stream));
     CK(cudaStreamSynchronize(w->stream));
@@ -948,10 +948,10 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         return fail(NANS_ERR_INVALID_ARGUMENT, "profile: dt must be finite and positive");
     CK(cudaSetDevice(w->device));
     cudaStream_t st = w->stream;
-    cudaEvent_t ev[6];
-    for (int i = 0; i < 6; ++i)
+    cudaEvent_t ev[7];
+    for (int i = 0; i < 7; ++i)
         CK(cudaEventCreate(&ev[i]));
-    for (int i = 0; i < 5; ++i)
+    for (int i = 0; i < 6; ++i)
         stage_ms[i] = 0.0f;
     DevWorld &d = w->dw;
     for (uint32_t k = 0; k < nsteps; ++k)
@@ -965,23 +965,25 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[1], st));
         enqueue_cull(w);
         CK(cudaEventRecord(ev[2], st));
-        launch_narrow_fast(w->narrow_warps, narrow_grid(w), st, w->dw);
+        launch_narrow_tiny(narrow_grid(w), st, w->dw);
         CK(cudaEventRecord(ev[3], st));
-        launch_narrow_big(st, w->dw);
+        launch_epa_medium(st, w->dw);
         CK(cudaEventRecord(ev[4], st));
-        k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+        launch_narrow_big(st, w->dw);
         CK(cudaEventRecord(ev[5], st));
+        k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+        CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());
         after_step(w, dt);
-        CK(cudaEventSynchronize(ev[5]));
-        for (int i = 0; i < 5; ++i)
+        CK(cudaEventSynchronize(ev[6]));
+        for (int i = 0; i < 6; ++i)
         {
             float ms = 0.0f;
             CK(cudaEventElapsedTime(&ms, ev[i], ev[i + 1]));
             stage_ms[i] += ms;
         }
     }
-    for (int i = 0; i < 6; ++i)
+    for (int i = 0; i < 7; ++i)
         cudaEventDestroy(ev[i]);
     return check_status(w);
 }
@@ -990,8 +992,8 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
 {
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
-    // sweep, [mask, write], scan, narrow, narrow_big, solve
-    uint32_t k = 5 + (w->cull_blocks > 0 ? 2u : 0u);
+    // sweep, [mask, write], scan, narrow_tiny, narrow_long, epa_medium, narrow_big, solve
+    uint32_t k = 7 + (w->cull_blocks > 0 ? 2u : 0u);
     if (batched)
         *batched = k;
     if (plain)

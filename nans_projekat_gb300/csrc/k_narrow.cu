@@ -26,20 +26,26 @@ enum
 {
     G_NOHIT = 0,
     G_FOUND = 1,
-    G_EVOLVING = 2
+    G_EVOLVING = 2,
+    G_BUDGET = 3 // still evolving after the caller's budget of EvolveSimplex calls
 };
 
 // TripleCross (code/nans.cpp:564-569): (A x B) x C = B * dot(C, A) - A * dot(C, B)
 __device__ __forceinline__ v3 triple_cross(v3 a, v3 b, v3 c) { return (dot3(c, a) * b) - (dot3(c, b) * a); }
 
+// CheckCollision's GJK loop (at most 65 EvolveSimplex calls). With budget < 65 it stops after
+// `budget` calls and returns G_BUDGET if the simplex is still evolving; rerunning with the
+// full budget reproduces the same sequence from the start.
 __device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,
-                                   GV &s3)
+                                   GV &s3, int budget = 65)
 {
     const v3 dir0 = normalize3(B.p - A.p);
     int n = 0;
     int res = G_EVOLVING;
     for (int it = 0; it <= 64; ++it)
     {
+        if (it >= budget)
+            return G_BUDGET;
         v3 dir = dir0;
         if (n == 1)
         {
@@ -176,22 +182,13 @@ __device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Sha
 // Polytope storage of one EPA. The vertex pool holds the GJK tetrahedron plus one support per
 // iteration; faces are an ordered list (vertex indices, normal, cached distance); edges are
 // the current horizon. FMAX / EMAX bound faces and edges.
-template <int FMAX, int EMAX, bool HASH> struct EpaBuf;
-
-// Slot of the horizon hash table: FIFO (head, tail) of live edges whose directed key is
-// (canonical P of the first vertex, canonical P of the second); valid while gen matches.
-struct HSlot
-{
-    unsigned key[6];
-    int head, tail;
-    unsigned gen;
-};
-
-template <int FMAX, int EMAX> struct EpaBuf<FMAX, EMAX, false>
+// Polytope of one warp-cooperative EPA (shared memory). The vertex pool holds the GJK
+// tetrahedron plus one support per iteration; faces are an ordered list (vertex indices,
+// normal, cached distance); edges are the current horizon.
+template <int FMAX, int EMAX> struct EpaBuf
 {
     static constexpr int kFaces = FMAX;
     static constexpr int kEdges = EMAX;
-    static constexpr bool kHash = false;
     float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
     float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
     float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
@@ -200,28 +197,7 @@ template <int FMAX, int EMAX> struct EpaBuf<FMAX, EMAX, false>
     unsigned char ea[EMAX], eb[EMAX];
     unsigned vis[FMAX / 32];
 };
-
-template <int FMAX, int EMAX> struct EpaBuf<FMAX, EMAX, true>
-{
-    static constexpr int kFaces = FMAX;
-    static constexpr int kEdges = EMAX;
-    static constexpr bool kHash = true;
-    static constexpr int kSlots = 2 * EMAX; // load factor <= 1/2
-    float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
-    float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
-    float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
-    float fnx[FMAX], fny[FMAX], fnz[FMAX], fd[FMAX];
-    unsigned char fa[FMAX], fb[FMAX], fc[FMAX];
-    unsigned char ea[EMAX], eb[EMAX];
-    unsigned vis[FMAX / 32];
-    int enext[EMAX];
-    unsigned char ealive[EMAX];
-    unsigned gen;
-    HSlot slot[kSlots];
-};
-
-using EpaFast = EpaBuf<kEpaFastFaces, kEpaFastEdges, false>; // shared memory, one per warp
-using EpaBig = EpaBuf<kEpaBigFaces, kEpaBigEdges, true>;     // global memory, one per slow-path warp
+using EpaFast = EpaBuf<kEpaFastFaces, kEpaFastEdges>; // shared memory, one per warp
 
 enum
 {
@@ -321,109 +297,6 @@ __device__ __forceinline__ unsigned canon_bits(float x)
 {
     unsigned b = __float_as_uint(x);
     return (b == 0x80000000u) ? 0u : b;
-}
-
-// Horizon for large polytopes, run by one lane: the same result as PushEdge in push order
-// (each push cancels the first live stored edge that is its reverse, else is appended), in
-// O(1) per push. Live edges with equal directed keys form FIFO queues, so "first live reverse
-// edge" is the head of the reverse key's queue. A vertex with a NaN coordinate equals nothing,
-// so its edges are appended without a key.
-template <class B> __device__ int horizon_hash(B &E, int nchunks)
-{
-    E.gen = E.gen + 1u;
-    const unsigned gen = E.gen;
-    int ne = 0;
-    for (int ch = 0; ch < nchunks; ++ch)
-    {
-        unsigned m = E.vis[ch];
-        while (m)
-        {
-            int f = ch * 32 + __ffs(m) - 1;
-            m &= m - 1;
-            int vv[4] = {E.fa[f], E.fb[f], E.fc[f], E.fa[f]};
-            for (int k = 0; k < 3; ++k)
-            {
-                int u = vv[k], v = vv[k + 1];
-                v3 pu = pool_p(E, u), pv = pool_p(E, v);
-                bool nan = isnan(pu.x) || isnan(pu.y) || isnan(pu.z) || isnan(pv.x) || isnan(pv.y) || isnan(pv.z);
-                unsigned ku[3] = {canon_bits(pu.x), canon_bits(pu.y), canon_bits(pu.z)};
-                unsigned kv[3] = {canon_bits(pv.x), canon_bits(pv.y), canon_bits(pv.z)};
-                if (!nan)
-                {
-                    // look up the reverse key (v, u)
-                    unsigned h = 2166136261u;
-                    for (int q = 0; q < 3; ++q)
-                        h = (h ^ kv[q]) * 16777619u;
-                    for (int q = 0; q < 3; ++q)
-                        h = (h ^ ku[q]) * 16777619u;
-                    int found = -1;
-                    for (int probe = 0; probe < B::kSlots; ++probe)
-                    {
-                        HSlot &sl = E.slot[(h + probe) & (B::kSlots - 1)];
-                        if (sl.gen != gen)
-                            break;
-                        if (sl.key[0] == kv[0] && sl.key[1] == kv[1] && sl.key[2] == kv[2] && sl.key[3] == ku[0] &&
-                            sl.key[4] == ku[1] && sl.key[5] == ku[2])
-                        {
-                            found = (int)((h + probe) & (B::kSlots - 1));
-                            break;
-                        }
-                    }
-                    if (found >= 0 && E.slot[found].head >= 0)
-                    {
-                        HSlot &sl = E.slot[found];
-                        int e = sl.head;
-                        E.ealive[e] = 0;
-                        sl.head = E.enext[e];
-                        if (sl.head < 0)
-                            sl.tail = -1;
-                        continue;
-                    }
-                }
-                if (ne >= B::kEdges)
-                    return -1;
-                int e = ne++;
-                E.ea[e] = (unsigned char)u;
-                E.eb[e] = (unsigned char)v;
-                E.ealive[e] = 1;
-                E.enext[e] = -1;
-                if (nan)
-                    continue;
-                unsigned h = 2166136261u;
-                for (int q = 0; q < 3; ++q)
-                    h = (h ^ ku[q]) * 16777619u;
-                for (int q = 0; q < 3; ++q)
-                    h = (h ^ kv[q]) * 16777619u;
-                for (int probe = 0; probe < B::kSlots; ++probe)
-                {
-                    HSlot &sl = E.slot[(h + probe) & (B::kSlots - 1)];
-                    if (sl.gen != gen)
-                    {
-                        sl.gen = gen;
-                        sl.key[0] = ku[0];
-                        sl.key[1] = ku[1];
-                        sl.key[2] = ku[2];
-                        sl.key[3] = kv[0];
-                        sl.key[4] = kv[1];
-                        sl.key[5] = kv[2];
-                        sl.head = sl.tail = e;
-                        break;
-                    }
-                    if (sl.key[0] == ku[0] && sl.key[1] == ku[1] && sl.key[2] == ku[2] && sl.key[3] == kv[0] &&
-                        sl.key[4] == kv[1] && sl.key[5] == kv[2])
-                    {
-                        if (sl.tail >= 0)
-                            E.enext[sl.tail] = e;
-                        else
-                            sl.head = e;
-                        sl.tail = e;
-                        break;
-                    }
-                }
-            }
-        }
-    }
-    return ne;
 }
 
 // ResolveCollision (code/nans.cpp:787-904) on one warp. Returns EPA_CONTACT with the contact
@@ -537,40 +410,6 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         __syncwarp();
         // horizon edges in face order
         int ne = 0;
-        if constexpr (B::kHash)
-        {
-            if (lane == 0)
-                ne = horizon_hash(E, nchunks);
-            ne = __shfl_sync(0xffffffffu, ne, 0);
-            __syncwarp();
-            if (ne < 0)
-                return EPA_OVERFLOW;
-            // keep the live edges in push order
-            int live = 0;
-            for (int base = 0; base < ne; base += 32)
-            {
-                int e = base + lane;
-                bool al = (e < ne) && E.ealive[e];
-                unsigned bal = __ballot_sync(0xffffffffu, al);
-                int dst = live + __popc(bal & ((1u << lane) - 1u));
-                unsigned char ta = 0, tb = 0;
-                if (al)
-                {
-                    ta = E.ea[e];
-                    tb = E.eb[e];
-                }
-                __syncwarp();
-                if (al)
-                {
-                    E.ea[dst] = ta;
-                    E.eb[dst] = tb;
-                }
-                __syncwarp();
-                live += __popc(bal);
-            }
-            ne = live;
-        }
-        else
         {
             bool ok = true;
             for (int ch = 0; ch < nchunks && ok; ++ch)
@@ -622,14 +461,6 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
             }
             __syncwarp();
             keep += __popc(sm);
-        }
-        if constexpr (B::kHash)
-        {
-            if (lane == 0)
-            {
-                atomicMax(w.epa_stats + 0, (unsigned)(keep + ne));
-                atomicMax(w.epa_stats + 1, (unsigned)ne);
-            }
         }
         if (keep + ne > B::kFaces)
             return EPA_OVERFLOW;
@@ -684,6 +515,7 @@ __device__ __forceinline__ void escalate(const DevWorld &w, int c, bool to_big)
     w.hit[c] = 0;
     if (!to_big)
     {
+        atomicAdd(w.epa_stats + 6, 1u);
         int q = atomicAdd(w.work_counter + 5, 1);
         if (q < w.med_cap)
         {
@@ -887,8 +719,36 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
     return EPA_NONE;
 }
 
-// Persistent: warps take 32 candidates at a time from a global queue; each lane runs GJK and,
-// on a hit, EPA; EPAs that outgrow the per-thread polytope are queued for the warp tier.
+// GJK then per-thread EPA for candidate c; with a budget below 65, a GJK still evolving is
+// queued for the long pass instead.
+__device__ __forceinline__ void narrow_one(const DevWorld &w, TinySmem &S, int t, int c, int budget)
+{
+    const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
+    GV s0, s1, s2, s3;
+    int g = gjk(w.verts, A, B, s0, s1, s2, s3, budget);
+    if (g == G_BUDGET)
+    {
+        w.long_cand[atomicAdd(w.work_counter + 7, 1)] = c;
+        return;
+    }
+    if (g != G_FOUND)
+    {
+        w.hit[c] = 0;
+        return;
+    }
+    v3 pa, pb, nn;
+    int r = epa_tiny(w, S, t, A, B, s0, s1, s2, s3, pa, pb, nn);
+    if (r == EPA_OVERFLOW)
+        escalate(w, c, false);
+    else
+        write_result(w, c, r, pa, pb, nn);
+}
+
+// Persistent: warps take 32 candidates at a time from a global queue; each lane runs GJK
+// (budget kGjkShort calls) and, on a hit, EPA; EPAs that outgrow the per-thread polytope are
+// queued for the warp tier, GJKs that need more calls for the long pass, so that the rare
+// long GJK runs share warps with each other instead of stalling 31 finished lanes.
+constexpr int kGjkShort = 8;
 __global__ void __launch_bounds__(kTinyThreads) k_narrow_tiny(DevWorld w)
 {
     __shared__ TinySmem S;
@@ -905,26 +765,23 @@ __global__ void __launch_bounds__(kTinyThreads) k_narrow_tiny(DevWorld w)
         const int c = base + lane;
         if (c >= n)
             continue;
-        const int a = w.cand_a[c], b = w.cand_b[c];
         const int sc = w.cand_meta[c] >> 3;
         if (c == 0 || (w.cand_meta[c - 1] >> 3) != sc)
             w.cand_begin[sc] = c;
         if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
             w.cand_end[sc] = c + 1;
-        const Shape A = load_shape(w, a), B = load_shape(w, b);
-        GV s0, s1, s2, s3;
-        if (gjk(w.verts, A, B, s0, s1, s2, s3) != G_FOUND)
-        {
-            w.hit[c] = 0;
-            continue;
-        }
-        v3 pa, pb, nn;
-        int r = epa_tiny(w, S, t, A, B, s0, s1, s2, s3, pa, pb, nn);
-        if (r == EPA_OVERFLOW)
-            escalate(w, c, false);
-        else
-            write_result(w, c, r, pa, pb, nn);
+        narrow_one(w, S, t, c, kGjkShort);
     }
+}
+
+// The long pass: candidates whose GJK needed more than kGjkShort calls, rerun in full.
+__global__ void __launch_bounds__(kTinyThreads) k_narrow_long(DevWorld w)
+{
+    __shared__ TinySmem S;
+    const int t = threadIdx.x;
+    const int n = w.work_counter[7];
+    for (int i = blockIdx.x * blockDim.x + t; i < n; i += gridDim.x * blockDim.x)
+        narrow_one(w, S, t, w.long_cand[i], 65);
 }
 
 // Tier 2: one warp per queued candidate, polytope of up to 128 faces in shared memory.
@@ -961,29 +818,506 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(
     }
 }
 
-// Tier 3: one warp per queued candidate, polytope in a per-warp global-memory arena.
-__global__ void __launch_bounds__(128) k_narrow_big(DevWorld w)
+// ------------------------------------------------------------------------------------
+// Tier 3: one block per queued candidate, polytope in a per-block global-memory arena.
+//
+// The horizon of a large polytope is built from counts instead of edge by edge. PushEdge
+// cancels the FIRST live stored edge that is the reverse of the pushed one and otherwise
+// appends. Group the pushes by their undirected key {P(u), P(v)} (positions compared with ==):
+// a push only ever cancels an edge of its own group, and the live edges of a group always run
+// in one direction (a push against them cancels one). So, per group, the survivors are exactly
+// the last |#(u,v) - #(v,u)| pushes of the majority direction; for a self-loop key
+// (P(u) == P(v)) the last push survives iff the group has an odd number of pushes; an edge
+// with a NaN coordinate equals nothing and always survives. Survivors keep push order.
+// Counting is parallel (hash table of groups); the "last n" ranks come from one ordered
+// reverse pass over the pushes in warp-sized chunks.
+// ------------------------------------------------------------------------------------
+struct EpaGiant
 {
-    const int lane = threadIdx.x & 31;
-    const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    EpaBig &E = *reinterpret_cast<EpaBig *>(w.epa_arena + (size_t)gwarp * sizeof(EpaBig));
+    float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
+    float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
+    float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
+    float fnx[kGiantFaces], fny[kGiantFaces], fnz[kGiantFaces], fd[kGiantFaces];
+    unsigned fidx[kGiantFaces];              // a | b << 8 | c << 16
+    unsigned vis[kGiantFaces / 32];
+    int chunk_pre[kGiantFaces / 32];
+    unsigned short push[kGiantPushes];       // u | v << 8
+    int pslot[kGiantPushes];                 // group slot, -1 for a NaN edge
+    unsigned char pdir[kGiantPushes];        // 0 / 1 orientation, 2 self-loop
+    unsigned char palive[kGiantPushes];
+    unsigned short edge[kGiantEdges];        // horizon: u | v << 8
+    unsigned long long skey[kGiantSlots];    // 0 = empty
+    int sfirst[kGiantSlots];
+    int scnt0[kGiantSlots], scnt1[kGiantSlots], squota[kGiantSlots];
+    unsigned char sqdir[kGiantSlots];
+};
+
+struct GiantShared
+{
+    float rd[32];
+    int ri[32];
+    int scan[32];
+    int bcast[4];
+};
+
+__device__ __forceinline__ v3 gpool(const EpaGiant &E, int i) { return mk3(E.px[i], E.py[i], E.pz[i]); }
+
+__device__ __forceinline__ void gpool_put(EpaGiant &E, int i, const GV &g)
+{
+    E.px[i] = g.p.x;
+    E.py[i] = g.p.y;
+    E.pz[i] = g.p.z;
+    E.ax[i] = g.sa.x;
+    E.ay[i] = g.sa.y;
+    E.az[i] = g.sa.z;
+    E.bx[i] = g.sb.x;
+    E.by[i] = g.sb.y;
+    E.bz[i] = g.sb.z;
+}
+
+__device__ __forceinline__ void gface_put(EpaGiant &E, int f, int a, int b, int c)
+{
+    v3 pa = gpool(E, a), pb = gpool(E, b), pc = gpool(E, c);
+    v3 n = normalize3(cross3(pb - pa, pc - pa));
+    if (dot3(pa, n) < 0.0f)
+        n = -1.0f * n;
+    E.fidx[f] = (unsigned)a | ((unsigned)b << 8) | ((unsigned)c << 16);
+    E.fnx[f] = n.x;
+    E.fny[f] = n.y;
+    E.fnz[f] = n.z;
+    E.fd[f] = fabsf(dot3(n, pa));
+}
+
+// Block-wide exclusive scan (blockDim a multiple of 32, at most 1024).
+__device__ __forceinline__ int gscan(int v, GiantShared &sh, int &total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        sh.scan[wid] = x;
+    __syncthreads();
+    if (wid == 0)
+    {
+        int t = (lane < nw) ? sh.scan[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o)
+                t += y;
+        }
+        if (lane < nw)
+            sh.scan[lane] = t;
+    }
+    __syncthreads();
+    int pre = (wid > 0 ? sh.scan[wid - 1] : 0) + x - v;
+    total = sh.scan[nw - 1];
+    __syncthreads();
+    return pre;
+}
+
+// Undirected group key of the edge (u, v): canonical positions ordered lexicographically.
+// Returns false for an edge with a NaN coordinate.
+__device__ __forceinline__ bool group_key(const EpaGiant &E, int u, int v, unsigned key[6], int &dir)
+{
+    v3 pu = gpool(E, u), pv = gpool(E, v);
+    if (isnan(pu.x) || isnan(pu.y) || isnan(pu.z) || isnan(pv.x) || isnan(pv.y) || isnan(pv.z))
+        return false;
+    unsigned ku[3] = {canon_bits(pu.x), canon_bits(pu.y), canon_bits(pu.z)};
+    unsigned kv[3] = {canon_bits(pv.x), canon_bits(pv.y), canon_bits(pv.z)};
+    int cmp = 0;
+    for (int q = 0; q < 3 && cmp == 0; ++q)
+        cmp = (ku[q] < kv[q]) ? -1 : (ku[q] > kv[q]) ? 1 : 0;
+    const unsigned *lo = (cmp <= 0) ? ku : kv, *hi = (cmp <= 0) ? kv : ku;
+    for (int q = 0; q < 3; ++q)
+    {
+        key[q] = lo[q];
+        key[3 + q] = hi[q];
+    }
+    dir = (cmp == 0) ? 2 : (cmp < 0 ? 0 : 1);
+    return true;
+}
+
+__device__ int epa_giant(const DevWorld &w, EpaGiant &E, GiantShared &sh, const Shape &A, const Shape &Bs, const GV &s0,
+                         const GV &s1, const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n)
+{
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
+    if (tid == 0)
+    {
+        gpool_put(E, 0, s0);
+        gpool_put(E, 1, s1);
+        gpool_put(E, 2, s2);
+        gpool_put(E, 3, s3);
+    }
+    __syncthreads();
+    if (tid == 0)
+        gface_put(E, 0, 0, 1, 2);
+    else if (tid == 1)
+        gface_put(E, 1, 0, 2, 3);
+    else if (tid == 2)
+        gface_put(E, 2, 0, 3, 1);
+    else if (tid == 3)
+        gface_put(E, 3, 1, 3, 2);
+    __syncthreads();
+    int nf = 4, nv = 4;
+    bool stale = false;
+    for (int it = 0; it <= 64; ++it)
+    {
+        if (nf == 0 && !stale)
+            return EPA_NONE;
+        // closest face (first minimum; a NaN face 0 stays the closest)
+        int ci = 0;
+        const float d0 = E.fd[0];
+        if (nf > 0 && !isnan(d0))
+        {
+            float bd = d0;
+            int bi = 0;
+            for (int f = tid; f < nf; f += nt)
+            {
+                float d = E.fd[f];
+                if (d < bd || (d == bd && f < bi))
+                {
+                    bd = d;
+                    bi = f;
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1)
+            {
+                float od = __shfl_xor_sync(0xffffffffu, bd, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (od < bd || (od == bd && oi < bi))
+                {
+                    bd = od;
+                    bi = oi;
+                }
+            }
+            if (lane == 0)
+            {
+                sh.rd[wid] = bd;
+                sh.ri[wid] = bi;
+            }
+            __syncthreads();
+            if (wid == 0)
+            {
+                bd = (lane < nw) ? sh.rd[lane] : d0;
+                bi = (lane < nw) ? sh.ri[lane] : 0;
+                for (int o = 16; o > 0; o >>= 1)
+                {
+                    float od = __shfl_xor_sync(0xffffffffu, bd, o);
+                    int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                    if (od < bd || (od == bd && oi < bi))
+                    {
+                        bd = od;
+                        bi = oi;
+                    }
+                }
+                if (lane == 0)
+                    sh.bcast[0] = bi;
+            }
+            __syncthreads();
+            ci = sh.bcast[0];
+            __syncthreads();
+        }
+        const float cur = E.fd[ci];
+        const v3 n = mk3(E.fnx[ci], E.fny[ci], E.fnz[ci]);
+        const GV ns = minkowski_support(w.verts, A, Bs, n);
+        if (dot3(n, ns.p) - cur < 0.001f)
+        {
+            unsigned fi = E.fidx[ci];
+            int ia = fi & 0xffu, ib = (fi >> 8) & 0xffu, ic = fi >> 16;
+            v3 pa = gpool(E, ia), pb = gpool(E, ib), pc = gpool(E, ic);
+            v3 p = cur * n;
+            v3 v0 = pb - pa, v1 = pc - pa, v2 = p - pa;
+            float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
+            float d20 = dot3(v2, v0), d21 = dot3(v2, v1);
+            float den = d00 * d11 - d01 * d01;
+            float bv = (d11 * d20 - d01 * d21) / den;
+            float bw = (d00 * d21 - d01 * d20) / den;
+            float bu = 1.0f - bv - bw;
+            if (fabsf(bu) > 1.0f || fabsf(bv) > 1.0f || fabsf(bw) > 1.0f)
+                return EPA_NONE;
+            if (!isfinite(bu) || !isfinite(bv) || !isfinite(bw))
+                return EPA_NONE;
+            v3 saa = mk3(E.ax[ia], E.ay[ia], E.az[ia]), sab = mk3(E.ax[ib], E.ay[ib], E.az[ib]),
+               sac = mk3(E.ax[ic], E.ay[ic], E.az[ic]);
+            v3 sba = mk3(E.bx[ia], E.by[ia], E.bz[ia]), sbb = mk3(E.bx[ib], E.by[ib], E.bz[ib]),
+               sbc = mk3(E.bx[ic], E.by[ic], E.bz[ic]);
+            out_pa = ((bu * saa) + (bv * sab)) + (bw * sac);
+            out_n = -1.0f * n;
+            out_pb = ((bu * sba) + (bv * sbb)) + (bw * sbc);
+            return EPA_CONTACT;
+        }
+        if (nf == 0)
+            return EPA_NONE;
+        // visibility bitmask, one 32-face chunk per warp at a time
+        const int nch = (nf + 31) >> 5;
+        for (int ch = wid; ch < nch; ch += nw)
+        {
+            int f = ch * 32 + lane;
+            bool vis = false;
+            if (f < nf)
+            {
+                v3 fa = gpool(E, E.fidx[f] & 0xffu);
+                vis = dot3(mk3(E.fnx[f], E.fny[f], E.fnz[f]), ns.p - fa) > 0.0f;
+            }
+            unsigned bal = __ballot_sync(0xffffffffu, vis);
+            if (lane == 0)
+                E.vis[ch] = bal;
+        }
+        __syncthreads();
+        // visible-face ranks: exclusive prefix of the chunk popcounts
+        int nvis = 0;
+        for (int base = 0; base < nch; base += nt)
+        {
+            int ch = base + tid;
+            int c = (ch < nch) ? __popc(E.vis[ch]) : 0;
+            int tot;
+            int pre = gscan(c, sh, tot);
+            if (ch < nch)
+                E.chunk_pre[ch] = nvis + pre;
+            nvis += tot;
+        }
+        const int m = 3 * nvis;
+        if (m > kGiantPushes)
+            return EPA_OVERFLOW;
+        __syncthreads();
+        for (int f = tid; f < nf; f += nt)
+        {
+            unsigned vm = E.vis[f >> 5];
+            int bit = f & 31;
+            if ((vm >> bit) & 1u)
+            {
+                int r = E.chunk_pre[f >> 5] + __popc(vm & ((1u << bit) - 1u));
+                unsigned fi = E.fidx[f];
+                unsigned a = fi & 0xffu, b = (fi >> 8) & 0xffu, c = fi >> 16;
+                E.push[3 * r] = (unsigned short)(a | (b << 8));
+                E.push[3 * r + 1] = (unsigned short)(b | (c << 8));
+                E.push[3 * r + 2] = (unsigned short)(c | (a << 8));
+            }
+        }
+        __syncthreads();
+        // group slots and counts
+        for (int k = tid; k < m; k += nt)
+        {
+            unsigned pk = E.push[k];
+            unsigned key[6];
+            int dir;
+            if (!group_key(E, pk & 0xffu, pk >> 8, key, dir))
+            {
+                E.pslot[k] = -1;
+                E.palive[k] = 1;
+                continue;
+            }
+            unsigned long long h = 1469598103934665603ull;
+            for (int q = 0; q < 6; ++q)
+                h = (h ^ key[q]) * 1099511628211ull;
+            h |= 1ull;
+            unsigned s = (unsigned)(h >> 20) & (kGiantSlots - 1);
+            for (int probe = 0; probe < kGiantSlots; ++probe)
+            {
+                unsigned long long prev = atomicCAS(&E.skey[s], 0ull, h);
+                if (prev == 0ull)
+                {
+                    E.sfirst[s] = k;
+                    break;
+                }
+                if (prev == h)
+                    break;
+                s = (s + 1) & (kGiantSlots - 1);
+            }
+            E.pslot[k] = (int)s;
+            E.pdir[k] = (unsigned char)dir;
+            atomicAdd(dir == 1 ? &E.scnt1[s] : &E.scnt0[s], 1);
+        }
+        if (tid == 0)
+            sh.bcast[1] = 0;
+        __syncthreads();
+        // equal 64-bit hashes must mean equal keys; and one thread per group sets its quota
+        for (int k = tid; k < m; k += nt)
+        {
+            int s = E.pslot[k];
+            if (s < 0)
+                continue;
+            int f = E.sfirst[s];
+            if (f != k)
+            {
+                unsigned ka[6], kb[6];
+                int da, db;
+                unsigned pk = E.push[k], pf = E.push[f];
+                group_key(E, pk & 0xffu, pk >> 8, ka, da);
+                group_key(E, pf & 0xffu, pf >> 8, kb, db);
+                for (int q = 0; q < 6; ++q)
+                    if (ka[q] != kb[q])
+                        sh.bcast[1] = 1;
+            }
+            else
+            {
+                int c0 = E.scnt0[s], c1 = E.scnt1[s];
+                if (E.pdir[k] == 2)
+                {
+                    E.squota[s] = c0 & 1;
+                    E.sqdir[s] = 2;
+                }
+                else
+                {
+                    int d = c0 - c1;
+                    E.squota[s] = d >= 0 ? d : -d;
+                    E.sqdir[s] = d >= 0 ? 0 : 1;
+                }
+            }
+        }
+        __syncthreads();
+        const bool collision = sh.bcast[1] != 0;
+        // survivors: the last `quota` pushes of the group's majority direction (reverse pass)
+        if (!collision && wid == 0)
+        {
+            for (int ch = (m - 1) >> 5; ch >= 0; --ch)
+            {
+                int k = ch * 32 + lane;
+                int s = (k < m) ? E.pslot[k] : -1;
+                bool cand = s >= 0 && E.pdir[k] == E.sqdir[s];
+                unsigned peers = __match_any_sync(0xffffffffu, cand ? s : -1 - lane);
+                int alive = 0;
+                if (cand)
+                {
+                    int later = __popc(peers & ~((2u << lane) - 1u));
+                    int leader = 31 - __clz(peers);
+                    int old = 0;
+                    if (lane == leader)
+                    {
+                        old = E.squota[s];
+                        E.squota[s] = old - __popc(peers);
+                    }
+                    old = __shfl_sync(peers, old, leader);
+                    alive = (old - later) > 0 ? 1 : 0;
+                }
+                if (s >= 0)
+                    E.palive[k] = (unsigned char)alive;
+            }
+        }
+        __syncthreads();
+        // clear the group table for the next iteration
+        for (int k = tid; k < m; k += nt)
+        {
+            int s = E.pslot[k];
+            if (s >= 0)
+            {
+                E.skey[s] = 0ull;
+                E.scnt0[s] = 0;
+                E.scnt1[s] = 0;
+            }
+        }
+        if (collision)
+            return EPA_OVERFLOW;
+        // horizon = surviving pushes in push order
+        int ne = 0;
+        for (int base = 0; base < m; base += nt)
+        {
+            int k = base + tid;
+            int al = (k < m) ? E.palive[k] : 0;
+            int tot;
+            int pre = gscan(al, sh, tot);
+            if (al && ne + pre < kGiantEdges)
+                E.edge[ne + pre] = E.push[k];
+            ne += tot;
+        }
+        if (ne > kGiantEdges)
+            return EPA_OVERFLOW;
+        // stable removal of the visible faces
+        int keep = 0;
+        for (int base = 0; base < nf; base += nt)
+        {
+            int f = base + tid;
+            bool stay = (f < nf) && !((E.vis[f >> 5] >> (f & 31)) & 1u);
+            int tot;
+            int pre = gscan(stay ? 1 : 0, sh, tot);
+            float nx = 0.f, ny = 0.f, nz = 0.f, d = 0.f;
+            unsigned fi = 0;
+            if (stay)
+            {
+                nx = E.fnx[f];
+                ny = E.fny[f];
+                nz = E.fnz[f];
+                d = E.fd[f];
+                fi = E.fidx[f];
+            }
+            __syncthreads();
+            if (stay)
+            {
+                int dst = keep + pre;
+                E.fnx[dst] = nx;
+                E.fny[dst] = ny;
+                E.fnz[dst] = nz;
+                E.fd[dst] = d;
+                E.fidx[dst] = fi;
+            }
+            keep += tot;
+            __syncthreads();
+        }
+        if (tid == 0)
+        {
+            atomicMax(w.epa_stats + 0, (unsigned)(keep + ne));
+            atomicMax(w.epa_stats + 1, (unsigned)ne);
+        }
+        if (keep + ne > kGiantFaces)
+            return EPA_OVERFLOW;
+        if (keep == 0 && ne == 0)
+        {
+            // every face removed: slot 0 keeps the last face of the list (nothing was moved)
+            if (tid == 0)
+            {
+                int l = nf - 1;
+                E.fidx[0] = E.fidx[l];
+                E.fnx[0] = E.fnx[l];
+                E.fny[0] = E.fny[l];
+                E.fnz[0] = E.fnz[l];
+                E.fd[0] = E.fd[l];
+            }
+            stale = true;
+        }
+        const int sv = nv++;
+        if (tid == 0)
+            gpool_put(E, sv, ns);
+        __syncthreads();
+        for (int j = tid; j < ne; j += nt)
+        {
+            unsigned ed = E.edge[j];
+            gface_put(E, keep + j, sv, ed & 0xffu, ed >> 8);
+        }
+        __syncthreads();
+        nf = keep + ne;
+    }
+    return EPA_NONE;
+}
+
+__global__ void __launch_bounds__(kGiantThreads) k_narrow_big(DevWorld w)
+{
+    __shared__ GiantShared sh;
+    __shared__ int s_q;
+    EpaGiant &E = *reinterpret_cast<EpaGiant *>(w.epa_arena + (size_t)blockIdx.x * sizeof(EpaGiant));
     const int n = min(w.work_counter[3], w.ovf_cap);
     for (;;)
     {
-        int q = 0;
-        if (lane == 0)
-            q = atomicAdd(w.work_counter + 2, 1);
-        q = __shfl_sync(0xffffffffu, q, 0);
+        if (threadIdx.x == 0)
+            s_q = atomicAdd(w.work_counter + 2, 1);
+        __syncthreads();
+        const int q = s_q;
+        __syncthreads();
         if (q >= n)
             break;
         const int cc = w.ovf_cand[q];
         const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
         GV s0, s1, s2, s3;
-        gjk(w.verts, A, B, s0, s1, s2, s3);
+        gjk(w.verts, A, B, s0, s1, s2, s3); // every thread: same inputs, same simplex
         v3 pa, pb, nn;
-        int r = epa_run(w, E, A, B, s0, s1, s2, s3, pa, pb, nn, lane);
-        __syncwarp();
-        if (lane == 0)
+        int r = epa_giant(w, E, sh, A, B, s0, s1, s2, s3, pa, pb, nn);
+        __syncthreads();
+        if (threadIdx.x == 0)
         {
             atomicAdd(w.epa_stats + 2, 1u);
             if (r == EPA_OVERFLOW)
@@ -998,10 +1332,12 @@ __global__ void __launch_bounds__(128) k_narrow_big(DevWorld w)
             }
             write_result(w, cc, r, pa, pb, nn);
         }
+        __syncthreads();
     }
 }
 
-size_t epa_big_bytes() { return sizeof(EpaBig); }
+size_t epa_big_bytes() { return sizeof(EpaGiant); }
+
 
 static size_t medium_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }
 
@@ -1022,15 +1358,26 @@ int narrow_blocks_per_sm(int warps)
     return per;
 }
 
-void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
+void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w)
 {
-    (void)warps;
-    narrow_attrs();
     k_narrow_tiny<<<grid, kTinyThreads, 0, st>>>(w);
+    k_narrow_long<<<grid, kTinyThreads, 0, st>>>(w);
+}
+
+void launch_epa_medium(cudaStream_t st, const DevWorld &w)
+{
+    narrow_attrs();
     k_epa_medium<4><<<w.medium_blocks, 128, medium_smem(4), st>>>(w);
 }
 
-void launch_narrow_big(cudaStream_t st, const DevWorld &w) { k_narrow_big<<<w.epa_arena_warps / 4, 128, 0, st>>>(w); }
+void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
+{
+    (void)warps;
+    launch_narrow_tiny(grid, st, w);
+    launch_epa_medium(st, w);
+}
+
+void launch_narrow_big(cudaStream_t st, const DevWorld &w) { k_narrow_big<<<w.epa_arena_warps, kGiantThreads, 0, st>>>(w); }
 
 void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
 {

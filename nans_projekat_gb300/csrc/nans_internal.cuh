@@ -81,9 +81,10 @@ struct DevWorld
     float4 *c_pa, *c_pb, *c_n;
     int *work_counter;                  // [0] narrowphase head, [1] solver head, [2] large-EPA
                                         // head, [3] large-EPA queue length, [5] warp-EPA queue
-                                        // length, [6] warp-EPA head
+                                        // length, [6] warp-EPA head, [7] long-GJK queue length
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
+    int *long_cand;                     // candidates whose GJK needs the long pass
     int medium_blocks;                  // warp-tier grid
     int ovf_cap;                        // large-EPA queue capacity
     int *ovf_cand;                      // candidates queued for the large-polytope tier
@@ -91,7 +92,8 @@ struct DevWorld
     int epa_arena_warps;
     unsigned *epa_stats;                // [0] max faces, [1] max horizon edges, [2] slow-path EPAs,
                                         // [3] overflowing candidate + 1, [4] its scene + 1,
-                                        // [5] EPAs that outgrew the slow path
+                                        // [5] EPAs that outgrew the slow path, [6] EPAs
+                                        // escalated to the warp tier
     // solver scratch, per candidate slot
     int *s_order, *s_wave, *s_perm, *s_wcnt;
     float4 *s_k;                        // 9 float4 of per-contact constants

@@ -25,20 +25,24 @@ constexpr int kPairsPerBlock = kCullThreads * kPairsPerThread;
 // reference's polytope is not always convex: with bodies flung to large coordinates the
 // supports repeat existing vertices, faces degenerate (NaN normals, never removed) and the
 // list keeps growing, at times geometrically, for all 65 iterations. On the 16,384-scene
-// stack workload ~4 EPAs in a million exceed 128 faces; the largest met so far (scene 10198,
-// step 135) reaches 485,688 faces and a 139,111-edge horizon, which the reference's own
-// algorithm needs 334 s of one CPU core to finish. The fast path keeps 128 faces / 32 edges per
-// warp in shared memory; an EPA that outgrows it is rerun by k_narrow_big in a per-warp
-// global-memory arena (2,097,152 faces, 524,288 edges, an O(1)-per-push horizon). Beyond that
-// the step reports NANS_ERR_EPA_CAPACITY.
+// stack workload ~2 EPAs in a thousand outgrow 12 vertices / 20 faces, ~4 in a million exceed
+// 128 faces, and the largest met so far (scene 10198, step 135) reaches 485,688 faces and a
+// 139,111-edge horizon (the reference's own algorithm needs 334 s of one CPU core for it).
+// Tier 1 runs EPA per thread (12 vertices, 20 faces, 12 edges); tier 2 per warp in shared
+// memory (128 faces, 32 edges); tier 3 per block in a global-memory arena (2,097,152 faces,
+// 4,194,304 horizon pushes, 1,048,576 horizon edges). Beyond that the pair gets no contact
+// and the event is counted (NANS_ERR_EPA_CAPACITY in strict worlds).
 constexpr int kEpaMaxVerts = 72;
 constexpr int kEpaFastFaces = 128;
 constexpr int kEpaFastEdges = 32;
-constexpr int kEpaBigFaces = 1 << 21;
-constexpr int kEpaBigEdges = 1 << 19;
-constexpr int kEpaArenaWarps = 16;     // slow-path warps (each with its own ~78 MB arena)
-constexpr int kEpaOverflowCap = 65536; // large-polytope EPAs queued per step
-constexpr int kEpaMediumCap = 1 << 20;  // warp-tier EPAs queued per step
+constexpr int kGiantFaces = 1 << 21;
+constexpr int kGiantPushes = 1 << 22;
+constexpr int kGiantEdges = 1 << 20;
+constexpr int kGiantSlots = 1 << 23;   // group table, load factor <= 1/2
+constexpr int kGiantThreads = 512;
+constexpr int kEpaArenaWarps = 4;      // tier-3 blocks, one ~330 MB arena each
+constexpr int kEpaOverflowCap = 65536; // tier-3 EPAs queued per step
+constexpr int kEpaMediumCap = 1 << 20; // tier-2 EPAs queued per step
 
 __global__ void k_sweep(DevWorld w, float pending_dt, float dt, int flags);
 __global__ void k_unpack(DevWorld w, const float *rec_cube, const float *rec_sphere, const float *rec_floor,
@@ -57,6 +61,8 @@ size_t epa_big_bytes();
 void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w);
 void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w);
 void launch_narrow_big(cudaStream_t st, const DevWorld &w);
+void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
+void launch_epa_medium(cudaStream_t st, const DevWorld &w);
 __global__ void k_solve(DevWorld w, float dt);
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);
 

@@ -235,18 +235,18 @@ class World:
         return a.value, b.value
 
     def profile(self, dt, n):
-        """Device milliseconds per stage summed over n steps: sweep, cull, narrowphase,
-        large-polytope EPA, solver."""
-        ms = np.zeros(5, np.float32)
+        """Device milliseconds per stage summed over n steps: sweep, cull, narrowphase
+        (GJK + per-thread EPA), warp-tier EPA, large-polytope EPA, solver."""
+        ms = np.zeros(6, np.float32)
         _check(self.lib.nans_profile_steps(self.h, dt, n, _ptr(ms)))
         return ms
 
     def epa_stats(self, reset=False):
-        out = np.zeros(6, np.uint32)
+        out = np.zeros(7, np.uint32)
         _check(self.lib.nans_world_epa_stats(self.h, _ptr(out), 1 if reset else 0))
         return dict(max_faces=int(out[0]), max_edges=int(out[1]), slow_epas=int(out[2]),
                     overflow_candidate=int(out[3]) - 1, overflow_scene=int(out[4]) - 1,
-                    overflows=int(out[5]))
+                    overflows=int(out[5]), warp_tier=int(out[6]))
 
     @property
     def n_bodies(self):

@@ -20,6 +20,8 @@
 #include <atomic>
 #include <algorithm>
 #include <string>
+#include <array>
+#include <map>
 #include <cstdio>
 #include <cstdlib>
 
@@ -519,6 +521,9 @@ static std::atomic<long long> g_epa_stale(0);     // EPAs that read the emptied 
 static std::atomic<long long> g_epa_big_contact(0); // EPAs above 1024 faces that returned a contact
 static std::atomic<long long> g_epa_iter_hist[5];  // EPAs ending after 1-4, 5-8, 9-16, 17-64, 65 iterations
 static std::atomic<long long> g_gjk_iters(0), g_gjk_calls(0);
+static std::atomic<long long> g_epa_tiny_fit[4]; // EPAs that fit (V<=12,F<=20,E<=12), exceed V, F, E
+static std::atomic<int> g_epa_hist_faces[64];
+static std::atomic<long long> g_gjk_hist[8]; // GJK runs by evolve calls: 1,2,3-4,5-8,9-16,17-32,33-64,65 + result
 static void atomic_max(std::atomic<int> &a, int v)
 {
     int cur = a.load();
@@ -533,10 +538,18 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
     struct BigCount
     {
         size_t peak = 0;
+        size_t peak_edges = 0;
         bool contact = false;
         int iters = 65;
         ~BigCount()
         {
+            int verts = 4 + iters - 1; // supports added before the final iteration
+            bool v_ok = verts <= 12, f_ok = peak <= 20, e_ok = peak_edges <= 12;
+            if (v_ok && f_ok && e_ok) g_epa_tiny_fit[0].fetch_add(1);
+            if (!v_ok) g_epa_tiny_fit[1].fetch_add(1);
+            if (!f_ok) g_epa_tiny_fit[2].fetch_add(1);
+            if (!e_ok) g_epa_tiny_fit[3].fetch_add(1);
+            g_epa_hist_faces[peak < 63 ? peak : 63].fetch_add(1);
             int b = iters <= 4 ? 0 : iters <= 8 ? 1 : iters <= 16 ? 2 : iters <= 64 ? 3 : 4;
             g_epa_iter_hist[b].fetch_add(1);
             if (peak > 1024 && contact) g_epa_big_contact.fetch_add(1);
@@ -624,12 +637,39 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             snprintf(buf, sizeof(buf), "it %d faces %zu nan %d visible %d closest %zu cur %.9g gap %.9g dupS %d",
                      it, F.size(), nanf, vis, ci, (double)cur, (double)(dot(cf.n, ns.P) - cur), dup);
             trace.push_back(buf);
-            if (F.size() > 600)
+            if (F.size() > 50000)
             {
-                for (auto &l : trace)
-                    fprintf(stderr, "%s\n", l.c_str());
-                fprintf(stderr, "----\n");
-                abort();
+                // group sizes of the horizon pushes by undirected P-edge key
+                std::vector<std::pair<std::array<float, 6>, int>> keys;
+                for (auto &f : F)
+                    if (dot(f.n, sub(ns.P, f.a.P)) > T(0))
+                    {
+                        const Vx<T> *vv[4] = {&f.a, &f.b, &f.c, &f.a};
+                        for (int k = 0; k < 3; ++k)
+                        {
+                            std::array<float, 6> a = {(float)vv[k]->P.x, (float)vv[k]->P.y, (float)vv[k]->P.z,
+                                                      (float)vv[k + 1]->P.x, (float)vv[k + 1]->P.y, (float)vv[k + 1]->P.z};
+                            std::array<float, 6> b = {a[3], a[4], a[5], a[0], a[1], a[2]};
+                            keys.push_back({std::min(a, b), 0});
+                        }
+                    }
+                std::sort(keys.begin(), keys.end());
+                std::map<int, long> hist;
+                for (size_t i = 0; i < keys.size();)
+                {
+                    size_t j = i;
+                    while (j < keys.size() && keys[j].first == keys[i].first)
+                        ++j;
+                    hist[(int)std::min<size_t>(j - i, 64)]++;
+                    i = j;
+                }
+                fprintf(stderr, "it %d faces %zu pushes %zu groups:", it, F.size(), keys.size());
+                for (auto &h : hist)
+                    fprintf(stderr, " %d:%ld", h.first, h.second);
+                fprintf(stderr, "\n");
+                static int printed = 0;
+                if (++printed >= 4)
+                    abort();
             }
         }
 #endif
@@ -665,6 +705,8 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             ++i;
         }
         atomic_max(g_epa_max_edges, (int)E.size());
+        big.peak_edges = std::max(big.peak_edges, E.size());
+        big.peak = std::max(big.peak, F.size() + E.size());
         if (F.empty() && E.empty())
         {
             g_epa_stale.fetch_add(1);
@@ -688,6 +730,10 @@ template <class T> static bool check_collision(const PairCtx<T> &p, Contact<T> &
         r = evolve(p, S);
     g_gjk_iters.fetch_add(it);
     g_gjk_calls.fetch_add(1);
+    {
+        int b = it <= 1 ? 0 : it <= 2 ? 1 : it <= 4 ? 2 : it <= 8 ? 3 : it <= 16 ? 4 : it <= 32 ? 5 : it <= 64 ? 6 : 7;
+        g_gjk_hist[b].fetch_add(1);
+    }
     if (r == Found)
         return epa(p, S, c);
     return false;
@@ -1178,7 +1224,10 @@ void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
 // [2] max iteration index, [3] EPA calls, [4..7] EPAs whose face list exceeded
 // 128, 256, 1024, 4096 faces, [8] of those above 128 with a NaN face 0, [9] EPAs whose
 // face list emptied, [10] EPAs above 1024 faces that returned a contact, [11..15] EPAs that
-// ended after 1-4, 5-8, 9-16, 17-64, 65 iterations, [16] GJK evolve calls, [17] GJK runs.
+// ended after 1-4, 5-8, 9-16, 17-64, 65 iterations, [16] GJK evolve calls, [17] GJK runs,
+// [18..21] EPAs fitting 12 vertices / 20 faces / 12 edges, exceeding each, [22..85] EPAs by
+// peak face count (after removal plus new faces), [86..93] GJK runs by evolve calls
+// (1, 2, 3-4, 5-8, 9-16, 17-32, 33-64, 65).
 void nanso_epa_stats(long long *out, int reset)
 {
     out[0] = g_epa_max_faces.load();
@@ -1194,6 +1243,12 @@ void nanso_epa_stats(long long *out, int reset)
         out[11 + i] = g_epa_iter_hist[i].load();
     out[16] = g_gjk_iters.load();
     out[17] = g_gjk_calls.load();
+    for (int i = 0; i < 4; ++i)
+        out[18 + i] = g_epa_tiny_fit[i].load();
+    for (int i = 0; i < 64; ++i)
+        out[22 + i] = g_epa_hist_faces[i].load();
+    for (int i = 0; i < 8; ++i)
+        out[86 + i] = g_gjk_hist[i].load();
     if (reset)
     {
         g_epa_big_contact = 0;
@@ -1201,6 +1256,12 @@ void nanso_epa_stats(long long *out, int reset)
             g_epa_iter_hist[i] = 0;
         g_gjk_iters = 0;
         g_gjk_calls = 0;
+        for (int i = 0; i < 4; ++i)
+            g_epa_tiny_fit[i] = 0;
+        for (int i = 0; i < 64; ++i)
+            g_epa_hist_faces[i] = 0;
+        for (int i = 0; i < 8; ++i)
+            g_gjk_hist[i] = 0;
         g_epa_stale = 0;
         g_epa_big_nan0 = 0;
         for (int i = 0; i < 4; ++i)

@@ -125,8 +125,10 @@ def sincos(x):
 
 
 def epa_stats(reset=True):
-    out = np.zeros(18, np.int64)
+    out = np.zeros(94, np.int64)
     lib().nanso_epa_stats(_ptr(out), 1 if reset else 0)
     return dict(max_faces=int(out[0]), max_edges=int(out[1]), max_iter=int(out[2]), calls=int(out[3]),
                 over128=int(out[4]), over256=int(out[5]), over1024=int(out[6]), over4096=int(out[7]), over128_nan_face0=int(out[8]), emptied=int(out[9]), over1024_contact=int(out[10]),
-                epa_iter_hist=[int(x) for x in out[11:16]], gjk_evolves=int(out[16]), gjk_runs=int(out[17]))
+                epa_iter_hist=[int(x) for x in out[11:16]], gjk_evolves=int(out[16]), gjk_runs=int(out[17]),
+                tiny_fit=[int(x) for x in out[18:22]], faces_hist=[int(x) for x in out[22:86]],
+                gjk_hist=[int(x) for x in out[86:94]])
