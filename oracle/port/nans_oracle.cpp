@@ -513,6 +513,9 @@ template <class T> static bool finite(T x) { return !(std::isnan(x) || std::isin
 
 // EPA size statistics (max faces, max horizon edges, max iterations), for sizing the
 // device's shared-memory buffers.
+// Statistics are off unless nanso_stats_enable(1) is called: the shared counters would
+// otherwise serialise the host threads of a timed run.
+static bool g_stats = false;
 static std::atomic<int> g_epa_max_faces(0), g_epa_max_edges(0), g_epa_max_iters(0);
 static std::atomic<long long> g_epa_calls(0);
 static std::atomic<long long> g_epa_big[4]; // EPAs whose face list exceeded 128, 256, 1024, 4096
@@ -534,7 +537,8 @@ static void atomic_max(std::atomic<int> &a, int v)
 
 template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>> &S, Contact<T> &out)
 {
-    g_epa_calls.fetch_add(1);
+    if (g_stats)
+        g_epa_calls.fetch_add(1);
     struct BigCount
     {
         size_t peak = 0;
@@ -543,6 +547,8 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
         int iters = 65;
         ~BigCount()
         {
+            if (!g_stats)
+                return;
             int verts = 4 + iters - 1; // supports added before the final iteration
             bool v_ok = verts <= 12, f_ok = peak <= 20, e_ok = peak_edges <= 12;
             if (v_ok && f_ok && e_ok) g_epa_tiny_fit[0].fetch_add(1);
@@ -597,11 +603,14 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             out.pb = add(add(mul(u, stale.a.SupB), mul(v, stale.b.SupB)), mul(w, stale.c.SupB));
             return true;
         }
-        atomic_max(g_epa_max_faces, (int)F.size());
-        if (F.size() > 128 && big.peak <= 128 && std::isnan(std::fabs(dot(F[0].n, F[0].a.P))))
-            g_epa_big_nan0.fetch_add(1);
+        if (g_stats)
+        {
+            atomic_max(g_epa_max_faces, (int)F.size());
+            if (F.size() > 128 && big.peak <= 128 && std::isnan(std::fabs(dot(F[0].n, F[0].a.P))))
+                g_epa_big_nan0.fetch_add(1);
+            atomic_max(g_epa_max_iters, it);
+        }
         big.peak = std::max(big.peak, F.size());
-        atomic_max(g_epa_max_iters, it);
         big.iters = it + 1;
         T cur = std::fabs(dot(F[0].n, F[0].a.P));
         size_t ci = 0;
@@ -704,12 +713,14 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
             }
             ++i;
         }
-        atomic_max(g_epa_max_edges, (int)E.size());
+        if (g_stats)
+            atomic_max(g_epa_max_edges, (int)E.size());
         big.peak_edges = std::max(big.peak_edges, E.size());
         big.peak = std::max(big.peak, F.size() + E.size());
         if (F.empty() && E.empty())
         {
-            g_epa_stale.fetch_add(1);
+            if (g_stats)
+                g_epa_stale.fetch_add(1);
             has_stale = true;
             stale = last_face;
         }
@@ -728,9 +739,10 @@ template <class T> static bool check_collision(const PairCtx<T> &p, Contact<T> &
     int it = 0;
     for (; r == Evolving && it <= 64; ++it)
         r = evolve(p, S);
-    g_gjk_iters.fetch_add(it);
-    g_gjk_calls.fetch_add(1);
+    if (g_stats)
     {
+        g_gjk_iters.fetch_add(it);
+        g_gjk_calls.fetch_add(1);
         int b = it <= 1 ? 0 : it <= 2 ? 1 : it <= 4 ? 2 : it <= 8 ? 3 : it <= 16 ? 4 : it <= 32 ? 5 : it <= 64 ? 6 : 7;
         g_gjk_hist[b].fetch_add(1);
     }
@@ -1219,6 +1231,9 @@ void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
     else
         w->sf[scene].k = Consts{cr, cf, iters};
 }
+
+// Turns the EPA / GJK statistics on or off (off by default).
+void nanso_stats_enable(int on) { g_stats = on != 0; }
 
 // EPA size statistics since the last reset: out[0] max faces, [1] max edges,
 // [2] max iteration index, [3] EPA calls, [4..7] EPAs whose face list exceeded

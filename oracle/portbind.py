@@ -50,6 +50,7 @@ def lib():
         L.nanso_set_constants.argtypes = [_P, _I, _F, _F, _I]
         L.nanso_sincosf.argtypes = [_P, _P, _P, _I]
         L.nanso_epa_stats.argtypes = [_P, _I]
+        L.nanso_stats_enable.argtypes = [_I]
         _LIB = L
     return _LIB
 
@@ -124,7 +125,12 @@ def sincos(x):
     return s, c
 
 
+def stats_enable(on=True):
+    lib().nanso_stats_enable(1 if on else 0)
+
+
 def epa_stats(reset=True):
+    """EPA / GJK statistics collected while stats_enable(True) is on."""
     out = np.zeros(94, np.int64)
     lib().nanso_epa_stats(_ptr(out), 1 if reset else 0)
     return dict(max_faces=int(out[0]), max_edges=int(out[1]), max_iter=int(out[2]), calls=int(out[3]),
