@@ -158,6 +158,15 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def measured_traffic(kernel):
+    """DRAM bytes per launch of a kernel from the committed ncu summary, or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    return None
+
+
 def measured_peaks():
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -360,12 +369,12 @@ def run_ours(args):
                               "warp_tier_epas": epa["warp_tier"]},
             },
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
-                         "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "unit": "GB/s", "frac": achieved / peak, "traffic": measured_traffic(names[dom]),
                          "peak_source": peak_kind + " hbm_gbs",
                          "bytes_per_launch": dom_bytes,
                          "stage_ms": {n: float(x) for n, x in zip(names, stage_ms)},
                          "sweep": {"achieved": sweep_gbs, "frac": sweep_gbs / peak,
-                                   "bytes_per_launch": sweep_bytes}},
+                                   "bytes_per_launch": sweep_bytes, "traffic": measured_traffic("k_sweep")}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(rec_bytes),
                     "d2h_bytes_per_step": int(rec_bytes + pin_f.nbytes),
                     "path": "nans_world_set_state + nans_batch_step(1) + nans_world_download, pinned host"},
