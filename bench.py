@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="skip the plain-path and single-large-scene measurements")
     return p.parse_args()
 
 
@@ -272,6 +274,50 @@ def run_reference_arm(args):
     print(json.dumps(line, default=_jsonable))
 
 
+def secondary_measurements(lib, batch, device):
+    """Plain path vs batched path on the same scenes, and the single large scene."""
+    import torch
+    from nans_projekat_gb300 import scenes
+    out = {}
+    # plain drop-in: one world per scene, stepped with nans_step (stage-by-stage launches and
+    # one synchronisation per call), on every 256th scene of the batched workload
+    sample = batch[::256]
+    worlds = []
+    for sc in sample:
+        wd = lib.World(device=device)
+        wd.upload(sc)
+        wd.step(DT, 2)
+        worlds.append(wd)
+    n = 20
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for wd in worlds:
+        wd.step(DT, n)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    bodies = sum(s.n_bodies for s in sample)
+    out["plain_path"] = {"value": bodies * n / t, "unit": UNIT, "scenes": len(sample), "steps": n,
+                         "sample": "every 256th scene of the workload, one world per scene, nans_step"}
+    for wd in worlds:
+        wd.close()
+    # one large scene: 4,096 boxes + 512 spheres in a 64^3 m box, plain path
+    big = scenes.random_scene(1)
+    wb = lib.World(device=device)
+    wb.upload(big)
+    wb.step(DT, 3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n = 60
+    wb.step(DT, n)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    out["large_scene_plain"] = {"value": big.n_bodies * n / t, "unit": UNIT, "bodies": big.n_bodies,
+                                "steps": n, "ms_per_step": 1000.0 * t / n,
+                                "workload": "random4608: 4,096 boxes + 512 spheres, 64^3 m box, plain path"}
+    wb.close()
+    return out
+
+
 def run_ours(args):
     import torch
     dist, rank, ws = dist_init()
@@ -347,6 +393,10 @@ def run_ours(args):
     rec_bytes = cubes.nbytes + spheres.nbytes
     launches_batched, _ = w.launches_per_step()
 
+    secondary = None
+    if rank == 0 and not args.no_secondary:
+        secondary = secondary_measurements(lib, batch, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_sample_rate(batch, args.cpu_seconds, os.cpu_count() or 1, "port")
@@ -379,6 +429,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": int(rec_bytes + pin_f.nbytes),
                     "path": "nans_world_set_state + nans_batch_step(1) + nans_world_download, pinned host"},
             "gpu_launches": int(launches_batched * args.steps),
+            "secondary": secondary,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
