@@ -1,0 +1,47 @@
+"""CPU test of bench.py's multi-rank plumbing with gloo and two ranks: every rank steps its own
+scene shard, the timed region uses the slowest rank, totals are summed."""
+import os
+import socket
+
+import pytest
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, ws, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws))
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    dist, r, n = bench.dist_init()
+    assert (r, n) == (rank, ws)
+    bench.barrier(dist)
+    slowest = bench.max_over_ranks(dist, float(10 + rank))
+    total = bench.sum_over_ranks(dist, float(100 * (rank + 1)))
+    shard = bench.make_workload(8, rank)
+    q.put((rank, slowest, total, shard[0].cubes["Position"].tobytes()))
+    dist.destroy_process_group()
+
+
+def test_two_rank_gloo_aggregation():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = [q.get(timeout=120) for _ in procs]
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    res.sort()
+    assert [r[1] for r in res] == [11.0, 11.0]        # max over ranks
+    assert [r[2] for r in res] == [300.0, 300.0]      # sum over ranks
+    assert res[0][3] != res[1][3]                     # independent shards per rank
