@@ -100,6 +100,7 @@ typedef struct nans_contact_pair
 #define NANS_ERR_EPA_CAPACITY 5     /* an EPA polytope outgrew its buffers (strict worlds) */
 #define NANS_ERR_NOT_UPLOADED 6     /* the world holds no scene yet */
 #define NANS_ERR_SCENE_TOO_LARGE 7  /* a scene has more bodies than the solver supports */
+#define NANS_ERR_NO_TAPE 8          /* nans_diff_backward without a current forward tape */
 
 /* ---- world ------------------------------------------------------------------------- */
 
@@ -206,6 +207,49 @@ int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain
 
 /* The project sine/cosine used by the Model rebuild, evaluated on the device (n values). */
 int nans_device_sincos(const float *x, float *s, float *c, uint32_t n);
+
+/* ---- differentiable rollout --------------------------------------------------------- */
+
+/* No counterpart in the reference, which computes no gradients. nans_diff_forward runs nsteps
+ * plain steps (the same kernels and results as nans_step, bit for bit) and keeps, in device
+ * memory, a tape of what the adjoint needs: per step the velocities before RK4 and, per
+ * contact, the solver's constants, relative velocities, applied impulses and active set.
+ * Tape size per step: 32 bytes per dynamic body plus 192 bytes per candidate pair.
+ *
+ * nans_diff_backward then returns the gradient of a loss L of the final state (the state
+ * nans_world_download returns) with respect to the initial state, the masses and the solver
+ * constants. The gradient is that of the rollout with each step's contact set and contact
+ * geometry (normals, contact points, depths) held at their forward values; within that, it
+ * is exact (up to FP32 rounding): the solver's impulses are differentiated through their
+ * closed form (normal impulse max(Ln, 0), friction clamped to +-sqrt(2) Cf Ln) on the active
+ * set of the forward pass, and RK4 through its exact polynomial form. Under that model, dL/d
+ * initial position and angles equal dL/d final position and angles. Mass gradients take the
+ * moment of inertia as proportional to the mass (fixed shape).
+ *
+ * Per-body arrays are float[n][3] (d_mass: float[n]) in record order: the cubes of all scenes
+ * in upload order, then the spheres. Per-scene arrays hold one float per scene. Input
+ * pointers may be NULL (zero); output pointers may be NULL (not wanted). The tape stays valid
+ * until the next step, upload, set_state or forward; the backward may run several times. */
+typedef struct nans_diff_grads
+{
+    const float *dl_position;  /* in: dL/d final Position */
+    const float *dl_angles;    /* in: dL/d final Angles */
+    const float *dl_velocity;  /* in: dL/d final V */
+    const float *dl_omega;     /* in: dL/d final W */
+    float *position0;          /* out: dL/d initial Position */
+    float *angles0;            /* out: dL/d initial Angles */
+    float *velocity0;          /* out: dL/d initial V */
+    float *omega0;             /* out: dL/d initial W */
+    float *mass;               /* out: dL/d Mass */
+    float *restitution;        /* out, per scene: dL/d Cr */
+    float *friction;           /* out, per scene: dL/d Cf */
+} nans_diff_grads;
+
+int nans_diff_forward(nans_world *world, const nans_step_params *params, float dt, uint32_t nsteps);
+int nans_diff_backward(nans_world *world, const nans_diff_grads *grads);
+
+/* Steps and device bytes held by the current tape. */
+int nans_diff_tape_info(nans_world *world, uint32_t *steps, uint64_t *bytes);
 
 /* ---- allocation-free solve -------------------------------------------------------- */
 

@@ -25,7 +25,7 @@ NVCC_FLAGS = ARCH + [
     "-I", CSRC, "-I", INCLUDE,
 ]
 
-SOURCES = ["k_sweep.cu", "k_cull.cu", "k_narrow.cu", "k_solve.cu", "api.cu", "noalloc.cu"]
+SOURCES = ["k_sweep.cu", "k_cull.cu", "k_narrow.cu", "k_solve.cu", "k_adjoint.cu", "api.cu", "noalloc.cu"]
 
 
 def nvcc():

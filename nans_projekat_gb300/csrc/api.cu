@@ -96,6 +96,22 @@ struct nans_world
     int g_steps = 0;
     float g_dt = 0.0f;
     int g_cfg = -1;
+
+    // differentiable rollout: the tape lives in a chunked device arena reused across forwards
+    bool tape_on = false;           // the solve records its adjoint data (s_fwd, s_maxw)
+    bool tape_valid = false;        // the tape describes the rollout that led to the state
+    float tape_dt = 0.0f;
+    float4 *fwd_buf = nullptr;      // 2 float4 per candidate slot (in cand_allocs)
+    int *d_maxw = nullptr;          // per scene (in allocs)
+    std::vector<void *> tape_chunks;
+    std::vector<size_t> tape_sizes;
+    size_t tape_chunk = 0, tape_off = 0, tape_bytes = 0;
+    std::vector<TapeStep> tape;
+    TapeStep *d_tape = nullptr;     // device copy of the step table
+    size_t d_tape_cap = 0;
+    float4 *d_adj4 = nullptr;       // gP, gA, gV, gW (in allocs)
+    float *d_adj1 = nullptr;        // g_invm, g_invi, g_z, g_zw, g_mass, then g_cr, g_cf per scene
+    float *d_stage = nullptr;       // 3 floats per dynamic body, record order
 };
 
 namespace
@@ -163,6 +179,8 @@ int alloc_candidates(nans_world *w, int cap)
     d.cand_cap = cap;
     int rc = NANS_OK;
     auto &L = w->cand_allocs;
+    w->fwd_buf = nullptr;
+    d.s_fwd = nullptr;
     if ((rc = dalloc(w, L, &d.cand_a, cap)) || (rc = dalloc(w, L, &d.cand_b, cap)) ||
         (rc = dalloc(w, L, &d.cand_meta, cap)) || (rc = dalloc(w, L, &d.hit, cap)) ||
         (rc = dalloc(w, L, &d.c_pa, cap)) || (rc = dalloc(w, L, &d.c_pb, cap)) || (rc = dalloc(w, L, &d.c_n, cap)) ||
@@ -170,6 +188,12 @@ int alloc_candidates(nans_world *w, int cap)
         (rc = dalloc(w, L, &d.s_perm, cap)) || (rc = dalloc(w, L, &d.s_wcnt, (size_t)cap + 1)) ||
         (rc = dalloc(w, L, &d.s_k, (size_t)9 * cap)) || (rc = dalloc(w, L, &d.long_cand, cap)))
         return rc;
+    if (w->tape_on)
+    {
+        if ((rc = dalloc(w, L, &w->fwd_buf, (size_t)2 * cap)))
+            return rc;
+        d.s_fwd = w->fwd_buf;
+    }
     return NANS_OK;
 }
 
@@ -223,6 +247,12 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     free_list(w->cand_allocs);
     drop_graph(w);
     w->uploaded = false;
+    w->tape_valid = false;
+    w->fwd_buf = nullptr;
+    w->d_maxw = nullptr;
+    w->d_adj4 = nullptr;
+    w->d_adj1 = nullptr;
+    w->d_stage = nullptr;
 
     const int S = (int)nscenes;
     const int ndyn = (int)(tc + ts);
@@ -459,6 +489,7 @@ int sweep_flags(const nans_world *w)
 
 void after_step(nans_world *w, float dt)
 {
+    w->tape_valid = false;
     w->pending = true;
     w->pending_dt = dt;
     w->model_input = false;
@@ -575,6 +606,7 @@ int ensure_graph(nans_world *w, float dt, int gsteps)
 
 int batch_steps(nans_world *w, float dt, uint32_t nsteps, uint32_t gsteps)
 {
+    w->tape_valid = false;
     uint32_t done = 0;
     int rc;
     while (done < nsteps && !steady(w, dt))
@@ -600,6 +632,76 @@ int batch_steps(nans_world *w, float dt, uint32_t nsteps, uint32_t gsteps)
 }
 
 int valid_dt(float dt) { return std::isfinite(dt) && dt > 0.0f; }
+
+// Bump allocation from the tape arena (256-byte aligned); new chunks of at least 256 MiB.
+template <class T> int tape_alloc(nans_world *w, T **out, size_t n)
+{
+    const size_t bytes = (std::max<size_t>(1, n) * sizeof(T) + 255) & ~(size_t)255;
+    while (w->tape_chunk < w->tape_chunks.size())
+    {
+        if (w->tape_off + bytes <= w->tape_sizes[w->tape_chunk])
+        {
+            *out = (T *)((char *)w->tape_chunks[w->tape_chunk] + w->tape_off);
+            w->tape_off += bytes;
+            w->tape_bytes += bytes;
+            return NANS_OK;
+        }
+        ++w->tape_chunk;
+        w->tape_off = 0;
+    }
+    const size_t size = std::max(bytes, (size_t)256 << 20);
+    void *p = nullptr;
+    cudaError_t e = cudaMalloc(&p, size);
+    if (e != cudaSuccess)
+        return fail(NANS_ERR_CUDA, std::string("diff_forward: tape allocation of ") + std::to_string(size) +
+                                       " bytes: " + cudaGetErrorString(e));
+    w->tape_chunks.push_back(p);
+    w->tape_sizes.push_back(size);
+    w->tape_chunk = w->tape_chunks.size() - 1;
+    w->tape_off = bytes;
+    w->tape_bytes += bytes;
+    *out = (T *)p;
+    return NANS_OK;
+}
+
+// One taped step: velocities before RK4 (and this step's external loads), the plain step with
+// the solve recording its adjoint data, then the candidate-indexed data copied by solve slot.
+int diff_step(nans_world *w, float dt)
+{
+    cudaStream_t st = w->stream;
+    DevWorld &d = w->dw;
+    const size_t nd = (size_t)w->n_dyn;
+    const int S = w->n_scenes;
+    TapeStep t{};
+    int rc;
+    if ((rc = tape_alloc(w, &t.v_pre, nd)) || (rc = tape_alloc(w, &t.w_pre, nd)))
+        return rc;
+    CK(cudaMemcpyAsync(t.v_pre, d.vel, nd * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    CK(cudaMemcpyAsync(t.w_pre, d.omg, nd * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    if (w->forces_pending)
+    {
+        if ((rc = tape_alloc(w, &t.f_ext, nd)) || (rc = tape_alloc(w, &t.t_ext, nd)))
+            return rc;
+        CK(cudaMemcpyAsync(t.f_ext, d.frc, nd * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+        CK(cudaMemcpyAsync(t.t_ext, d.trq, nd * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    }
+    if ((rc = step_eager(w, dt, true)))
+        return rc;
+    int nc = 0;
+    CK(cudaMemcpyAsync(&nc, d.n_cand, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    nc = std::max(0, std::min(nc, w->cand_cap));
+    if ((rc = tape_alloc(w, &t.a, nc)) || (rc = tape_alloc(w, &t.b, nc)) || (rc = tape_alloc(w, &t.type, nc)) ||
+        (rc = tape_alloc(w, &t.k, (size_t)9 * nc)) || (rc = tape_alloc(w, &t.fwd, (size_t)2 * nc)) ||
+        (rc = tape_alloc(w, &t.wend, (size_t)nc + 1)) || (rc = tape_alloc(w, &t.cand_begin, S)) ||
+        (rc = tape_alloc(w, &t.maxw, S)))
+        return rc;
+    const int grid = std::max(1, std::min((std::max(nc, S) + 255) / 256, 8 * w->sm_count));
+    k_tape_copy<<<grid, 256, 0, st>>>(d, t);
+    CK(cudaGetLastError());
+    w->tape.push_back(t);
+    return NANS_OK;
+}
 
 } // namespace
 
@@ -647,6 +749,10 @@ int nans_world_destroy(nans_world *w)
         cudaFree(w->d_pairs_out);
     if (w->d_snap)
         cudaFree(w->d_snap);
+    for (void *p : w->tape_chunks)
+        cudaFree(p);
+    if (w->d_tape)
+        cudaFree(w->d_tape);
     if (w->stream)
         cudaStreamDestroy(w->stream);
     delete w;
@@ -823,6 +929,140 @@ int nans_world_set_state(nans_world *w, const nans_cube *cubes, const nans_spher
     w->pending = false;
     w->model_input = (flags & NANS_UPLOAD_KEEP_MODEL) != 0;
     w->forces_pending = true;
+    w->tape_valid = false;
+    return NANS_OK;
+}
+
+int nans_diff_forward(nans_world *w, const nans_step_params *params, float dt, uint32_t nsteps)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "diff_forward: null world");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "diff_forward: no scene uploaded");
+    if (!valid_dt(dt))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "diff_forward: dt must be finite and positive");
+    if (nsteps == 0)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "diff_forward: zero steps");
+    CK(cudaSetDevice(w->device));
+    if (params)
+        set_params_all(w, params);
+    CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), w->stream));
+    w->tape.clear();
+    w->tape_chunk = 0;
+    w->tape_off = 0;
+    w->tape_bytes = 0;
+    w->tape_valid = false;
+    int rc = NANS_OK;
+    if (!w->d_maxw && (rc = dalloc(w, w->allocs, &w->d_maxw, w->n_scenes)))
+        return rc;
+    if (!w->fwd_buf && (rc = dalloc(w, w->cand_allocs, &w->fwd_buf, (size_t)2 * w->cand_cap)))
+        return rc;
+    w->tape_on = true;
+    w->dw.s_fwd = w->fwd_buf;
+    w->dw.s_maxw = w->d_maxw;
+    for (uint32_t i = 0; i < nsteps && rc == NANS_OK; ++i)
+        rc = diff_step(w, dt);
+    w->tape_on = false;
+    w->dw.s_fwd = nullptr;
+    w->dw.s_maxw = nullptr;
+    if (rc)
+        return rc;
+    if ((rc = check_status(w)))
+        return rc;
+    w->tape_dt = dt;
+    w->tape_valid = true;
+    return NANS_OK;
+}
+
+int nans_diff_backward(nans_world *w, const nans_diff_grads *g)
+{
+    if (!w || !g)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "diff_backward: null world or gradients");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "diff_backward: no scene uploaded");
+    if (!w->tape_valid || w->tape.empty())
+        return fail(NANS_ERR_NO_TAPE, "diff_backward: no tape for the current state (nans_diff_forward must be "
+                                      "the last call that stepped or set the state)");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    const size_t nd = (size_t)w->n_dyn;
+    const int S = w->n_scenes;
+    int rc;
+    if (!w->d_adj4 && ((rc = dalloc(w, w->allocs, &w->d_adj4, 4 * nd)) ||
+                       (rc = dalloc(w, w->allocs, &w->d_adj1, 5 * nd + 2 * (size_t)S)) ||
+                       (rc = dalloc(w, w->allocs, &w->d_stage, 3 * nd))))
+        return rc;
+    const size_t nst = w->tape.size();
+    if (w->d_tape_cap < nst)
+    {
+        if (w->d_tape)
+            cudaFree(w->d_tape);
+        w->d_tape = nullptr;
+        w->d_tape_cap = 0;
+        CK(cudaMalloc(&w->d_tape, nst * sizeof(TapeStep)));
+        w->d_tape_cap = nst;
+    }
+    CK(cudaMemcpyAsync(w->d_tape, w->tape.data(), nst * sizeof(TapeStep), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(w->d_adj1, 0, (5 * nd + 2 * (size_t)S) * sizeof(float), st));
+    float4 *gP = w->d_adj4, *gA = gP + nd, *gV = gA + nd, *gW = gV + nd;
+    const int nb = (int)((nd + kSweepThreads - 1) / kSweepThreads);
+    const float *ins[4] = {g->dl_position, g->dl_angles, g->dl_velocity, g->dl_omega};
+    float4 *dst[4] = {gP, gA, gV, gW};
+    for (int i = 0; i < 4; ++i)
+    {
+        if (ins[i] && nd)
+            CK(cudaMemcpyAsync(w->d_stage, ins[i], 3 * nd * sizeof(float), cudaMemcpyHostToDevice, st));
+        if (nd)
+            k_rec_to_body<<<nb, kSweepThreads, 0, st>>>(ins[i] ? w->d_stage : nullptr, w->d_body_rec, w->n_cubes,
+                                                         w->n_dyn, dst[i]);
+    }
+    AdjointBufs b{};
+    b.gP = gP;
+    b.gA = gA;
+    b.gV = gV;
+    b.gW = gW;
+    b.g_invm = w->d_adj1;
+    b.g_invi = b.g_invm + nd;
+    b.g_z = b.g_invi + nd;
+    b.g_zw = b.g_z + nd;
+    b.g_mass = b.g_zw + nd;
+    b.g_cr = b.g_mass + nd;
+    b.g_cf = b.g_cr + S;
+    const int grid = std::max(1, std::min(S, 16 * w->sm_count));
+    k_adjoint<<<grid, adjoint_threads(), 0, st>>>(w->dw, w->d_tape, (int)nst, w->tape_dt, b);
+    CK(cudaGetLastError());
+    float *outs[4] = {g->position0, g->angles0, g->velocity0, g->omega0};
+    const float4 *src[4] = {gP, gA, gV, gW};
+    for (int i = 0; i < 4; ++i)
+        if (outs[i] && nd)
+        {
+            k_body_to_rec<<<nb, kSweepThreads, 0, st>>>(src[i], nullptr, w->d_body_rec, w->n_cubes, w->n_dyn,
+                                                         w->d_stage, 3);
+            CK(cudaMemcpyAsync(outs[i], w->d_stage, 3 * nd * sizeof(float), cudaMemcpyDeviceToHost, st));
+        }
+    if (g->mass && nd)
+    {
+        k_body_to_rec<<<nb, kSweepThreads, 0, st>>>(nullptr, b.g_mass, w->d_body_rec, w->n_cubes, w->n_dyn,
+                                                     w->d_stage, 1);
+        CK(cudaMemcpyAsync(g->mass, w->d_stage, nd * sizeof(float), cudaMemcpyDeviceToHost, st));
+    }
+    if (g->restitution)
+        CK(cudaMemcpyAsync(g->restitution, b.g_cr, S * sizeof(float), cudaMemcpyDeviceToHost, st));
+    if (g->friction)
+        CK(cudaMemcpyAsync(g->friction, b.g_cf, S * sizeof(float), cudaMemcpyDeviceToHost, st));
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
+    return NANS_OK;
+}
+
+int nans_diff_tape_info(nans_world *w, uint32_t *steps, uint64_t *bytes)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "diff_tape_info: null world");
+    if (steps)
+        *steps = w->tape_valid ? (uint32_t)w->tape.size() : 0;
+    if (bytes)
+        *bytes = w->tape_valid ? (uint64_t)w->tape_bytes : 0;
     return NANS_OK;
 }
 

@@ -98,7 +98,10 @@ __device__ __forceinline__ float friction_bound(float cf, float sum)
     return (float)(1.4142135623730951 * (double)cf * (double)sum);
 }
 
-// Velocity-dependent part of Constraint (code/nans.cpp:1149-1156, 1171-1328).
+// Velocity-dependent part of Constraint (code/nans.cpp:1149-1156, 1171-1328). With a tape
+// attached (w.s_fwd) it also records, per contact, what the adjoint needs: the relative
+// normal / tangent velocities, the applied impulses and the active set of the closed form
+// (normal impulse max(Ln, 0), tangent impulses clamp(Lt, -mu*Ln, mu*Ln)).
 __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const float4 *k, float cr, float cf,
                                               int iters)
 {
@@ -141,6 +144,24 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
         if (st2 > m2)
             st2 = m2;
         dt2 = st2 - old;
+    }
+    if (w.s_fwd)
+    {
+        float ln = (-jdvn + bias) * jn;
+        float lt1 = (-jdvt1) * jt1, lt2 = (-jdvt2) * jt2;
+        float mu = (float)(1.4142135623730951 * (double)cf);
+        unsigned flags = 0;
+        if (ln > 0.0f && iters > 0)
+        {
+            flags |= 1u;
+            float bound = mu * ln;
+            flags |= (lt1 > bound ? 1u : (lt1 < -bound ? 2u : 0u)) << 1;
+            flags |= (lt2 > bound ? 1u : (lt2 < -bound ? 2u : 0u)) << 3;
+        }
+        else
+            flags |= (3u << 1) | (3u << 3);
+        w.s_fwd[2 * (size_t)c] = make_float4(jdvn, jdvt1, jdvt2, __uint_as_float(flags));
+        w.s_fwd[2 * (size_t)c + 1] = make_float4(dn, dt1, dt2, ln);
     }
     v3 li = dn * n, lt1 = dt1 * t1, lt2 = dt2 * t2;
     v3 ai1 = dn * xyz(k[3]), ai2 = dn * xyz(k[4]);
@@ -203,6 +224,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt)
         }
         if (nh == 0)
         {
+            if (tid == 0 && w.s_maxw)
+                w.s_maxw[s] = 0;
             __syncthreads();
             continue;
         }
@@ -247,6 +270,8 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt)
             __syncthreads();
         }
         const int maxw = s_maxw;
+        if (tid == 0 && w.s_maxw)
+            w.s_maxw[s] = maxw;
         // (3) counting sort by wave: s_wcnt[cb + wave] (waves 1..maxw, maxw <= nh)
         for (int i = tid; i <= maxw; i += blockDim.x)
             w.s_wcnt[cb + i] = 0;

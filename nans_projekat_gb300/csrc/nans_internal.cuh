@@ -98,6 +98,8 @@ struct DevWorld
     int *s_order, *s_wave, *s_perm, *s_wcnt;
     float4 *s_k;                        // 9 float4 of per-contact constants
     int *s_last;                        // per body: last wave touching it
+    float4 *s_fwd;                      // adjoint tape of the solve (2 float4 per slot) or null
+    int *s_maxw;                        // per scene: highest wave of the last solve, or null
     unsigned *status;
 };
 

@@ -66,4 +66,36 @@ void launch_epa_medium(cudaStream_t st, const DevWorld &w);
 __global__ void k_solve(DevWorld w, float dt);
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);
 
+// One step of the differentiable rollout's tape. Contact data is stored by solve slot: slot
+// cand_begin[s] + i holds the i-th contact of scene s in wave order, so one wave is a
+// contiguous slot range [wend[cb + w - 1], wend[cb + w]) offset by cb.
+struct TapeStep
+{
+    int *a, *b, *type;        // per slot: bodies and pair type
+    float4 *k;                // per slot: 9 float4 of contact constants (k_solve layout)
+    float4 *fwd;              // per slot: (JdVn, JdVt1, JdVt2, flags), (dn, dt1, dt2, Ln)
+    int *wend;                // per slot index: end of each wave (k_solve's s_wcnt)
+    int *cand_begin, *maxw;   // per scene
+    float4 *v_pre, *w_pre;    // per dynamic body: V, W before this step's RK4
+    float4 *f_ext, *t_ext;    // per dynamic body: external force / torque of this step, or null
+};
+
+// Adjoint accumulators, per dynamic body (float4 xyz) / per scene.
+struct AdjointBufs
+{
+    const float4 *gP, *gA;    // dL/d(final position / angles); constant through the rollout
+    float4 *gV, *gW;          // in: dL/d(final V, W); out: dL/d(initial V, W)
+    float *g_invm, *g_invi;   // accumulated dL/d(1/m), dL/d(1/I)
+    float *g_z, *g_zw;        // accumulated dL/dz, dL/dzw of the RK4 closed form
+    float *g_mass;            // out: dL/dm (moment of inertia proportional to mass)
+    float *g_cr, *g_cf;       // out, per scene: dL/d restitution, dL/d friction
+};
+
+int adjoint_threads();
+__global__ void k_tape_copy(DevWorld w, TapeStep t);
+__global__ void k_adjoint(DevWorld w, const TapeStep *steps, int nsteps, float h, AdjointBufs g);
+__global__ void k_rec_to_body(const float *in_rec, const int *body_rec, int n_cubes, int n_dyn, float4 *out);
+__global__ void k_body_to_rec(const float4 *in, const float *in_scalar, const int *body_rec, int n_cubes, int n_dyn,
+                              float *out_rec, int comps);
+
 } // namespace nans

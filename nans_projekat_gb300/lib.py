@@ -25,6 +25,7 @@ ERRORS = {
     5: "NANS_ERR_EPA_CAPACITY",
     6: "NANS_ERR_NOT_UPLOADED",
     7: "NANS_ERR_SCENE_TOO_LARGE",
+    8: "NANS_ERR_NO_TAPE",
 }
 UPLOAD_KEEP_MODEL = 1
 WORLD_ALL_PAIRS = 1
@@ -36,7 +37,8 @@ EXPORTS = (
     "nans_batch_step", "nans_batch_autotune", "nans_world_download", "nans_world_set_state",
     "nans_get_pairs", "nans_world_status", "nans_world_counts", "nans_world_stream",
     "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps",
-    "nans_world_epa_stats", "nans_solve_contacts_static",
+    "nans_world_epa_stats", "nans_solve_contacts_static", "nans_diff_forward", "nans_diff_backward",
+    "nans_diff_tape_info",
 )
 
 
@@ -52,6 +54,12 @@ class WorldDesc(ctypes.Structure):
 
 class StepParams(ctypes.Structure):
     _fields_ = [("cr", ctypes.c_float), ("cf", ctypes.c_float), ("iterations", ctypes.c_int32)]
+
+
+class DiffGrads(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("dl_position", "dl_angles", "dl_velocity", "dl_omega", "position0",
+                                              "angles0", "velocity0", "omega0", "mass", "restitution",
+                                              "friction")]
 
 
 _LIB = None
@@ -88,6 +96,9 @@ def load(path=LIB_PATH):
     L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
     L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
     L.nans_world_epa_stats.argtypes = [_P, _P, ctypes.c_int]
+    L.nans_diff_forward.argtypes = [_P, ctypes.POINTER(StepParams), _F, _U]
+    L.nans_diff_backward.argtypes = [_P, ctypes.POINTER(DiffGrads)]
+    L.nans_diff_tape_info.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(ctypes.c_uint64)]
     L.nans_solve_contacts_static.argtypes = [_U, _U, _P, _P, _P, _P, _P, _P, _P, _U, _F, _F, ctypes.c_int32,
                                              _F, _P]
     _LIB = L
@@ -247,6 +258,45 @@ class World:
         return dict(max_faces=int(out[0]), max_edges=int(out[1]), slow_epas=int(out[2]),
                     overflow_candidate=int(out[3]) - 1, overflow_scene=int(out[4]) - 1,
                     overflows=int(out[5]), warp_tier=int(out[6]))
+
+    # -- differentiable rollout -------------------------------------------------------
+    def diff_forward(self, dt, n, params=None):
+        """n plain steps that also record the adjoint's tape (same results as step)."""
+        p = None
+        if params is not None:
+            p = ctypes.byref(StepParams(params.cr, params.cf, params.iterations))
+        _check(self.lib.nans_diff_forward(self.h, p, dt, n))
+
+    def diff_backward(self, dl_position=None, dl_angles=None, dl_velocity=None, dl_omega=None):
+        """Gradients of a loss of the final state with respect to the initial state, the
+        masses and the solver constants of the last diff_forward. Per-body arrays are
+        (n_bodies, 3) in record order (all cubes, then all spheres); returns a dict with
+        position0, angles0, velocity0, omega0 (n_bodies, 3), mass (n_bodies,), restitution
+        and friction (n_scenes,)."""
+        nb, ns = self.n_bodies, len(self.scenes)
+
+        def inp(a):
+            if a is None:
+                return None
+            a = np.ascontiguousarray(a, np.float32)
+            if a.shape != (nb, 3):
+                raise ValueError("gradient input must have shape (%d, 3)" % nb)
+            return a
+        ins = [inp(a) for a in (dl_position, dl_angles, dl_velocity, dl_omega)]
+        out = dict(position0=np.zeros((nb, 3), np.float32), angles0=np.zeros((nb, 3), np.float32),
+                   velocity0=np.zeros((nb, 3), np.float32), omega0=np.zeros((nb, 3), np.float32),
+                   mass=np.zeros(nb, np.float32), restitution=np.zeros(ns, np.float32),
+                   friction=np.zeros(ns, np.float32))
+        g = DiffGrads(*([_ptr(a) for a in ins] + [_ptr(out[k]) for k in ("position0", "angles0", "velocity0",
+                                                                        "omega0", "mass", "restitution",
+                                                                        "friction")]))
+        _check(self.lib.nans_diff_backward(self.h, ctypes.byref(g)))
+        return out
+
+    def diff_tape_info(self):
+        n, b = _U(), ctypes.c_uint64()
+        _check(self.lib.nans_diff_tape_info(self.h, ctypes.byref(n), ctypes.byref(b)))
+        return n.value, b.value
 
     @property
     def n_bodies(self):
