@@ -315,7 +315,45 @@ def secondary_measurements(lib, batch, device):
                                 "steps": n, "ms_per_step": 1000.0 * t / n,
                                 "workload": "random4608: 4,096 boxes + 512 spheres, 64^3 m box, plain path"}
     wb.close()
+    out["differentiable"] = differentiable_measurement(lib, device)
     return out
+
+
+def differentiable_measurement(lib, device):
+    """1,024 scenes of a 4x4x2 box stack plus a sphere, 120 steps: the plain forward, the
+    taped forward (nans_diff_forward) and the adjoint (nans_diff_backward, host gradient
+    arrays in and out), wall clock around the synchronous calls."""
+    import torch
+    from nans_projekat_gb300 import scenes
+    grid = scenes.grid_stack_batch(1024, seed=3)
+    n = 120
+    wg = lib.World(device=device)
+    wg.upload_batch(grid)
+    wg.step(DT, 2)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        torch.cuda.synchronize()
+        return 1e3 * (time.perf_counter() - t0), r
+
+    wg.upload_batch(grid)
+    t_plain, _ = timed(lambda: wg.step(DT, n))
+    wg.upload_batch(grid)
+    t_fwd, _ = timed(lambda: wg.diff_forward(DT, n))
+    steps, tape_bytes = wg.diff_tape_info()
+    rng = np.random.default_rng(0)
+    wts = [rng.normal(size=(wg.n_bodies, 3)).astype(np.float32) for _ in range(4)]
+    wg.diff_backward(*wts)
+    t_bwd = min(timed(lambda: wg.diff_backward(*wts))[0] for _ in range(3))
+    bodies = wg.n_bodies
+    wg.close()
+    return {"workload": "grid33x1024: 1,024 scenes of a 4x4x2 stack of unit boxes + one 20 m/s sphere",
+            "bodies": bodies, "steps": n, "plain_forward_ms": t_plain, "taped_forward_ms": t_fwd,
+            "backward_ms": t_bwd, "backward_over_forward": t_bwd / t_fwd,
+            "tape_bytes": int(tape_bytes), "tape_steps": int(steps),
+            "forward_value": bodies * n / (t_fwd / 1e3), "unit": UNIT}
 
 
 def run_ours(args):
