@@ -399,7 +399,7 @@ def run_ours(args):
     # per-stage device time from a live event-timed pass over the same world
     prof_steps = 10
     stage_ms = w.profile(DT, prof_steps) / prof_steps
-    names = ["k_sweep", "k_cull (3 kernels)", "k_narrow_tiny", "k_epa_medium", "k_narrow_big", "k_solve"]
+    names = ["k_sweep", "k_cull (3 kernels)", "k_narrow_tiny", "k_epa_medium", "k_narrow_big (block + giant tiers)", "k_solve"]
     dom = int(np.argmax(stage_ms))
     peak, peak_kind = measured_peaks()
     n_boxes = int(sum(len(s.cubes) for s in batch))
@@ -454,7 +454,7 @@ def run_ours(args):
                 "candidates_per_step": n_cand, "contacts_per_step": n_contacts,
                 "large_epa": {"slow_path_epas": epa["slow_epas"], "max_faces": epa["max_faces"],
                               "max_horizon_edges": epa["max_edges"], "beyond_capacity": epa["overflows"],
-                              "warp_tier_epas": epa["warp_tier"]},
+                              "warp_tier_epas": epa["warp_tier"], "giant_tier_epas": epa["giant_tier"]},
             },
             "roofline": {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": measured_traffic(names[dom]),

@@ -187,10 +187,11 @@ int nans_world_status(nans_world *world, uint32_t *status_bits);
 int nans_world_counts(nans_world *world, uint32_t *candidates, uint32_t *contacts);
 
 /* Large-polytope EPA statistics since upload (or the last reset): out[0] largest face list
- * and out[1] largest horizon seen by the large-polytope path, out[2] EPAs that took that path,
- * out[3] candidate index + 1 and out[4] scene + 1 of the last EPA that outgrew it (0 if none),
- * out[5] EPAs that outgrew it, out[6] EPAs escalated from the per-thread tier to the warp
- * tier. out holds 7 entries. */
+ * and out[1] largest horizon seen by the block and giant tiers, out[2] EPAs that went beyond
+ * the warp tier, out[3] candidate index + 1 and out[4] scene + 1 of the last EPA that outgrew
+ * the giant tier (0 if none), out[5] EPAs that outgrew it, out[6] EPAs escalated from the
+ * per-thread tier to the warp tier, out[7] EPAs escalated from the block tier (32,768 faces)
+ * to the giant tier. out holds 8 entries. */
 int nans_world_epa_stats(nans_world *world, uint32_t *out, int reset);
 
 /* The world's CUDA stream (a cudaStream_t), for event timing by the caller. */

@@ -383,9 +383,11 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.pair_mask, (size_t)((pair_acc + 31) / 32))) ||
         (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.n_cand, 1)) ||
         (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
-        (rc = dalloc(w, L, &d.work_counter, 8)) || (rc = dalloc(w, L, &d.status, 1)) ||
+        (rc = dalloc(w, L, &d.work_counter, kWorkCounters)) || (rc = dalloc(w, L, &d.status, 1)) ||
         (rc = dalloc(w, L, &d.ovf_cand, kEpaOverflowCap)) || (rc = dalloc(w, L, &d.med_cand, kEpaMediumCap)) ||
         (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes() * (size_t)kEpaArenaWarps)) ||
+        (rc = dalloc(w, L, &d.blk_arena, epa_block_bytes() * (size_t)(kBlockPerSm * w->sm_count))) ||
+        (rc = dalloc(w, L, &d.giant_cand, kGiantQueueCap)) ||
         (rc = dalloc(w, L, &d.epa_stats, 8)) ||
         (rc = dalloc(w, L, &w->d_rec_cube, (size_t)61 * tc)) || (rc = dalloc(w, L, &w->d_rec_sphere, (size_t)37 * ts)) ||
         (rc = dalloc(w, L, &w->d_rec_floor, (size_t)61 * S)) || (rc = dalloc(w, L, &w->d_small, 2)) ||
@@ -409,6 +411,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.med_cap = kEpaMediumCap;
     d.medium_blocks = 2 * w->sm_count;
     d.epa_arena_warps = kEpaArenaWarps;
+    d.blk_blocks = kBlockPerSm * w->sm_count;
+    d.giant_cap = kGiantQueueCap;
     cudaStream_t st = w->stream;
     CK(cudaMemcpyAsync(p_cube0, sc_cube0.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_nc, sc_nc.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -432,6 +436,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     CK(cudaMemcpyAsync(w->d_rec_floor, floors, S * sizeof(nans_cube), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
     CK(cudaMemsetAsync(d.epa_arena, 0, epa_big_bytes() * (size_t)kEpaArenaWarps, st));
+    CK(cudaMemsetAsync(d.blk_arena, 0, epa_block_bytes() * (size_t)d.blk_blocks, st));
     CK(cudaMemsetAsync(d.epa_stats, 0, 8 * sizeof(unsigned), st));
     CK(cudaMemsetAsync(d.n_cand, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, S * sizeof(int), st));
@@ -503,7 +508,7 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
 {
     cudaStream_t st = w->stream;
     DevWorld &d = w->dw;
-    CK(cudaMemsetAsync(d.work_counter, 0, 8 * sizeof(int), st));
+    CK(cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
     k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
@@ -580,7 +585,7 @@ int ensure_graph(nans_world *w, float dt, int gsteps)
     DevWorld &d = w->dw;
     for (int i = 0; i < gsteps; ++i)
     {
-        cudaMemsetAsync(d.work_counter, 0, 8 * sizeof(int), st);
+        cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st);
         cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st);
         cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st);
         k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, dt, dt,
@@ -1149,7 +1154,7 @@ int nans_world_epa_stats(nans_world *w, uint32_t *out, int reset)
     if (!w->uploaded)
         return fail(NANS_ERR_NOT_UPLOADED, "epa_stats: no scene uploaded");
     CK(cudaSetDevice(w->device));
-    CK(cudaMemcpyAsync(out, w->dw.epa_stats, 7 * sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
+    CK(cudaMemcpyAsync(out, w->dw.epa_stats, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream));
     if (reset)
         CK(cudaMemsetAsync(w->dw.epa_stats, 0, 8 * sizeof(unsigned), w->stream));
     CK(cudaStreamSynchronize(w->stream));
@@ -1196,7 +1201,7 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
     DevWorld &d = w->dw;
     for (uint32_t k = 0; k < nsteps; ++k)
     {
-        CK(cudaMemsetAsync(d.work_counter, 0, 8 * sizeof(int), st));
+        CK(cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
         CK(cudaEventRecord(ev[0], st));
@@ -1232,8 +1237,9 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
 {
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
-    // sweep, [mask, write], scan, narrow_tiny, narrow_long, epa_medium, narrow_big, solve
-    uint32_t k = 7 + (w->cull_blocks > 0 ? 2u : 0u);
+    // sweep, [mask, write], scan, narrow_tiny, narrow_long, epa_medium, block EPA, giant EPA,
+    // solve
+    uint32_t k = 8 + (w->cull_blocks > 0 ? 2u : 0u);
     if (batched)
         *batched = k;
     if (plain)

@@ -832,25 +832,28 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(
 // Counting is parallel (hash table of groups); the "last n" ranks come from one ordered
 // reverse pass over the pushes in warp-sized chunks.
 // ------------------------------------------------------------------------------------
-struct EpaGiant
+template <int F, int P, int E, int S> struct EpaArena
 {
+    static constexpr int kFaces = F, kPushes = P, kEdges = E, kSlots = S;
     float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
     float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
     float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
-    float fnx[kGiantFaces], fny[kGiantFaces], fnz[kGiantFaces], fd[kGiantFaces];
-    unsigned fidx[kGiantFaces];              // a | b << 8 | c << 16
-    unsigned vis[kGiantFaces / 32];
-    int chunk_pre[kGiantFaces / 32];
-    unsigned short push[kGiantPushes];       // u | v << 8
-    int pslot[kGiantPushes];                 // group slot, -1 for a NaN edge
-    unsigned char pdir[kGiantPushes];        // 0 / 1 orientation, 2 self-loop
-    unsigned char palive[kGiantPushes];
-    unsigned short edge[kGiantEdges];        // horizon: u | v << 8
-    unsigned long long skey[kGiantSlots];    // 0 = empty
-    int sfirst[kGiantSlots];
-    int scnt0[kGiantSlots], scnt1[kGiantSlots], squota[kGiantSlots];
-    unsigned char sqdir[kGiantSlots];
+    float fnx[F], fny[F], fnz[F], fd[F];
+    unsigned fidx[F];                        // a | b << 8 | c << 16
+    unsigned vis[F / 32];
+    int chunk_pre[F / 32];
+    unsigned short push[P];                  // u | v << 8
+    int pslot[P];                            // group slot, -1 for a NaN edge
+    unsigned char pdir[P];                   // 0 / 1 orientation, 2 self-loop
+    unsigned char palive[P];
+    unsigned short edge[E];                  // horizon: u | v << 8
+    unsigned long long skey[S];              // 0 = empty
+    int sfirst[S];
+    int scnt0[S], scnt1[S], squota[S];
+    unsigned char sqdir[S];
 };
+using EpaBlock = EpaArena<kBlockFaces, kBlockPushes, kBlockEdges, kBlockSlots>;
+using EpaGiant = EpaArena<kGiantFaces, kGiantPushes, kGiantEdges, kGiantSlots>;
 
 struct GiantShared
 {
@@ -860,9 +863,9 @@ struct GiantShared
     int bcast[4];
 };
 
-__device__ __forceinline__ v3 gpool(const EpaGiant &E, int i) { return mk3(E.px[i], E.py[i], E.pz[i]); }
+template <class A> __device__ __forceinline__ v3 gpool(const A &E, int i) { return mk3(E.px[i], E.py[i], E.pz[i]); }
 
-__device__ __forceinline__ void gpool_put(EpaGiant &E, int i, const GV &g)
+template <class A> __device__ __forceinline__ void gpool_put(A &E, int i, const GV &g)
 {
     E.px[i] = g.p.x;
     E.py[i] = g.p.y;
@@ -875,7 +878,7 @@ __device__ __forceinline__ void gpool_put(EpaGiant &E, int i, const GV &g)
     E.bz[i] = g.sb.z;
 }
 
-__device__ __forceinline__ void gface_put(EpaGiant &E, int f, int a, int b, int c)
+template <class A> __device__ __forceinline__ void gface_put(A &E, int f, int a, int b, int c)
 {
     v3 pa = gpool(E, a), pb = gpool(E, b), pc = gpool(E, c);
     v3 n = normalize3(cross3(pb - pa, pc - pa));
@@ -923,7 +926,8 @@ __device__ __forceinline__ int gscan(int v, GiantShared &sh, int &total)
 
 // Undirected group key of the edge (u, v): canonical positions ordered lexicographically.
 // Returns false for an edge with a NaN coordinate.
-__device__ __forceinline__ bool group_key(const EpaGiant &E, int u, int v, unsigned key[6], int &dir)
+template <class A>
+__device__ __forceinline__ bool group_key(const A &E, int u, int v, unsigned key[6], int &dir)
 {
     v3 pu = gpool(E, u), pv = gpool(E, v);
     if (isnan(pu.x) || isnan(pu.y) || isnan(pu.z) || isnan(pv.x) || isnan(pv.y) || isnan(pv.z))
@@ -943,7 +947,8 @@ __device__ __forceinline__ bool group_key(const EpaGiant &E, int u, int v, unsig
     return true;
 }
 
-__device__ int epa_giant(const DevWorld &w, EpaGiant &E, GiantShared &sh, const Shape &A, const Shape &Bs, const GV &s0,
+template <class Arena>
+__device__ int epa_giant(const DevWorld &w, Arena &E, GiantShared &sh, const Shape &A, const Shape &Bs, const GV &s0,
                          const GV &s1, const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n)
 {
     const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
@@ -1083,7 +1088,7 @@ __device__ int epa_giant(const DevWorld &w, EpaGiant &E, GiantShared &sh, const 
             nvis += tot;
         }
         const int m = 3 * nvis;
-        if (m > kGiantPushes)
+        if (m > Arena::kPushes)
             return EPA_OVERFLOW;
         __syncthreads();
         for (int f = tid; f < nf; f += nt)
@@ -1117,8 +1122,8 @@ __device__ int epa_giant(const DevWorld &w, EpaGiant &E, GiantShared &sh, const 
             for (int q = 0; q < 6; ++q)
                 h = (h ^ key[q]) * 1099511628211ull;
             h |= 1ull;
-            unsigned s = (unsigned)(h >> 20) & (kGiantSlots - 1);
-            for (int probe = 0; probe < kGiantSlots; ++probe)
+            unsigned s = (unsigned)(h >> 20) & (Arena::kSlots - 1);
+            for (int probe = 0; probe < Arena::kSlots; ++probe)
             {
                 unsigned long long prev = atomicCAS(&E.skey[s], 0ull, h);
                 if (prev == 0ull)
@@ -1128,7 +1133,7 @@ __device__ int epa_giant(const DevWorld &w, EpaGiant &E, GiantShared &sh, const 
                 }
                 if (prev == h)
                     break;
-                s = (s + 1) & (kGiantSlots - 1);
+                s = (s + 1) & (Arena::kSlots - 1);
             }
             E.pslot[k] = (int)s;
             E.pdir[k] = (unsigned char)dir;
@@ -1222,11 +1227,11 @@ __device__ int epa_giant(const DevWorld &w, EpaGiant &E, GiantShared &sh, const 
             int al = (k < m) ? E.palive[k] : 0;
             int tot;
             int pre = gscan(al, sh, tot);
-            if (al && ne + pre < kGiantEdges)
+            if (al && ne + pre < Arena::kEdges)
                 E.edge[ne + pre] = E.push[k];
             ne += tot;
         }
-        if (ne > kGiantEdges)
+        if (ne > Arena::kEdges)
             return EPA_OVERFLOW;
         // stable removal of the visible faces
         int keep = 0;
@@ -1264,7 +1269,7 @@ __device__ int epa_giant(const DevWorld &w, EpaGiant &E, GiantShared &sh, const 
             atomicMax(w.epa_stats + 0, (unsigned)(keep + ne));
             atomicMax(w.epa_stats + 1, (unsigned)ne);
         }
-        if (keep + ne > kGiantFaces)
+        if (keep + ne > Arena::kFaces)
             return EPA_OVERFLOW;
         if (keep == 0 && ne == 0)
         {
@@ -1295,22 +1300,29 @@ __device__ int epa_giant(const DevWorld &w, EpaGiant &E, GiantShared &sh, const 
     return EPA_NONE;
 }
 
-__global__ void __launch_bounds__(kGiantThreads) k_narrow_big(DevWorld w)
+// Tier 3 (TIER == 3): the block-EPA queue, arenas of 32,768 faces, many blocks; an EPA that
+// outgrows its arena is queued for tier 4. Tier 4: the giant queue, arenas of 2,097,152
+// faces, a few blocks; beyond that the pair gets no contact.
+template <class Arena, int TIER, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_narrow_big(DevWorld w)
 {
     __shared__ GiantShared sh;
     __shared__ int s_q;
-    EpaGiant &E = *reinterpret_cast<EpaGiant *>(w.epa_arena + (size_t)blockIdx.x * sizeof(EpaGiant));
-    const int n = min(w.work_counter[3], w.ovf_cap);
+    unsigned char *base = (TIER == 3) ? w.blk_arena : w.epa_arena;
+    Arena &E = *reinterpret_cast<Arena *>(base + (size_t)blockIdx.x * sizeof(Arena));
+    const int n = (TIER == 3) ? min(w.work_counter[3], w.ovf_cap) : min(w.work_counter[8], w.giant_cap);
+    const int *queue = (TIER == 3) ? w.ovf_cand : w.giant_cand;
+    int *head = w.work_counter + ((TIER == 3) ? 2 : 9);
     for (;;)
     {
         if (threadIdx.x == 0)
-            s_q = atomicAdd(w.work_counter + 2, 1);
+            s_q = atomicAdd(head, 1);
         __syncthreads();
         const int q = s_q;
         __syncthreads();
         if (q >= n)
             break;
-        const int cc = w.ovf_cand[q];
+        const int cc = queue[q];
         const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
         GV s0, s1, s2, s3;
         gjk(w.verts, A, B, s0, s1, s2, s3); // every thread: same inputs, same simplex
@@ -1319,24 +1331,41 @@ __global__ void __launch_bounds__(kGiantThreads) k_narrow_big(DevWorld w)
         __syncthreads();
         if (threadIdx.x == 0)
         {
-            atomicAdd(w.epa_stats + 2, 1u);
-            if (r == EPA_OVERFLOW)
+            if (TIER == 3)
+                atomicAdd(w.epa_stats + 2, 1u);
+            bool done = true;
+            if (r == EPA_OVERFLOW && TIER == 3)
             {
-                // Beyond the arena the pair gets no contact, which is what the reference
-                // returns for every EPA that does not converge within its 65 iterations.
-                atomicOr(w.status, (unsigned)ST_EPA_FACES);
-                atomicAdd(w.epa_stats + 5, 1u);
-                w.epa_stats[3] = (unsigned)cc + 1u;
-                w.epa_stats[4] = (unsigned)(w.cand_meta[cc] >> 3) + 1u;
-                r = EPA_NONE;
+                int g = atomicAdd(w.work_counter + 8, 1);
+                if (g < w.giant_cap)
+                {
+                    w.giant_cand[g] = cc;
+                    atomicAdd(w.epa_stats + 7, 1u);
+                    w.hit[cc] = 0;
+                    done = false;
+                }
             }
-            write_result(w, cc, r, pa, pb, nn);
+            if (done)
+            {
+                if (r == EPA_OVERFLOW)
+                {
+                    // Beyond the arena the pair gets no contact, which is what the reference
+                    // returns for every EPA that does not converge within its 65 iterations.
+                    atomicOr(w.status, (unsigned)ST_EPA_FACES);
+                    atomicAdd(w.epa_stats + 5, 1u);
+                    w.epa_stats[3] = (unsigned)cc + 1u;
+                    w.epa_stats[4] = (unsigned)(w.cand_meta[cc] >> 3) + 1u;
+                    r = EPA_NONE;
+                }
+                write_result(w, cc, r, pa, pb, nn);
+            }
         }
         __syncthreads();
     }
 }
 
 size_t epa_big_bytes() { return sizeof(EpaGiant); }
+size_t epa_block_bytes() { return sizeof(EpaBlock); }
 
 
 static size_t medium_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }
@@ -1377,7 +1406,11 @@ void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
     launch_epa_medium(st, w);
 }
 
-void launch_narrow_big(cudaStream_t st, const DevWorld &w) { k_narrow_big<<<w.epa_arena_warps, kGiantThreads, 0, st>>>(w); }
+void launch_narrow_big(cudaStream_t st, const DevWorld &w)
+{
+    k_narrow_big<EpaBlock, 3, kBlockThreads><<<w.blk_blocks, kBlockThreads, 0, st>>>(w);
+    k_narrow_big<EpaGiant, 4, kGiantThreads><<<w.epa_arena_warps, kGiantThreads, 0, st>>>(w);
+}
 
 void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
 {

@@ -79,21 +79,27 @@ struct DevWorld
     // narrowphase output, per candidate
     int *hit;
     float4 *c_pa, *c_pb, *c_n;
-    int *work_counter;                  // [0] narrowphase head, [1] solver head, [2] large-EPA
-                                        // head, [3] large-EPA queue length, [5] warp-EPA queue
-                                        // length, [6] warp-EPA head, [7] long-GJK queue length
+    int *work_counter;                  // [0] narrowphase head, [1] solver head, [2] block-EPA
+                                        // head, [3] block-EPA queue length, [5] warp-EPA queue
+                                        // length, [6] warp-EPA head, [7] long-GJK queue length,
+                                        // [8] giant-EPA queue length, [9] giant-EPA head
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
     int *long_cand;                     // candidates whose GJK needs the long pass
     int medium_blocks;                  // warp-tier grid
-    int ovf_cap;                        // large-EPA queue capacity
-    int *ovf_cand;                      // candidates queued for the large-polytope tier
-    unsigned char *epa_arena;           // slow-path polytope buffers, one per warp
-    int epa_arena_warps;
-    unsigned *epa_stats;                // [0] max faces, [1] max horizon edges, [2] slow-path EPAs,
-                                        // [3] overflowing candidate + 1, [4] its scene + 1,
-                                        // [5] EPAs that outgrew the slow path, [6] EPAs
-                                        // escalated to the warp tier
+    int ovf_cap;                        // block-EPA queue capacity
+    int *ovf_cand;                      // candidates queued for the block tier
+    unsigned char *blk_arena;           // block-tier polytope buffers, one per block
+    int blk_blocks;                     // block-tier grid
+    int giant_cap;                      // giant-EPA queue capacity
+    int *giant_cand;                    // candidates queued for the giant tier
+    unsigned char *epa_arena;           // giant-tier polytope buffers, one per block
+    int epa_arena_warps;                // giant-tier grid
+    unsigned *epa_stats;                // [0] max faces, [1] max horizon edges, [2] block- and
+                                        // giant-tier EPAs, [3] overflowing candidate + 1, [4] its
+                                        // scene + 1, [5] EPAs that outgrew the giant tier, [6]
+                                        // EPAs escalated to the warp tier, [7] EPAs escalated to
+                                        // the giant tier
     // solver scratch, per candidate slot
     int *s_order, *s_wave, *s_perm, *s_wcnt;
     float4 *s_k;                        // 9 float4 of per-contact constants

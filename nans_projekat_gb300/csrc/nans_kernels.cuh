@@ -29,19 +29,28 @@ constexpr int kPairsPerBlock = kCullThreads * kPairsPerThread;
 // 128 faces, and the largest met so far (scene 10198, step 135) reaches 485,688 faces and a
 // 139,111-edge horizon (the reference's own algorithm needs 334 s of one CPU core for it).
 // Tier 1 runs EPA per thread (12 vertices, 20 faces, 12 edges); tier 2 per warp in shared
-// memory (128 faces, 32 edges); tier 3 per block in a global-memory arena (2,097,152 faces,
-// 4,194,304 horizon pushes, 1,048,576 horizon edges). Beyond that the pair gets no contact
-// and the event is counted (NANS_ERR_EPA_CAPACITY in strict worlds).
+// memory (128 faces, 32 edges); tier 3 per block in a global-memory arena of 32,768 faces,
+// two blocks per SM; tier 4 per block in an arena of 2,097,152 faces, 4,194,304 horizon
+// pushes and 1,048,576 horizon edges. Beyond that the pair gets no contact and the event is
+// counted (NANS_ERR_EPA_CAPACITY in strict worlds).
 constexpr int kEpaMaxVerts = 72;
 constexpr int kEpaFastFaces = 128;
 constexpr int kEpaFastEdges = 32;
+constexpr int kBlockFaces = 1 << 15;
+constexpr int kBlockPushes = 1 << 16;
+constexpr int kBlockEdges = 1 << 15;
+constexpr int kBlockSlots = 1 << 17;
+constexpr int kBlockThreads = 256;
+constexpr int kBlockPerSm = 2;
 constexpr int kGiantFaces = 1 << 21;
 constexpr int kGiantPushes = 1 << 22;
 constexpr int kGiantEdges = 1 << 20;
 constexpr int kGiantSlots = 1 << 23;   // group table, load factor <= 1/2
 constexpr int kGiantThreads = 512;
-constexpr int kEpaArenaWarps = 4;      // tier-3 blocks, one ~330 MB arena each
+constexpr int kEpaArenaWarps = 4;      // tier-4 blocks, one ~330 MB arena each
 constexpr int kEpaOverflowCap = 65536; // tier-3 EPAs queued per step
+constexpr int kGiantQueueCap = 4096;   // tier-4 EPAs queued per step
+constexpr int kWorkCounters = 16;
 constexpr int kEpaMediumCap = 1 << 20; // tier-2 EPAs queued per step
 
 __global__ void k_sweep(DevWorld w, float pending_dt, float dt, int flags);
@@ -58,6 +67,7 @@ __global__ void k_cull_write(DevWorld w);
 
 int narrow_blocks_per_sm(int warps);
 size_t epa_big_bytes();
+size_t epa_block_bytes();
 void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w);
 void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w);
 void launch_narrow_big(cudaStream_t st, const DevWorld &w);

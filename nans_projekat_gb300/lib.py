@@ -253,11 +253,11 @@ class World:
         return ms
 
     def epa_stats(self, reset=False):
-        out = np.zeros(7, np.uint32)
+        out = np.zeros(8, np.uint32)
         _check(self.lib.nans_world_epa_stats(self.h, _ptr(out), 1 if reset else 0))
         return dict(max_faces=int(out[0]), max_edges=int(out[1]), slow_epas=int(out[2]),
                     overflow_candidate=int(out[3]) - 1, overflow_scene=int(out[4]) - 1,
-                    overflows=int(out[5]), warp_tier=int(out[6]))
+                    overflows=int(out[5]), warp_tier=int(out[6]), giant_tier=int(out[7]))
 
     # -- differentiable rollout -------------------------------------------------------
     def diff_forward(self, dt, n, params=None):
