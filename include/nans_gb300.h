@@ -117,6 +117,8 @@ typedef struct nans_contact_pair
                                       NANS_ERR_EPA_CAPACITY; default: that pair gets no
                                       contact (the reference's result for every EPA that does
                                       not converge) and the event is counted */
+#define NANS_WORLD_TEST_GIANT_TIER 4u /* testing: every EPA beyond the warp tier's 128 faces
+                                      runs on the grid-wide tier (results are the same) */
 
 typedef struct nans_world_desc
 {

@@ -385,7 +385,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
         (rc = dalloc(w, L, &d.work_counter, kWorkCounters)) || (rc = dalloc(w, L, &d.status, 1)) ||
         (rc = dalloc(w, L, &d.ovf_cand, kEpaOverflowCap)) || (rc = dalloc(w, L, &d.med_cand, kEpaMediumCap)) ||
-        (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes() * (size_t)kEpaArenaWarps)) ||
+        (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes())) ||
+        (rc = dalloc(w, L, &d.giant_scratch, epa_giant_scratch_bytes())) ||
         (rc = dalloc(w, L, &d.blk_arena, epa_block_bytes() * (size_t)(kBlockPerSm * w->sm_count))) ||
         (rc = dalloc(w, L, &d.giant_cand, kGiantQueueCap)) ||
         (rc = dalloc(w, L, &d.epa_stats, 8)) ||
@@ -410,8 +411,9 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.ovf_cap = kEpaOverflowCap;
     d.med_cap = kEpaMediumCap;
     d.medium_blocks = 2 * w->sm_count;
-    d.epa_arena_warps = kEpaArenaWarps;
+    d.giant_blocks = giant_grid(w->sm_count);
     d.blk_blocks = kBlockPerSm * w->sm_count;
+    d.blk_face_limit = (w->flags & NANS_WORLD_TEST_GIANT_TIER) ? 0 : kBlockFaces;
     d.giant_cap = kGiantQueueCap;
     cudaStream_t st = w->stream;
     CK(cudaMemcpyAsync(p_cube0, sc_cube0.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -435,8 +437,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         CK(cudaMemcpyAsync(w->d_rec_sphere, spheres, ts * sizeof(nans_sphere), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(w->d_rec_floor, floors, S * sizeof(nans_cube), cudaMemcpyHostToDevice, st));
     CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
-    CK(cudaMemsetAsync(d.epa_arena, 0, epa_big_bytes() * (size_t)kEpaArenaWarps, st));
-    CK(cudaMemsetAsync(d.blk_arena, 0, epa_block_bytes() * (size_t)d.blk_blocks, st));
+    CK(cudaMemsetAsync(d.giant_scratch, 0, epa_giant_scratch_bytes(), st));
     CK(cudaMemsetAsync(d.epa_stats, 0, 8 * sizeof(unsigned), st));
     CK(cudaMemsetAsync(d.n_cand, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, S * sizeof(int), st));
@@ -473,11 +474,12 @@ void enqueue_cull(nans_world *w)
         k_cull_write<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
 }
 
-void enqueue_narrow_solve(nans_world *w, float dt)
+cudaError_t enqueue_narrow_solve(nans_world *w, float dt)
 {
     cudaStream_t st = w->stream;
-    launch_narrow(w->narrow_warps, narrow_grid(w), st, w->dw);
+    cudaError_t e = (cudaError_t)launch_narrow(w->narrow_warps, narrow_grid(w), st, w->dw);
     k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+    return e;
 }
 
 int sweep_flags(const nans_world *w)
@@ -541,7 +543,7 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
             CK(cudaGetLastError());
         }
     }
-    enqueue_narrow_solve(w, dt);
+    CK(enqueue_narrow_solve(w, dt));
     CK(cudaGetLastError());
     after_step(w, dt);
     return NANS_OK;
@@ -554,6 +556,8 @@ int check_status(nans_world *w)
     CK(cudaStreamSynchronize(w->stream));
     if (status & ST_CANDIDATES)
         return fail(NANS_ERR_CAPACITY, "step: more candidate pairs than the world's capacity");
+    if (status & ST_EPA_TIMEOUT)
+        return fail(NANS_ERR_EPA_CAPACITY, "step: the large-polytope EPA's grid barrier timed out");
     if ((status & (ST_EPA_FACES | ST_EPA_EDGES)) && (w->flags & NANS_WORLD_STRICT_EPA))
         return fail(NANS_ERR_EPA_CAPACITY, "step: an EPA polytope outgrew the large-polytope buffers");
     return NANS_OK;
@@ -1214,7 +1218,7 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[3], st));
         launch_epa_medium(st, w->dw);
         CK(cudaEventRecord(ev[4], st));
-        launch_narrow_big(st, w->dw);
+        CK((cudaError_t)launch_narrow_big(st, w->dw));
         CK(cudaEventRecord(ev[5], st));
         k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
         CK(cudaEventRecord(ev[6], st));

@@ -17,167 +17,10 @@
 // stored normal bit for bit (same operands, same operations, the flip is an exact negation),
 // so each face's distance |dot(N, A)| is computed once when the face is created.
 // The warp's lanes share the per-face loops; the sequential parts run redundantly.
-#include "nans_kernels.cuh"
+#include "nans_gjk.cuh"
 
 namespace nans
 {
-
-enum
-{
-    G_NOHIT = 0,
-    G_FOUND = 1,
-    G_EVOLVING = 2,
-    G_BUDGET = 3 // still evolving after the caller's budget of EvolveSimplex calls
-};
-
-// TripleCross (code/nans.cpp:564-569): (A x B) x C = B * dot(C, A) - A * dot(C, B)
-__device__ __forceinline__ v3 triple_cross(v3 a, v3 b, v3 c) { return (dot3(c, a) * b) - (dot3(c, b) * a); }
-
-// CheckCollision's GJK loop (at most 65 EvolveSimplex calls). With budget < 65 it stops after
-// `budget` calls and returns G_BUDGET if the simplex is still evolving; rerunning with the
-// full budget reproduces the same sequence from the start.
-__device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,
-                                   GV &s3, int budget = 65)
-{
-    const v3 dir0 = normalize3(B.p - A.p);
-    int n = 0;
-    int res = G_EVOLVING;
-    for (int it = 0; it <= 64; ++it)
-    {
-        if (it >= budget)
-            return G_BUDGET;
-        v3 dir = dir0;
-        if (n == 1)
-        {
-            dir = -1.0f * dir;
-        }
-        else if (n == 2)
-        {
-            // ClosestPointOnLine (code/nans.cpp:539-562)
-            v3 a = s0.p, b = s1.p;
-            v3 l = normalize3(b - a);
-            float ln = len3(l);
-            float v = dot3(-a, l) / ln;
-            float u = dot3(b, l) / ln;
-            v3 cp;
-            if (u <= 0.0f)
-                cp = b;
-            else if (v <= 0.0f)
-                cp = a;
-            else
-                cp = (u * a) + (v * b);
-            if (v <= 0.0f)
-                n = 1;
-            else if (u <= 0.0f)
-            {
-                s0 = s1;
-                n = 1;
-            }
-            dir = -cp;
-        }
-        else if (n == 3)
-        {
-            v3 a0 = -s0.p;
-            v3 e1 = s1.p - s0.p;
-            v3 e2 = s2.p - s0.p;
-            v3 tn = cross3(e1, e2);
-            v3 e1n = cross3(e1, tn);
-            v3 e2n = cross3(tn, e2);
-            if (dot3(e2n, a0) > 0.0f)
-            {
-                if (dot3(e2, a0) > 0.0f)
-                {
-                    dir = triple_cross(e2, a0, e2);
-                    s1 = s2;
-                    n = 2;
-                }
-                else if (dot3(e1, a0) > 0.0f)
-                {
-                    dir = triple_cross(e1, a0, e1);
-                    n = 2;
-                }
-                else
-                {
-                    dir = a0;
-                    n = 1;
-                }
-            }
-            else if (dot3(e1n, a0) > 0.0f)
-            {
-                if (dot3(e1, a0) > 0.0f)
-                {
-                    dir = triple_cross(e1, a0, e1);
-                    n = 2;
-                }
-                else
-                {
-                    dir = a0;
-                    n = 1;
-                }
-            }
-            else if (dot3(tn, a0) > 0.0f)
-            {
-                dir = tn;
-            }
-            else
-            {
-                dir = -tn;
-                GV t = s1;
-                s1 = s2;
-                s2 = t;
-            }
-        }
-        else if (n == 4)
-        {
-            v3 da = s0.p - s3.p;
-            v3 db = s1.p - s3.p;
-            v3 dc = s2.p - s3.p;
-            v3 d0 = -1.0f * s3.p;
-            v3 abd = cross3(da, db);
-            v3 bcd = cross3(db, dc);
-            v3 cad = cross3(dc, da);
-            if (dot3(abd, d0) > 0.0f)
-            {
-                s2 = s3;
-                n = 3;
-                dir = abd;
-            }
-            else if (dot3(bcd, d0) > 0.0f)
-            {
-                s0 = s1;
-                s1 = s2;
-                s2 = s3;
-                n = 3;
-                dir = bcd;
-            }
-            else if (dot3(cad, d0) > 0.0f)
-            {
-                s1 = s2;
-                s2 = s3;
-                n = 3;
-                dir = cad;
-            }
-            else
-                return G_FOUND;
-        }
-        if (len3(dir) <= 0.0001f)
-            return G_NOHIT;
-        GV nv = minkowski_support(verts, A, B, dir);
-        if (n == 0)
-            s0 = nv;
-        else if (n == 1)
-            s1 = nv;
-        else if (n == 2)
-            s2 = nv;
-        else
-            s3 = nv;
-        ++n;
-        res = (dot3(dir, nv.p) >= 0.0f) ? G_EVOLVING : G_NOHIT;
-        if (res != G_EVOLVING)
-            return res;
-    }
-    return G_NOHIT; // iteration cap reached while still evolving: no collision
-}
 
 // Polytope storage of one EPA. The vertex pool holds the GJK tetrahedron plus one support per
 // iteration; faces are an ordered list (vertex indices, normal, cached distance); edges are
@@ -199,12 +42,6 @@ template <int FMAX, int EMAX> struct EpaBuf
 };
 using EpaFast = EpaBuf<kEpaFastFaces, kEpaFastEdges>; // shared memory, one per warp
 
-enum
-{
-    EPA_NONE = 0,
-    EPA_CONTACT = 1,
-    EPA_OVERFLOW = -1
-};
 
 template <class B> __device__ __forceinline__ v3 pool_p(const B &E, int i) { return mk3(E.px[i], E.py[i], E.pz[i]); }
 
@@ -290,13 +127,6 @@ template <class B> __device__ __forceinline__ bool push_edge(B &E, int &ne, int 
     __syncwarp();
     ++ne;
     return true;
-}
-
-// Canonical bits of a coordinate for vertex equality: -0 and +0 compare equal.
-__device__ __forceinline__ unsigned canon_bits(float x)
-{
-    unsigned b = __float_as_uint(x);
-    return (b == 0x80000000u) ? 0u : b;
 }
 
 // ResolveCollision (code/nans.cpp:787-904) on one warp. Returns EPA_CONTACT with the contact
@@ -496,16 +326,6 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
     return EPA_NONE;
 }
 
-__device__ __forceinline__ void write_result(const DevWorld &w, int cc, int res, v3 pa, v3 pb, v3 nn)
-{
-    w.hit[cc] = (res == EPA_CONTACT) ? 1 : 0;
-    if (res == EPA_CONTACT)
-    {
-        w.c_pa[cc] = f4(pa, 0.0f);
-        w.c_pb[cc] = f4(pb, 0.0f);
-        w.c_n[cc] = f4(nn, 0.0f);
-    }
-}
 
 // Queues a candidate whose EPA outgrew the current tier: the warp tier (capacity med_cap),
 // then the large-polytope tier (capacity ovf_cap). The next tier reruns GJK (deterministic,
@@ -818,554 +638,6 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(
     }
 }
 
-// ------------------------------------------------------------------------------------
-// Tier 3: one block per queued candidate, polytope in a per-block global-memory arena.
-//
-// The horizon of a large polytope is built from counts instead of edge by edge. PushEdge
-// cancels the FIRST live stored edge that is the reverse of the pushed one and otherwise
-// appends. Group the pushes by their undirected key {P(u), P(v)} (positions compared with ==):
-// a push only ever cancels an edge of its own group, and the live edges of a group always run
-// in one direction (a push against them cancels one). So, per group, the survivors are exactly
-// the last |#(u,v) - #(v,u)| pushes of the majority direction; for a self-loop key
-// (P(u) == P(v)) the last push survives iff the group has an odd number of pushes; an edge
-// with a NaN coordinate equals nothing and always survives. Survivors keep push order.
-// Counting is parallel (hash table of groups); the "last n" ranks come from one ordered
-// reverse pass over the pushes in warp-sized chunks.
-// ------------------------------------------------------------------------------------
-template <int F, int P, int E, int S> struct EpaArena
-{
-    static constexpr int kFaces = F, kPushes = P, kEdges = E, kSlots = S;
-    float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
-    float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
-    float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
-    float fnx[F], fny[F], fnz[F], fd[F];
-    unsigned fidx[F];                        // a | b << 8 | c << 16
-    unsigned vis[F / 32];
-    int chunk_pre[F / 32];
-    unsigned short push[P];                  // u | v << 8
-    int pslot[P];                            // group slot, -1 for a NaN edge
-    unsigned char pdir[P];                   // 0 / 1 orientation, 2 self-loop
-    unsigned char palive[P];
-    unsigned short edge[E];                  // horizon: u | v << 8
-    unsigned long long skey[S];              // 0 = empty
-    int sfirst[S];
-    int scnt0[S], scnt1[S], squota[S];
-    unsigned char sqdir[S];
-};
-using EpaBlock = EpaArena<kBlockFaces, kBlockPushes, kBlockEdges, kBlockSlots>;
-using EpaGiant = EpaArena<kGiantFaces, kGiantPushes, kGiantEdges, kGiantSlots>;
-
-struct GiantShared
-{
-    float rd[32];
-    int ri[32];
-    int scan[32];
-    int bcast[4];
-};
-
-template <class A> __device__ __forceinline__ v3 gpool(const A &E, int i) { return mk3(E.px[i], E.py[i], E.pz[i]); }
-
-template <class A> __device__ __forceinline__ void gpool_put(A &E, int i, const GV &g)
-{
-    E.px[i] = g.p.x;
-    E.py[i] = g.p.y;
-    E.pz[i] = g.p.z;
-    E.ax[i] = g.sa.x;
-    E.ay[i] = g.sa.y;
-    E.az[i] = g.sa.z;
-    E.bx[i] = g.sb.x;
-    E.by[i] = g.sb.y;
-    E.bz[i] = g.sb.z;
-}
-
-template <class A> __device__ __forceinline__ void gface_put(A &E, int f, int a, int b, int c)
-{
-    v3 pa = gpool(E, a), pb = gpool(E, b), pc = gpool(E, c);
-    v3 n = normalize3(cross3(pb - pa, pc - pa));
-    if (dot3(pa, n) < 0.0f)
-        n = -1.0f * n;
-    E.fidx[f] = (unsigned)a | ((unsigned)b << 8) | ((unsigned)c << 16);
-    E.fnx[f] = n.x;
-    E.fny[f] = n.y;
-    E.fnz[f] = n.z;
-    E.fd[f] = fabsf(dot3(n, pa));
-}
-
-// Block-wide exclusive scan (blockDim a multiple of 32, at most 1024).
-__device__ __forceinline__ int gscan(int v, GiantShared &sh, int &total)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    int x = v;
-    for (int o = 1; o < 32; o <<= 1)
-    {
-        int y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o)
-            x += y;
-    }
-    if (lane == 31)
-        sh.scan[wid] = x;
-    __syncthreads();
-    if (wid == 0)
-    {
-        int t = (lane < nw) ? sh.scan[lane] : 0;
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            int y = __shfl_up_sync(0xffffffffu, t, o);
-            if (lane >= o)
-                t += y;
-        }
-        if (lane < nw)
-            sh.scan[lane] = t;
-    }
-    __syncthreads();
-    int pre = (wid > 0 ? sh.scan[wid - 1] : 0) + x - v;
-    total = sh.scan[nw - 1];
-    __syncthreads();
-    return pre;
-}
-
-// Undirected group key of the edge (u, v): canonical positions ordered lexicographically.
-// Returns false for an edge with a NaN coordinate.
-template <class A>
-__device__ __forceinline__ bool group_key(const A &E, int u, int v, unsigned key[6], int &dir)
-{
-    v3 pu = gpool(E, u), pv = gpool(E, v);
-    if (isnan(pu.x) || isnan(pu.y) || isnan(pu.z) || isnan(pv.x) || isnan(pv.y) || isnan(pv.z))
-        return false;
-    unsigned ku[3] = {canon_bits(pu.x), canon_bits(pu.y), canon_bits(pu.z)};
-    unsigned kv[3] = {canon_bits(pv.x), canon_bits(pv.y), canon_bits(pv.z)};
-    int cmp = 0;
-    for (int q = 0; q < 3 && cmp == 0; ++q)
-        cmp = (ku[q] < kv[q]) ? -1 : (ku[q] > kv[q]) ? 1 : 0;
-    const unsigned *lo = (cmp <= 0) ? ku : kv, *hi = (cmp <= 0) ? kv : ku;
-    for (int q = 0; q < 3; ++q)
-    {
-        key[q] = lo[q];
-        key[3 + q] = hi[q];
-    }
-    dir = (cmp == 0) ? 2 : (cmp < 0 ? 0 : 1);
-    return true;
-}
-
-template <class Arena>
-__device__ int epa_giant(const DevWorld &w, Arena &E, GiantShared &sh, const Shape &A, const Shape &Bs, const GV &s0,
-                         const GV &s1, const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n)
-{
-    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = nt >> 5;
-    if (tid == 0)
-    {
-        gpool_put(E, 0, s0);
-        gpool_put(E, 1, s1);
-        gpool_put(E, 2, s2);
-        gpool_put(E, 3, s3);
-    }
-    __syncthreads();
-    if (tid == 0)
-        gface_put(E, 0, 0, 1, 2);
-    else if (tid == 1)
-        gface_put(E, 1, 0, 2, 3);
-    else if (tid == 2)
-        gface_put(E, 2, 0, 3, 1);
-    else if (tid == 3)
-        gface_put(E, 3, 1, 3, 2);
-    __syncthreads();
-    int nf = 4, nv = 4;
-    bool stale = false;
-    for (int it = 0; it <= 64; ++it)
-    {
-        if (nf == 0 && !stale)
-            return EPA_NONE;
-        // closest face (first minimum; a NaN face 0 stays the closest)
-        int ci = 0;
-        const float d0 = E.fd[0];
-        if (nf > 0 && !isnan(d0))
-        {
-            float bd = d0;
-            int bi = 0;
-            for (int f = tid; f < nf; f += nt)
-            {
-                float d = E.fd[f];
-                if (d < bd || (d == bd && f < bi))
-                {
-                    bd = d;
-                    bi = f;
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1)
-            {
-                float od = __shfl_xor_sync(0xffffffffu, bd, o);
-                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (od < bd || (od == bd && oi < bi))
-                {
-                    bd = od;
-                    bi = oi;
-                }
-            }
-            if (lane == 0)
-            {
-                sh.rd[wid] = bd;
-                sh.ri[wid] = bi;
-            }
-            __syncthreads();
-            if (wid == 0)
-            {
-                bd = (lane < nw) ? sh.rd[lane] : d0;
-                bi = (lane < nw) ? sh.ri[lane] : 0;
-                for (int o = 16; o > 0; o >>= 1)
-                {
-                    float od = __shfl_xor_sync(0xffffffffu, bd, o);
-                    int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                    if (od < bd || (od == bd && oi < bi))
-                    {
-                        bd = od;
-                        bi = oi;
-                    }
-                }
-                if (lane == 0)
-                    sh.bcast[0] = bi;
-            }
-            __syncthreads();
-            ci = sh.bcast[0];
-            __syncthreads();
-        }
-        const float cur = E.fd[ci];
-        const v3 n = mk3(E.fnx[ci], E.fny[ci], E.fnz[ci]);
-        const GV ns = minkowski_support(w.verts, A, Bs, n);
-        if (dot3(n, ns.p) - cur < 0.001f)
-        {
-            unsigned fi = E.fidx[ci];
-            int ia = fi & 0xffu, ib = (fi >> 8) & 0xffu, ic = fi >> 16;
-            v3 pa = gpool(E, ia), pb = gpool(E, ib), pc = gpool(E, ic);
-            v3 p = cur * n;
-            v3 v0 = pb - pa, v1 = pc - pa, v2 = p - pa;
-            float d00 = dot3(v0, v0), d01 = dot3(v0, v1), d11 = dot3(v1, v1);
-            float d20 = dot3(v2, v0), d21 = dot3(v2, v1);
-            float den = d00 * d11 - d01 * d01;
-            float bv = (d11 * d20 - d01 * d21) / den;
-            float bw = (d00 * d21 - d01 * d20) / den;
-            float bu = 1.0f - bv - bw;
-            if (fabsf(bu) > 1.0f || fabsf(bv) > 1.0f || fabsf(bw) > 1.0f)
-                return EPA_NONE;
-            if (!isfinite(bu) || !isfinite(bv) || !isfinite(bw))
-                return EPA_NONE;
-            v3 saa = mk3(E.ax[ia], E.ay[ia], E.az[ia]), sab = mk3(E.ax[ib], E.ay[ib], E.az[ib]),
-               sac = mk3(E.ax[ic], E.ay[ic], E.az[ic]);
-            v3 sba = mk3(E.bx[ia], E.by[ia], E.bz[ia]), sbb = mk3(E.bx[ib], E.by[ib], E.bz[ib]),
-               sbc = mk3(E.bx[ic], E.by[ic], E.bz[ic]);
-            out_pa = ((bu * saa) + (bv * sab)) + (bw * sac);
-            out_n = -1.0f * n;
-            out_pb = ((bu * sba) + (bv * sbb)) + (bw * sbc);
-            return EPA_CONTACT;
-        }
-        if (nf == 0)
-            return EPA_NONE;
-        // visibility bitmask, one 32-face chunk per warp at a time
-        const int nch = (nf + 31) >> 5;
-        for (int ch = wid; ch < nch; ch += nw)
-        {
-            int f = ch * 32 + lane;
-            bool vis = false;
-            if (f < nf)
-            {
-                v3 fa = gpool(E, E.fidx[f] & 0xffu);
-                vis = dot3(mk3(E.fnx[f], E.fny[f], E.fnz[f]), ns.p - fa) > 0.0f;
-            }
-            unsigned bal = __ballot_sync(0xffffffffu, vis);
-            if (lane == 0)
-                E.vis[ch] = bal;
-        }
-        __syncthreads();
-        // visible-face ranks: exclusive prefix of the chunk popcounts
-        int nvis = 0;
-        for (int base = 0; base < nch; base += nt)
-        {
-            int ch = base + tid;
-            int c = (ch < nch) ? __popc(E.vis[ch]) : 0;
-            int tot;
-            int pre = gscan(c, sh, tot);
-            if (ch < nch)
-                E.chunk_pre[ch] = nvis + pre;
-            nvis += tot;
-        }
-        const int m = 3 * nvis;
-        if (m > Arena::kPushes)
-            return EPA_OVERFLOW;
-        __syncthreads();
-        for (int f = tid; f < nf; f += nt)
-        {
-            unsigned vm = E.vis[f >> 5];
-            int bit = f & 31;
-            if ((vm >> bit) & 1u)
-            {
-                int r = E.chunk_pre[f >> 5] + __popc(vm & ((1u << bit) - 1u));
-                unsigned fi = E.fidx[f];
-                unsigned a = fi & 0xffu, b = (fi >> 8) & 0xffu, c = fi >> 16;
-                E.push[3 * r] = (unsigned short)(a | (b << 8));
-                E.push[3 * r + 1] = (unsigned short)(b | (c << 8));
-                E.push[3 * r + 2] = (unsigned short)(c | (a << 8));
-            }
-        }
-        __syncthreads();
-        // group slots and counts
-        for (int k = tid; k < m; k += nt)
-        {
-            unsigned pk = E.push[k];
-            unsigned key[6];
-            int dir;
-            if (!group_key(E, pk & 0xffu, pk >> 8, key, dir))
-            {
-                E.pslot[k] = -1;
-                E.palive[k] = 1;
-                continue;
-            }
-            unsigned long long h = 1469598103934665603ull;
-            for (int q = 0; q < 6; ++q)
-                h = (h ^ key[q]) * 1099511628211ull;
-            h |= 1ull;
-            unsigned s = (unsigned)(h >> 20) & (Arena::kSlots - 1);
-            for (int probe = 0; probe < Arena::kSlots; ++probe)
-            {
-                unsigned long long prev = atomicCAS(&E.skey[s], 0ull, h);
-                if (prev == 0ull)
-                {
-                    E.sfirst[s] = k;
-                    break;
-                }
-                if (prev == h)
-                    break;
-                s = (s + 1) & (Arena::kSlots - 1);
-            }
-            E.pslot[k] = (int)s;
-            E.pdir[k] = (unsigned char)dir;
-            atomicAdd(dir == 1 ? &E.scnt1[s] : &E.scnt0[s], 1);
-        }
-        if (tid == 0)
-            sh.bcast[1] = 0;
-        __syncthreads();
-        // equal 64-bit hashes must mean equal keys; and one thread per group sets its quota
-        for (int k = tid; k < m; k += nt)
-        {
-            int s = E.pslot[k];
-            if (s < 0)
-                continue;
-            int f = E.sfirst[s];
-            if (f != k)
-            {
-                unsigned ka[6], kb[6];
-                int da, db;
-                unsigned pk = E.push[k], pf = E.push[f];
-                group_key(E, pk & 0xffu, pk >> 8, ka, da);
-                group_key(E, pf & 0xffu, pf >> 8, kb, db);
-                for (int q = 0; q < 6; ++q)
-                    if (ka[q] != kb[q])
-                        sh.bcast[1] = 1;
-            }
-            else
-            {
-                int c0 = E.scnt0[s], c1 = E.scnt1[s];
-                if (E.pdir[k] == 2)
-                {
-                    E.squota[s] = c0 & 1;
-                    E.sqdir[s] = 2;
-                }
-                else
-                {
-                    int d = c0 - c1;
-                    E.squota[s] = d >= 0 ? d : -d;
-                    E.sqdir[s] = d >= 0 ? 0 : 1;
-                }
-            }
-        }
-        __syncthreads();
-        const bool collision = sh.bcast[1] != 0;
-        // survivors: the last `quota` pushes of the group's majority direction (reverse pass)
-        if (!collision && wid == 0)
-        {
-            for (int ch = (m - 1) >> 5; ch >= 0; --ch)
-            {
-                int k = ch * 32 + lane;
-                int s = (k < m) ? E.pslot[k] : -1;
-                bool cand = s >= 0 && E.pdir[k] == E.sqdir[s];
-                unsigned peers = __match_any_sync(0xffffffffu, cand ? s : -1 - lane);
-                int alive = 0;
-                if (cand)
-                {
-                    int later = __popc(peers & ~((2u << lane) - 1u));
-                    int leader = 31 - __clz(peers);
-                    int old = 0;
-                    if (lane == leader)
-                    {
-                        old = E.squota[s];
-                        E.squota[s] = old - __popc(peers);
-                    }
-                    old = __shfl_sync(peers, old, leader);
-                    alive = (old - later) > 0 ? 1 : 0;
-                }
-                if (s >= 0)
-                    E.palive[k] = (unsigned char)alive;
-            }
-        }
-        __syncthreads();
-        // clear the group table for the next iteration
-        for (int k = tid; k < m; k += nt)
-        {
-            int s = E.pslot[k];
-            if (s >= 0)
-            {
-                E.skey[s] = 0ull;
-                E.scnt0[s] = 0;
-                E.scnt1[s] = 0;
-            }
-        }
-        if (collision)
-            return EPA_OVERFLOW;
-        // horizon = surviving pushes in push order
-        int ne = 0;
-        for (int base = 0; base < m; base += nt)
-        {
-            int k = base + tid;
-            int al = (k < m) ? E.palive[k] : 0;
-            int tot;
-            int pre = gscan(al, sh, tot);
-            if (al && ne + pre < Arena::kEdges)
-                E.edge[ne + pre] = E.push[k];
-            ne += tot;
-        }
-        if (ne > Arena::kEdges)
-            return EPA_OVERFLOW;
-        // stable removal of the visible faces
-        int keep = 0;
-        for (int base = 0; base < nf; base += nt)
-        {
-            int f = base + tid;
-            bool stay = (f < nf) && !((E.vis[f >> 5] >> (f & 31)) & 1u);
-            int tot;
-            int pre = gscan(stay ? 1 : 0, sh, tot);
-            float nx = 0.f, ny = 0.f, nz = 0.f, d = 0.f;
-            unsigned fi = 0;
-            if (stay)
-            {
-                nx = E.fnx[f];
-                ny = E.fny[f];
-                nz = E.fnz[f];
-                d = E.fd[f];
-                fi = E.fidx[f];
-            }
-            __syncthreads();
-            if (stay)
-            {
-                int dst = keep + pre;
-                E.fnx[dst] = nx;
-                E.fny[dst] = ny;
-                E.fnz[dst] = nz;
-                E.fd[dst] = d;
-                E.fidx[dst] = fi;
-            }
-            keep += tot;
-            __syncthreads();
-        }
-        if (tid == 0)
-        {
-            atomicMax(w.epa_stats + 0, (unsigned)(keep + ne));
-            atomicMax(w.epa_stats + 1, (unsigned)ne);
-        }
-        if (keep + ne > Arena::kFaces)
-            return EPA_OVERFLOW;
-        if (keep == 0 && ne == 0)
-        {
-            // every face removed: slot 0 keeps the last face of the list (nothing was moved)
-            if (tid == 0)
-            {
-                int l = nf - 1;
-                E.fidx[0] = E.fidx[l];
-                E.fnx[0] = E.fnx[l];
-                E.fny[0] = E.fny[l];
-                E.fnz[0] = E.fnz[l];
-                E.fd[0] = E.fd[l];
-            }
-            stale = true;
-        }
-        const int sv = nv++;
-        if (tid == 0)
-            gpool_put(E, sv, ns);
-        __syncthreads();
-        for (int j = tid; j < ne; j += nt)
-        {
-            unsigned ed = E.edge[j];
-            gface_put(E, keep + j, sv, ed & 0xffu, ed >> 8);
-        }
-        __syncthreads();
-        nf = keep + ne;
-    }
-    return EPA_NONE;
-}
-
-// Tier 3 (TIER == 3): the block-EPA queue, arenas of 32,768 faces, many blocks; an EPA that
-// outgrows its arena is queued for tier 4. Tier 4: the giant queue, arenas of 2,097,152
-// faces, a few blocks; beyond that the pair gets no contact.
-template <class Arena, int TIER, int THREADS>
-__global__ void __launch_bounds__(THREADS) k_narrow_big(DevWorld w)
-{
-    __shared__ GiantShared sh;
-    __shared__ int s_q;
-    unsigned char *base = (TIER == 3) ? w.blk_arena : w.epa_arena;
-    Arena &E = *reinterpret_cast<Arena *>(base + (size_t)blockIdx.x * sizeof(Arena));
-    const int n = (TIER == 3) ? min(w.work_counter[3], w.ovf_cap) : min(w.work_counter[8], w.giant_cap);
-    const int *queue = (TIER == 3) ? w.ovf_cand : w.giant_cand;
-    int *head = w.work_counter + ((TIER == 3) ? 2 : 9);
-    for (;;)
-    {
-        if (threadIdx.x == 0)
-            s_q = atomicAdd(head, 1);
-        __syncthreads();
-        const int q = s_q;
-        __syncthreads();
-        if (q >= n)
-            break;
-        const int cc = queue[q];
-        const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
-        GV s0, s1, s2, s3;
-        gjk(w.verts, A, B, s0, s1, s2, s3); // every thread: same inputs, same simplex
-        v3 pa, pb, nn;
-        int r = epa_giant(w, E, sh, A, B, s0, s1, s2, s3, pa, pb, nn);
-        __syncthreads();
-        if (threadIdx.x == 0)
-        {
-            if (TIER == 3)
-                atomicAdd(w.epa_stats + 2, 1u);
-            bool done = true;
-            if (r == EPA_OVERFLOW && TIER == 3)
-            {
-                int g = atomicAdd(w.work_counter + 8, 1);
-                if (g < w.giant_cap)
-                {
-                    w.giant_cand[g] = cc;
-                    atomicAdd(w.epa_stats + 7, 1u);
-                    w.hit[cc] = 0;
-                    done = false;
-                }
-            }
-            if (done)
-            {
-                if (r == EPA_OVERFLOW)
-                {
-                    // Beyond the arena the pair gets no contact, which is what the reference
-                    // returns for every EPA that does not converge within its 65 iterations.
-                    atomicOr(w.status, (unsigned)ST_EPA_FACES);
-                    atomicAdd(w.epa_stats + 5, 1u);
-                    w.epa_stats[3] = (unsigned)cc + 1u;
-                    w.epa_stats[4] = (unsigned)(w.cand_meta[cc] >> 3) + 1u;
-                    r = EPA_NONE;
-                }
-                write_result(w, cc, r, pa, pb, nn);
-            }
-        }
-        __syncthreads();
-    }
-}
-
-size_t epa_big_bytes() { return sizeof(EpaGiant); }
-size_t epa_block_bytes() { return sizeof(EpaBlock); }
 
 
 static size_t medium_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }
@@ -1406,16 +678,11 @@ void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
     launch_epa_medium(st, w);
 }
 
-void launch_narrow_big(cudaStream_t st, const DevWorld &w)
-{
-    k_narrow_big<EpaBlock, 3, kBlockThreads><<<w.blk_blocks, kBlockThreads, 0, st>>>(w);
-    k_narrow_big<EpaGiant, 4, kGiantThreads><<<w.epa_arena_warps, kGiantThreads, 0, st>>>(w);
-}
 
-void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
+int launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
 {
     launch_narrow_fast(warps, grid, st, w);
-    launch_narrow_big(st, w);
+    return launch_narrow_big(st, w);
 }
 
 } // namespace nans

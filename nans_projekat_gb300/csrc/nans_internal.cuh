@@ -43,6 +43,7 @@ enum StatusBits
     ST_CANDIDATES = 1u << 2,     // candidate capacity exceeded
     ST_EPA_EMPTY = 1u << 3,      // EPA face list emptied (reference would read a stale face)
     ST_SOLVER_BODIES = 1u << 4,  // scene too large for the solver's wave table
+    ST_EPA_TIMEOUT = 1u << 5,    // a giant-tier grid barrier timed out (pair: no contact)
 };
 
 struct DevWorld
@@ -91,10 +92,12 @@ struct DevWorld
     int *ovf_cand;                      // candidates queued for the block tier
     unsigned char *blk_arena;           // block-tier polytope buffers, one per block
     int blk_blocks;                     // block-tier grid
+    int blk_face_limit;                 // block-tier face capacity (lowered only by a test flag)
     int giant_cap;                      // giant-EPA queue capacity
     int *giant_cand;                    // candidates queued for the giant tier
-    unsigned char *epa_arena;           // giant-tier polytope buffers, one per block
-    int epa_arena_warps;                // giant-tier grid
+    unsigned char *epa_arena;           // giant-tier polytope buffers (one, grid-wide)
+    unsigned char *giant_scratch;       // giant-tier group table, team scratch and barrier
+    int giant_blocks;                   // giant-tier grid (cooperative launch)
     unsigned *epa_stats;                // [0] max faces, [1] max horizon edges, [2] block- and
                                         // giant-tier EPAs, [3] overflowing candidate + 1, [4] its
                                         // scene + 1, [5] EPAs that outgrew the giant tier, [6]

@@ -30,24 +30,17 @@ constexpr int kPairsPerBlock = kCullThreads * kPairsPerThread;
 // 139,111-edge horizon (the reference's own algorithm needs 334 s of one CPU core for it).
 // Tier 1 runs EPA per thread (12 vertices, 20 faces, 12 edges); tier 2 per warp in shared
 // memory (128 faces, 32 edges); tier 3 per block in a global-memory arena of 32,768 faces,
-// two blocks per SM; tier 4 per block in an arena of 2,097,152 faces, 4,194,304 horizon
-// pushes and 1,048,576 horizon edges. Beyond that the pair gets no contact and the event is
+// two blocks per SM; tier 4 on the whole grid (cooperative launch) in an arena of 8,388,608
+// faces and 4,194,304 horizon edges. Beyond that the pair gets no contact and the event is
 // counted (NANS_ERR_EPA_CAPACITY in strict worlds).
 constexpr int kEpaMaxVerts = 72;
 constexpr int kEpaFastFaces = 128;
 constexpr int kEpaFastEdges = 32;
-constexpr int kBlockFaces = 1 << 15;
-constexpr int kBlockPushes = 1 << 16;
+constexpr int kBlockFaces = 1 << 15;   // tier 3 arena (two blocks per SM)
 constexpr int kBlockEdges = 1 << 15;
-constexpr int kBlockSlots = 1 << 17;
-constexpr int kBlockThreads = 256;
 constexpr int kBlockPerSm = 2;
-constexpr int kGiantFaces = 1 << 21;
-constexpr int kGiantPushes = 1 << 22;
-constexpr int kGiantEdges = 1 << 20;
-constexpr int kGiantSlots = 1 << 23;   // group table, load factor <= 1/2
-constexpr int kGiantThreads = 512;
-constexpr int kEpaArenaWarps = 4;      // tier-4 blocks, one ~330 MB arena each
+constexpr int kGiantFaces = 1 << 23;   // tier 4 arena (one, the whole grid per EPA)
+constexpr int kGiantEdges = 1 << 22;
 constexpr int kEpaOverflowCap = 65536; // tier-3 EPAs queued per step
 constexpr int kGiantQueueCap = 4096;   // tier-4 EPAs queued per step
 constexpr int kWorkCounters = 16;
@@ -68,9 +61,11 @@ __global__ void k_cull_write(DevWorld w);
 int narrow_blocks_per_sm(int warps);
 size_t epa_big_bytes();
 size_t epa_block_bytes();
-void launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w);
+size_t epa_giant_scratch_bytes();
+int giant_grid(int sm_count);
+int launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w);
 void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w);
-void launch_narrow_big(cudaStream_t st, const DevWorld &w);
+int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaError_t
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
 __global__ void k_solve(DevWorld w, float dt);

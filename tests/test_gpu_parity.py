@@ -34,8 +34,8 @@ def test_device_sincos_matches_oracle(nl, oracle_lib):
     assert np.all(np.isnan(s_d[~fin])) and np.all(np.isnan(c_d[~fin]))
 
 
-def _run_plain_digests(nl, scene, nsteps, all_pairs=False):
-    w = nl.World(all_pairs=all_pairs)
+def _run_plain_digests(nl, scene, nsteps, all_pairs=False, giant_tier_only=False):
+    w = nl.World(all_pairs=all_pairs, giant_tier_only=giant_tier_only)
     w.upload(scene)
     dt = np.float32(scene.constants.dt)
     out = []
@@ -61,6 +61,38 @@ def test_plain_step_reproduces_reference_golden(nl, case):
             assert ok, (f, first_difference(saved["cubes_%d" % k], cubes, STATE_FIELDS))
             assert same_fields(saved["spheres_%d" % k], spheres, STATE_FIELDS)[0]
             assert same_fields(saved["pairs_%d" % k], pairs, PAIR_FIELDS)[0]
+
+
+LARGE_EPA_CASES = [c for c in GOLDEN_CASES if "bigepa" in c or "emptied" in c]
+
+
+@pytest.mark.parametrize("case", LARGE_EPA_CASES)
+def test_grid_wide_epa_tier_reproduces_reference_golden(nl, case):
+    """The same reference fixtures with every EPA beyond the warp tier's 128 faces routed to the
+    grid-wide tier (cooperative launch) instead of the per-block tier."""
+    scene, meta, digests, _ = load_golden(case)
+    res = _run_plain_digests(nl, scene, meta["nsteps"], giant_tier_only=True)
+    for k, (d, _, _, _) in enumerate(res, start=1):
+        if d != digests[k - 1]:
+            pytest.fail("%s: step %d differs from the reference" % (case, k))
+
+
+def test_grid_wide_epa_tier_in_graphs(nl):
+    """The grid-wide tier inside the batched path's CUDA graphs: the large-EPA fixtures as one
+    batch, final state and contacts against the reference's digests."""
+    cases = [load_golden(c) for c in LARGE_EPA_CASES]
+    dt = np.float32(cases[0][0].constants.dt)
+    cases = [c for c in cases if np.float32(c[0].constants.dt) == dt and
+             c[0].rebuild_models == cases[0][0].rebuild_models]
+    n = min(c[1]["nsteps"] for c in cases)
+    w = nl.World(giant_tier_only=True)
+    w.upload_batch([c[0] for c in cases])
+    w.batch_step(dt, n, graph_steps=max(1, n // 3))
+    state = w.download()
+    for i, (_, _, digests, _) in enumerate(cases):
+        cubes, spheres, _ = w.scene_state(i, state)
+        assert step_digest(cubes, spheres, w.pairs(i)) == digests[n - 1], LARGE_EPA_CASES[i]
+    w.close()
 
 
 def test_demo_frames_model_and_vertices(nl):
