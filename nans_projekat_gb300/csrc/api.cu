@@ -1241,9 +1241,9 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
 {
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
-    // sweep, [mask, write], scan, narrow_tiny, narrow_long, epa_medium, block EPA, giant EPA,
+    // sweep, [mask, write], scan, gjk, gjk_long, epa_tiny, epa_medium, block EPA, giant EPA,
     // solve
-    uint32_t k = 8 + (w->cull_blocks > 0 ? 2u : 0u);
+    uint32_t k = 9 + (w->cull_blocks > 0 ? 2u : 0u);
     if (batched)
         *batched = k;
     if (plain)

@@ -17,6 +17,8 @@
 // stored normal bit for bit (same operands, same operations, the flip is an exact negation),
 // so each face's distance |dot(N, A)| is computed once when the face is created.
 // The warp's lanes share the per-face loops; the sequential parts run redundantly.
+#include <algorithm>
+
 #include "nans_gjk.cuh"
 
 namespace nans
@@ -539,40 +541,82 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
     return EPA_NONE;
 }
 
-// GJK then per-thread EPA for candidate c; with a budget below 65, a GJK still evolving is
-// queued for the long pass instead.
-__device__ __forceinline__ void narrow_one(const DevWorld &w, TinySmem &S, int t, int c, int budget)
+// GJK and the per-thread EPA run as separate kernels. The GJK pass keeps its registers low
+// and its code small; a hit's final simplex (4 x (P, SupA, SupB), 36 floats) goes to the
+// candidate's solver-constant slot (s_k, 9 float4, written only later by the solver) and the
+// candidate to a compact queue (s_order, likewise free until the solver), so the EPA pass runs
+// only hits, every lane on an EPA.
+__device__ __forceinline__ void store_simplex(const DevWorld &w, int c, const GV &s0, const GV &s1, const GV &s2,
+                                              const GV &s3)
+{
+    float4 *o = w.s_k + 9 * (size_t)c;
+    o[0] = make_float4(s0.p.x, s0.p.y, s0.p.z, s0.sa.x);
+    o[1] = make_float4(s0.sa.y, s0.sa.z, s0.sb.x, s0.sb.y);
+    o[2] = make_float4(s0.sb.z, s1.p.x, s1.p.y, s1.p.z);
+    o[3] = make_float4(s1.sa.x, s1.sa.y, s1.sa.z, s1.sb.x);
+    o[4] = make_float4(s1.sb.y, s1.sb.z, s2.p.x, s2.p.y);
+    o[5] = make_float4(s2.p.z, s2.sa.x, s2.sa.y, s2.sa.z);
+    o[6] = make_float4(s2.sb.x, s2.sb.y, s2.sb.z, s3.p.x);
+    o[7] = make_float4(s3.p.y, s3.p.z, s3.sa.x, s3.sa.y);
+    o[8] = make_float4(s3.sa.z, s3.sb.x, s3.sb.y, s3.sb.z);
+}
+
+__device__ __forceinline__ void load_simplex(const DevWorld &w, int c, GV &s0, GV &s1, GV &s2, GV &s3)
+{
+    const float4 *o = w.s_k + 9 * (size_t)c;
+    const float4 q0 = o[0], q1 = o[1], q2 = o[2], q3 = o[3], q4 = o[4], q5 = o[5], q6 = o[6], q7 = o[7], q8 = o[8];
+    s0.p = mk3(q0.x, q0.y, q0.z);
+    s0.sa = mk3(q0.w, q1.x, q1.y);
+    s0.sb = mk3(q1.z, q1.w, q2.x);
+    s1.p = mk3(q2.y, q2.z, q2.w);
+    s1.sa = mk3(q3.x, q3.y, q3.z);
+    s1.sb = mk3(q3.w, q4.x, q4.y);
+    s2.p = mk3(q4.z, q4.w, q5.x);
+    s2.sa = mk3(q5.y, q5.z, q5.w);
+    s2.sb = mk3(q6.x, q6.y, q6.z);
+    s3.p = mk3(q6.w, q7.x, q7.y);
+    s3.sa = mk3(q7.z, q7.w, q8.x);
+    s3.sb = mk3(q8.y, q8.z, q8.w);
+}
+
+// Appends c to the EPA queue when `hit` (one atomic per warp).
+__device__ __forceinline__ void enqueue_epa(const DevWorld &w, int c, bool hit)
+{
+    const unsigned act = __activemask();
+    const unsigned bal = __ballot_sync(act, hit);
+    if (!hit)
+        return;
+    const int lane = threadIdx.x & 31, leader = __ffs(bal) - 1;
+    int base = 0;
+    if (lane == leader)
+        base = atomicAdd(w.work_counter + 10, __popc(bal));
+    base = __shfl_sync(bal, base, leader);
+    w.s_order[base + __popc(bal & ((1u << lane) - 1u))] = c;
+}
+
+// GJK of candidate c; with a budget below 65, a GJK still evolving is queued for the long pass.
+__device__ __forceinline__ void gjk_one(const DevWorld &w, int c, int budget)
 {
     const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
     GV s0, s1, s2, s3;
-    int g = gjk(w.verts, A, B, s0, s1, s2, s3, budget);
-    if (g == G_BUDGET)
-    {
+    const int g = gjk(w.verts, A, B, s0, s1, s2, s3, budget);
+    if (g == G_FOUND)
+        store_simplex(w, c, s0, s1, s2, s3);
+    else if (g == G_BUDGET)
         w.long_cand[atomicAdd(w.work_counter + 7, 1)] = c;
-        return;
-    }
-    if (g != G_FOUND)
-    {
-        w.hit[c] = 0;
-        return;
-    }
-    v3 pa, pb, nn;
-    int r = epa_tiny(w, S, t, A, B, s0, s1, s2, s3, pa, pb, nn);
-    if (r == EPA_OVERFLOW)
-        escalate(w, c, false);
     else
-        write_result(w, c, r, pa, pb, nn);
+        w.hit[c] = 0;
+    enqueue_epa(w, c, g == G_FOUND);
 }
 
 // Persistent: warps take 32 candidates at a time from a global queue; each lane runs GJK
-// (budget kGjkShort calls) and, on a hit, EPA; EPAs that outgrow the per-thread polytope are
-// queued for the warp tier, GJKs that need more calls for the long pass, so that the rare
+// (budget kGjkShort calls); GJKs that need more calls go to the long pass, so that the rare
 // long GJK runs share warps with each other instead of stalling 31 finished lanes.
 constexpr int kGjkShort = 8;
-__global__ void __launch_bounds__(kTinyThreads) k_narrow_tiny(DevWorld w)
+constexpr int kGjkThreads = 128;
+__global__ void __launch_bounds__(kGjkThreads) k_gjk(DevWorld w)
 {
-    __shared__ TinySmem S;
-    const int lane = threadIdx.x & 31, t = threadIdx.x;
+    const int lane = threadIdx.x & 31;
     const int n = *w.n_cand;
     for (;;)
     {
@@ -590,18 +634,47 @@ __global__ void __launch_bounds__(kTinyThreads) k_narrow_tiny(DevWorld w)
             w.cand_begin[sc] = c;
         if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
             w.cand_end[sc] = c + 1;
-        narrow_one(w, S, t, c, kGjkShort);
+        gjk_one(w, c, kGjkShort);
     }
 }
 
 // The long pass: candidates whose GJK needed more than kGjkShort calls, rerun in full.
-__global__ void __launch_bounds__(kTinyThreads) k_narrow_long(DevWorld w)
+__global__ void __launch_bounds__(kGjkThreads) k_gjk_long(DevWorld w)
+{
+    const int n = w.work_counter[7];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        gjk_one(w, w.long_cand[i], 65);
+}
+
+// Tier 1 EPA: one thread per hit from the queue; EPAs that outgrow the per-thread polytope
+// are queued for the warp tier.
+__global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
 {
     __shared__ TinySmem S;
-    const int t = threadIdx.x;
-    const int n = w.work_counter[7];
-    for (int i = blockIdx.x * blockDim.x + t; i < n; i += gridDim.x * blockDim.x)
-        narrow_one(w, S, t, w.long_cand[i], 65);
+    const int lane = threadIdx.x & 31, t = threadIdx.x;
+    const int n = w.work_counter[10];
+    for (;;)
+    {
+        int base = 0;
+        if (lane == 0)
+            base = atomicAdd(w.work_counter + 11, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const int i = base + lane;
+        if (i >= n)
+            continue;
+        const int c = w.s_order[i];
+        const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
+        GV s0, s1, s2, s3;
+        load_simplex(w, c, s0, s1, s2, s3);
+        v3 pa, pb, nn;
+        const int r = epa_tiny(w, S, t, A, B, s0, s1, s2, s3, pa, pb, nn);
+        if (r == EPA_OVERFLOW)
+            escalate(w, c, false);
+        else
+            write_result(w, c, r, pa, pb, nn);
+    }
 }
 
 // Tier 2: one warp per queued candidate, polytope of up to 128 faces in shared memory.
@@ -655,14 +728,29 @@ int narrow_blocks_per_sm(int warps)
 {
     (void)warps;
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_narrow_tiny, kTinyThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gjk, kGjkThreads, 0);
     return per;
+}
+
+static int epa_tiny_grid()
+{
+    static int grid = 0;
+    if (grid == 0)
+    {
+        int dev = 0, sms = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_epa_tiny, kTinyThreads, 0);
+        grid = std::max(1, per) * std::max(1, sms);
+    }
+    return grid;
 }
 
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w)
 {
-    k_narrow_tiny<<<grid, kTinyThreads, 0, st>>>(w);
-    k_narrow_long<<<grid, kTinyThreads, 0, st>>>(w);
+    k_gjk<<<grid, kGjkThreads, 0, st>>>(w);
+    k_gjk_long<<<grid, kGjkThreads, 0, st>>>(w);
+    k_epa_tiny<<<epa_tiny_grid(), kTinyThreads, 0, st>>>(w);
 }
 
 void launch_epa_medium(cudaStream_t st, const DevWorld &w)

@@ -83,7 +83,9 @@ struct DevWorld
     int *work_counter;                  // [0] narrowphase head, [1] solver head, [2] block-EPA
                                         // head, [3] block-EPA queue length, [5] warp-EPA queue
                                         // length, [6] warp-EPA head, [7] long-GJK queue length,
-                                        // [8] giant-EPA queue length, [9] giant-EPA head
+                                        // [8] giant-EPA queue length, [9] giant-EPA head,
+                                        // [10] per-thread EPA queue length (queue: s_order),
+                                        // [11] per-thread EPA head
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
     int *long_cand;                     // candidates whose GJK needs the long pass
@@ -104,8 +106,9 @@ struct DevWorld
                                         // EPAs escalated to the warp tier, [7] EPAs escalated to
                                         // the giant tier
     // solver scratch, per candidate slot
-    int *s_order, *s_wave, *s_perm, *s_wcnt;
-    float4 *s_k;                        // 9 float4 of per-contact constants
+    int *s_order, *s_wave, *s_perm, *s_wcnt; // s_order doubles as the narrowphase's EPA queue
+    float4 *s_k;                        // 9 float4 of per-contact constants; during the
+                                        // narrowphase the GJK simplex of a hit
     int *s_last;                        // per body: last wave touching it
     float4 *s_fwd;                      // adjoint tape of the solve (2 float4 per slot) or null
     int *s_maxw;                        // per scene: highest wave of the last solve, or null
