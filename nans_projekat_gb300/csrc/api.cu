@@ -43,7 +43,6 @@ int fail(int code, const std::string &msg)
             return fail(NANS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));                         \
     } while (0)
 
-constexpr int kSolveThreadsHost = 256;
 } // namespace
 
 // Lets other translation units of the library report through nans_last_error().
@@ -162,7 +161,7 @@ size_t solve_smem(const nans_world *w) { return (size_t)std::max(1, w->max_scene
 int solve_grid(nans_world *w)
 {
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve, kSolveThreadsHost, solve_smem(w));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve, solve_threads(), solve_smem(w));
     if (per < 1)
         per = 1;
     if (w->solve_bpsm > 0)
@@ -478,7 +477,7 @@ cudaError_t enqueue_narrow_solve(nans_world *w, float dt)
 {
     cudaStream_t st = w->stream;
     cudaError_t e = (cudaError_t)launch_narrow(w->narrow_warps, narrow_grid(w), st, w->dw);
-    k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+    k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt);
     return e;
 }
 
@@ -1220,7 +1219,7 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[4], st));
         CK((cudaError_t)launch_narrow_big(st, w->dw));
         CK(cudaEventRecord(ev[5], st));
-        k_solve<<<solve_grid(w), kSolveThreadsHost, solve_smem(w), st>>>(w->dw, dt);
+        k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());
         after_step(w, dt);

@@ -614,7 +614,8 @@ __device__ __forceinline__ void gjk_one(const DevWorld &w, int c, int budget)
 // long GJK runs share warps with each other instead of stalling 31 finished lanes.
 constexpr int kGjkShort = 8;
 constexpr int kGjkThreads = 128;
-__global__ void __launch_bounds__(kGjkThreads) k_gjk(DevWorld w)
+// six blocks per SM (at most 85 registers): measured best against 4, 5 and 8
+__global__ void __launch_bounds__(kGjkThreads, 6) k_gjk(DevWorld w)
 {
     const int lane = threadIdx.x & 31;
     const int n = *w.n_cand;
@@ -639,7 +640,7 @@ __global__ void __launch_bounds__(kGjkThreads) k_gjk(DevWorld w)
 }
 
 // The long pass: candidates whose GJK needed more than kGjkShort calls, rerun in full.
-__global__ void __launch_bounds__(kGjkThreads) k_gjk_long(DevWorld w)
+__global__ void __launch_bounds__(kGjkThreads, 6) k_gjk_long(DevWorld w)
 {
     const int n = w.work_counter[7];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)

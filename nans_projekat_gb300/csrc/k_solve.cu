@@ -18,8 +18,13 @@
 namespace nans
 {
 
-constexpr int kSolveThreads = 256;
-constexpr int kWaveChunk = 1024;
+// One scene per block; the waves are latency-bound (a contact's 10-iteration loop per wave),
+// so small blocks let many scenes share an SM.
+#ifndef NANS_SOLVE_THREADS
+#define NANS_SOLVE_THREADS 64
+#endif
+constexpr int kSolveThreads = NANS_SOLVE_THREADS;
+constexpr int kWaveChunk = 512;
 
 __device__ __forceinline__ int block_scan_excl(int v, int *sh, int *total)
 {
@@ -92,18 +97,17 @@ __device__ __forceinline__ void contact_constants(const DevWorld &w, int c, floa
     k[8] = make_float4(r2t2.x, r2t2.y, r2t2.z, 0.0f);
 }
 
-// sqrt(2) * Cf * Sum in double, stored to float (code/nans.cpp:1199, 1214)
-__device__ __forceinline__ float friction_bound(float cf, float sum)
-{
-    return (float)(1.4142135623730951 * (double)cf * (double)sum);
-}
+// sqrt(2) * Cf * Sum in double, stored to float (code/nans.cpp:1199, 1214). The product is
+// evaluated left to right, so sqrt(2) * Cf (c2) is computed once per scene.
+__device__ __forceinline__ double friction_scale(float cf) { return 1.4142135623730951 * (double)cf; }
+__device__ __forceinline__ float friction_bound(double c2, float sum) { return (float)(c2 * (double)sum); }
 
 // Velocity-dependent part of Constraint (code/nans.cpp:1149-1156, 1171-1328). With a tape
 // attached (w.s_fwd) it also records, per contact, what the adjoint needs: the relative
 // normal / tangent velocities, the applied impulses and the active set of the closed form
 // (normal impulse max(Ln, 0), tangent impulses clamp(Lt, -mu*Ln, mu*Ln)).
 __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const float4 *k, float cr, float cf,
-                                              int iters)
+                                              double c2, int iters)
 {
     int a = w.cand_a[c], b = w.cand_b[c];
     int type = w.cand_meta[c] & 7;
@@ -129,7 +133,7 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
         float lt1 = (-jdvt1) * jt1;
         old = st1;
         st1 = st1 + lt1;
-        float m1 = friction_bound(cf, sn);
+        float m1 = friction_bound(c2, sn);
         if (st1 < -m1)
             st1 = -m1;
         if (st1 > m1)
@@ -138,7 +142,7 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
         float lt2 = (-jdvt2) * jt2;
         old = st2;
         st2 = st2 + lt2;
-        float m2 = friction_bound(cf, sn);
+        float m2 = friction_bound(c2, sn);
         if (st2 < -m2)
             st2 = -m2;
         if (st2 > m2)
@@ -312,6 +316,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt)
         __syncthreads();
         // (5) waves in order
         const float cr = w.sc_cr[s], cf = w.sc_cf[s];
+        const double c2 = friction_scale(cf);
         const int iters = w.sc_iters[s];
         for (int wv = 1; wv <= maxw; ++wv)
         {
@@ -323,7 +328,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt)
 #pragma unroll
                 for (int q = 0; q < 9; ++q)
                     k[q] = __ldcg(w.s_k + (size_t)9 * c + q);
-                contact_apply(w, c, k, cr, cf, iters);
+                contact_apply(w, c, k, cr, cf, c2, iters);
             }
             __syncthreads();
         }
@@ -374,5 +379,7 @@ __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int 
     if (threadIdx.x == 0)
         *count = n;
 }
+
+int solve_threads() { return kSolveThreads; }
 
 } // namespace nans
