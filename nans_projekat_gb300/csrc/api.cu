@@ -60,6 +60,8 @@ struct nans_world
     uint32_t flags = 0;
     uint32_t max_cand_req = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t stream2 = nullptr;   // the later EPA tiers, alongside the first solve pass
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int sm_count = 0;
 
     int n_scenes = 0, n_dyn = 0, n_all = 0, n_cubes = 0, n_spheres = 0;
@@ -382,6 +384,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.pair_mask, (size_t)((pair_acc + 31) / 32))) ||
         (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.n_cand, 1)) ||
         (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
+        (rc = dalloc(w, L, &d.scene_late, S)) || (rc = dalloc(w, L, &d.late_list, S)) ||
         (rc = dalloc(w, L, &d.work_counter, kWorkCounters)) || (rc = dalloc(w, L, &d.status, 1)) ||
         (rc = dalloc(w, L, &d.ovf_cand, kEpaOverflowCap)) || (rc = dalloc(w, L, &d.med_cand, kEpaMediumCap)) ||
         (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes())) ||
@@ -441,6 +444,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     CK(cudaMemsetAsync(d.n_cand, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, S * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, S * sizeof(int), st));
+    CK(cudaMemsetAsync(d.scene_late, 0, S * sizeof(int), st));
     const int mode = 1 | ((flags & NANS_UPLOAD_KEEP_MODEL) ? 2 : 0);
     k_unpack<<<(nall + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(
         d, w->d_rec_cube, w->d_rec_sphere, w->d_rec_floor, w->d_body_rec, mode, w->d_prm, w->d_model_in);
@@ -473,12 +477,27 @@ void enqueue_cull(nans_world *w)
         k_cull_write<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
 }
 
+// Narrowphase and solve. The EPA tiers beyond the per-thread one run on the second stream
+// while the first solve pass handles every scene they do not touch; the second pass solves
+// the rest after them. Both streams are joined before the function returns (also under
+// stream capture).
 cudaError_t enqueue_narrow_solve(nans_world *w, float dt)
 {
-    cudaStream_t st = w->stream;
-    cudaError_t e = (cudaError_t)launch_narrow(w->narrow_warps, narrow_grid(w), st, w->dw);
-    k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt);
-    return e;
+    cudaStream_t st = w->stream, st2 = w->stream2;
+    launch_narrow_tiny(narrow_grid(w), st, w->dw);
+    cudaError_t e = cudaEventRecord(w->ev_fork, st);
+    if (e == cudaSuccess)
+        e = cudaStreamWaitEvent(st2, w->ev_fork, 0);
+    if (e != cudaSuccess)
+        return e;
+    launch_epa_medium(st2, w->dw);
+    e = (cudaError_t)launch_narrow_big(st2, w->dw);
+    k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt, 0);
+    cudaError_t e2 = cudaEventRecord(w->ev_join, st2);
+    if (e2 == cudaSuccess)
+        e2 = cudaStreamWaitEvent(st, w->ev_join, 0);
+    k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt, 1);
+    return e != cudaSuccess ? e : e2;
 }
 
 int sweep_flags(const nans_world *w)
@@ -512,6 +531,7 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
     CK(cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
+    CK(cudaMemsetAsync(d.scene_late, 0, w->n_scenes * sizeof(int), st));
     k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
                                                                                        sweep_flags(w));
     enqueue_cull(w);
@@ -591,6 +611,7 @@ int ensure_graph(nans_world *w, float dt, int gsteps)
         cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st);
         cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st);
         cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st);
+        cudaMemsetAsync(d.scene_late, 0, w->n_scenes * sizeof(int), st);
         k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, dt, dt,
                                                                                            SW_INTEGRATE | SW_APPLY_VEL);
         enqueue_cull(w);
@@ -733,9 +754,23 @@ int nans_world_create(const nans_world_desc *desc, nans_world **out)
     if (e == cudaSuccess)
         e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess)
+        e = cudaStreamCreateWithFlags(&w->stream2, cudaStreamNonBlocking);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&w->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess)
+        e = cudaEventCreateWithFlags(&w->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&w->sm_count, cudaDevAttrMultiProcessorCount, w->device);
     if (e != cudaSuccess)
     {
+        if (w->stream)
+            cudaStreamDestroy(w->stream);
+        if (w->stream2)
+            cudaStreamDestroy(w->stream2);
+        if (w->ev_fork)
+            cudaEventDestroy(w->ev_fork);
+        if (w->ev_join)
+            cudaEventDestroy(w->ev_join);
         delete w;
         return fail(NANS_ERR_CUDA, std::string("create: ") + cudaGetErrorString(e));
     }
@@ -763,6 +798,12 @@ int nans_world_destroy(nans_world *w)
         cudaFree(w->d_tape);
     if (w->stream)
         cudaStreamDestroy(w->stream);
+    if (w->stream2)
+        cudaStreamDestroy(w->stream2);
+    if (w->ev_fork)
+        cudaEventDestroy(w->ev_fork);
+    if (w->ev_join)
+        cudaEventDestroy(w->ev_join);
     delete w;
     return NANS_OK;
 }
@@ -1207,6 +1248,8 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
+        CK(cudaMemsetAsync(d.scene_late, 0, w->n_scenes * sizeof(int), st));
+    CK(cudaMemsetAsync(d.scene_late, 0, w->n_scenes * sizeof(int), st));
         CK(cudaEventRecord(ev[0], st));
         k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
                                                                                            sweep_flags(w));
@@ -1219,7 +1262,8 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[4], st));
         CK((cudaError_t)launch_narrow_big(st, w->dw));
         CK(cudaEventRecord(ev[5], st));
-        k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt);
+        k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt, 0);
+        k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt, 1);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());
         after_step(w, dt);
@@ -1241,8 +1285,8 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
     // sweep, [mask, write], scan, gjk, gjk_long, epa_tiny, epa_medium, block EPA, giant EPA,
-    // solve
-    uint32_t k = 9 + (w->cull_blocks > 0 ? 2u : 0u);
+    // solve (two passes)
+    uint32_t k = 10 + (w->cull_blocks > 0 ? 2u : 0u);
     if (batched)
         *batched = k;
     if (plain)

@@ -335,6 +335,9 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
 __device__ __forceinline__ void escalate(const DevWorld &w, int c, bool to_big)
 {
     w.hit[c] = 0;
+    const int sc = w.cand_meta[c] >> 3;
+    if (atomicExch(w.scene_late + sc, 1) == 0)
+        w.late_list[atomicAdd(w.work_counter + 13, 1)] = sc;
     if (!to_big)
     {
         atomicAdd(w.epa_stats + 6, 1u);
@@ -768,10 +771,6 @@ void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
 }
 
 
-int launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w)
-{
-    launch_narrow_fast(warps, grid, st, w);
-    return launch_narrow_big(st, w);
-}
+
 
 } // namespace nans

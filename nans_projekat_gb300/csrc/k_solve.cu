@@ -193,7 +193,10 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
 }
 
 // Dynamic shared memory: int last[max_scene_bodies] (wave of the last contact per body).
-__global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt)
+// pass 0 solves every scene whose contacts are all known after the per-thread EPA tier
+// (largest first); pass 1 the scenes with a candidate in the later EPA tiers, so that pass 0
+// can run while those tiers do.
+__global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt, int pass)
 {
     extern __shared__ int s_last[];
     __shared__ int sh[32];
@@ -204,13 +207,28 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt)
     {
         if (tid == 0)
         {
-            int q = atomicAdd(w.work_counter + 1, 1);
-            s_scene = (q < w.n_scenes) ? w.sc_order[q] : -1;
+            if (pass == 0)
+            {
+                int q = atomicAdd(w.work_counter + 1, 1);
+                s_scene = (q < w.n_scenes) ? w.sc_order[q] : -1;
+                if (s_scene >= 0 && w.scene_late[s_scene])
+                    s_scene = -2;
+            }
+            else
+            {
+                int q = atomicAdd(w.work_counter + 12, 1);
+                s_scene = (q < min(w.work_counter[13], w.n_scenes)) ? w.late_list[q] : -1;
+            }
         }
         __syncthreads();
         const int s = s_scene;
-        if (s < 0)
+        if (s == -1)
             break;
+        if (s < 0)
+        {
+            __syncthreads();
+            continue;
+        }
         const int cb = w.cand_begin[s], ce = w.cand_end[s];
         const int c0 = w.sc_cube0[s];
         const int nb = w.sc_nc[s] + w.sc_ns[s];

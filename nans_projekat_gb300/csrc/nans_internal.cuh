@@ -77,6 +77,9 @@ struct DevWorld
     unsigned *pair_mask;                // one bit per pair in the pair space
     int *block_hits;                    // per cull block hit count, then exclusive offsets
     int *cand_begin, *cand_end;         // per scene candidate range
+    int *scene_late;                    // per scene: 1 if a candidate went beyond the per-thread
+                                        // EPA tier (solved after those tiers)
+    int *late_list;                     // the late scenes, in no particular order
     // narrowphase output, per candidate
     int *hit;
     float4 *c_pa, *c_pb, *c_n;
@@ -85,7 +88,8 @@ struct DevWorld
                                         // length, [6] warp-EPA head, [7] long-GJK queue length,
                                         // [8] giant-EPA queue length, [9] giant-EPA head,
                                         // [10] per-thread EPA queue length (queue: s_order),
-                                        // [11] per-thread EPA head
+                                        // [11] per-thread EPA head, [12] late-solve head,
+                                        // [13] late-scene count
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
     int *long_cand;                     // candidates whose GJK needs the long pass

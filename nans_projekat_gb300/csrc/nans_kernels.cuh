@@ -63,12 +63,11 @@ size_t epa_big_bytes();
 size_t epa_block_bytes();
 size_t epa_giant_scratch_bytes();
 int giant_grid(int sm_count);
-int launch_narrow(int warps, int grid, cudaStream_t st, const DevWorld &w);
 void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w);
 int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaError_t
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
-__global__ void k_solve(DevWorld w, float dt);
+__global__ void k_solve(DevWorld w, float dt, int pass);
 int solve_threads();
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);
 
