@@ -410,12 +410,29 @@ def run_ours(args):
     achieved = dom_bytes / (stage_ms[dom] / 1000.0) / 1e9
     sweep_gbs = sweep_bytes / (stage_ms[0] / 1000.0) / 1e9
 
-    # end to end through the C ABI with pinned host buffers: set_state (H2D), one step,
-    # download (D2H), every step
+    # end to end through the C ABI with pinned host buffers, every step: the whole dynamic
+    # state in (Position, Angles, V, W as float[n][3], H2D), one step, the whole state out (D2H)
+    def pinned(shape, dtype):
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        return torch.empty(max(1, n), dtype=torch.uint8, pin_memory=True).numpy()[:n].view(dtype).reshape(shape)
+
+    state = tuple(pinned((bodies, 3), np.float32) for _ in range(4))
+    w.get_state_arrays(out=state)
+    barrier(dist, device)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        w.lib.nans_world_set_state_arrays(w.h, *[a.ctypes.data for a in state])
+        w.batch_step(DT, 1, args.graph_steps)
+        w.lib.nans_world_get_state_arrays(w.h, *[a.ctypes.data for a in state])
+    te2e = time.perf_counter() - t0
+    te2e = max_over_ranks(dist, te2e, device)
+    e2e_value = total_bodies * args.e2e_steps / te2e
+    state_bytes = sum(a.nbytes for a in state)
+
+    # the same through the reference's record layouts (cube 244 B, sphere 148 B)
     cubes, spheres, floors = w.download()
-    pin_c = torch.empty(cubes.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(CUBE_DTYPE)
-    pin_s = torch.empty(max(1, spheres.nbytes), dtype=torch.uint8, pin_memory=True).numpy()[:spheres.nbytes]
-    pin_s = pin_s.view(SPHERE_DTYPE)
+    pin_c = pinned((len(cubes),), CUBE_DTYPE)
+    pin_s = pinned((len(spheres),), SPHERE_DTYPE)
     pin_c[:] = cubes
     pin_s[:] = spheres
     pin_f = np.zeros(len(floors), CUBE_DTYPE)
@@ -425,10 +442,11 @@ def run_ours(args):
         w.set_state(pin_c, pin_s, keep_model=True)
         w.batch_step(DT, 1, args.graph_steps)
         w.lib.nans_world_download(w.h, pin_c.ctypes.data, pin_s.ctypes.data, pin_f.ctypes.data)
-    te2e = time.perf_counter() - t0
-    te2e = max_over_ranks(dist, te2e, device)
-    e2e_value = total_bodies * args.e2e_steps / te2e
-    rec_bytes = cubes.nbytes + spheres.nbytes
+    trec = max_over_ranks(dist, time.perf_counter() - t0, device)
+    e2e_records = {"value": total_bodies * args.e2e_steps / trec, "unit": UNIT,
+                   "h2d_bytes_per_step": int(cubes.nbytes + spheres.nbytes),
+                   "d2h_bytes_per_step": int(cubes.nbytes + spheres.nbytes + pin_f.nbytes),
+                   "path": "nans_world_set_state + nans_batch_step(1) + nans_world_download (records), pinned host"}
     launches_batched, _ = w.launches_per_step()
 
     secondary = None
@@ -463,9 +481,10 @@ def run_ours(args):
                          "stage_ms": {n: float(x) for n, x in zip(names, stage_ms)},
                          "sweep": {"achieved": sweep_gbs, "frac": sweep_gbs / peak,
                                    "bytes_per_launch": sweep_bytes, "traffic": measured_traffic("k_sweep")}},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(rec_bytes),
-                    "d2h_bytes_per_step": int(rec_bytes + pin_f.nbytes),
-                    "path": "nans_world_set_state + nans_batch_step(1) + nans_world_download, pinned host"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(state_bytes),
+                    "d2h_bytes_per_step": int(state_bytes),
+                    "path": "nans_world_set_state_arrays + nans_batch_step(1) + nans_world_get_state_arrays, "
+                            "pinned host", "records": e2e_records},
             "gpu_launches": int(launches_batched * args.steps),
             "secondary": secondary,
             "clocks": clocks,

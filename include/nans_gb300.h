@@ -178,6 +178,17 @@ int nans_world_download(nans_world *world, nans_cube *cubes, nans_sphere *sphere
  * NANS_UPLOAD_KEEP_MODEL, Model) of every body from records laid out as at upload. */
 int nans_world_set_state(nans_world *world, const nans_cube *cubes, const nans_sphere *spheres, uint32_t flags);
 
+/* The dynamic state as four float[n_bodies][3] arrays in record order (the cubes of every
+ * scene in upload order, then the spheres): Position, Angles, V, W. Any pointer may be NULL
+ * (that quantity is left as it is / not read back). A compact alternative to the records for
+ * hosts that exchange state every step (64 bytes per body instead of 244 / 148). set_state
+ * applies the last step's pending IntegrateVelocities first, then overwrites; the next step
+ * rebuilds Model from Position / Angles and applies no external forces. get_state applies the
+ * pending IntegrateVelocities, like nans_world_download, and synchronises. */
+int nans_world_set_state_arrays(nans_world *world, const float *position, const float *angles, const float *velocity,
+                                const float *omega);
+int nans_world_get_state_arrays(nans_world *world, float *position, float *angles, float *velocity, float *omega);
+
 /* Contact list of one scene after its last DetectCollisions, in the reference's order
  * (CC i<j, CF, SF, CS, SS). *count receives the full count even when it exceeds cap. */
 int nans_get_pairs(nans_world *world, uint32_t scene, nans_contact_pair *out, uint32_t cap, uint32_t *count);

@@ -113,6 +113,7 @@ struct nans_world
     float4 *d_adj4 = nullptr;       // gP, gA, gV, gW (in allocs)
     float *d_adj1 = nullptr;        // g_invm, g_invi, g_z, g_zw, g_mass, then g_cr, g_cf per scene
     float *d_stage = nullptr;       // 3 floats per dynamic body, record order
+    float *d_state_stage = nullptr; // 4 x 3 floats per dynamic body (state arrays, record order)
 };
 
 namespace
@@ -254,6 +255,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     w->d_adj4 = nullptr;
     w->d_adj1 = nullptr;
     w->d_stage = nullptr;
+    w->d_state_stage = nullptr;
 
     const int S = (int)nscenes;
     const int ndyn = (int)(tc + ts);
@@ -1112,6 +1114,79 @@ int nans_diff_tape_info(nans_world *w, uint32_t *steps, uint64_t *bytes)
         *steps = w->tape_valid ? (uint32_t)w->tape.size() : 0;
     if (bytes)
         *bytes = w->tape_valid ? (uint64_t)w->tape_bytes : 0;
+    return NANS_OK;
+}
+
+int nans_world_set_state_arrays(nans_world *w, const float *position, const float *angles, const float *velocity,
+                                const float *omega)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "set_state_arrays: null world");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "set_state_arrays: no scene uploaded");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    const size_t n3 = 3 * (size_t)w->n_dyn;
+    int rc;
+    if (!w->d_state_stage && (rc = dalloc(w, w->allocs, &w->d_state_stage, 4 * n3)))
+        return rc;
+    const int nb = (w->n_all + kSweepThreads - 1) / kSweepThreads;
+    if (w->pending)
+    {
+        k_sweep<<<nb, kSweepThreads, 0, st>>>(w->dw, w->pending_dt, 0.0f, SW_APPLY_VEL);
+        w->pending = false;
+    }
+    const float *src[4] = {position, angles, velocity, omega};
+    int mask = 0;
+    for (int q = 0; q < 4; ++q)
+        if (src[q] && n3)
+        {
+            CK(cudaMemcpyAsync(w->d_state_stage + q * n3, src[q], n3 * sizeof(float), cudaMemcpyHostToDevice, st));
+            mask |= 1 << q;
+        }
+    if (mask)
+        k_state_in<<<nb, kSweepThreads, 0, st>>>(w->dw, w->d_state_stage, w->d_body_rec, w->n_cubes, mask);
+    CK(cudaGetLastError());
+    w->model_input = false;
+    w->forces_pending = false;
+    w->tape_valid = false;
+    return NANS_OK;
+}
+
+int nans_world_get_state_arrays(nans_world *w, float *position, float *angles, float *velocity, float *omega)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "get_state_arrays: null world");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "get_state_arrays: no scene uploaded");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    const size_t n3 = 3 * (size_t)w->n_dyn;
+    int rc;
+    if (!w->d_state_stage && (rc = dalloc(w, w->allocs, &w->d_state_stage, 4 * n3)))
+        return rc;
+    const int nb = (w->n_all + kSweepThreads - 1) / kSweepThreads;
+    if (w->pending)
+    {
+        k_sweep<<<nb, kSweepThreads, 0, st>>>(w->dw, w->pending_dt, 0.0f, SW_APPLY_VEL);
+        w->pending = false;
+        w->model_input = false;
+    }
+    float *dst[4] = {position, angles, velocity, omega};
+    int mask = 0;
+    for (int q = 0; q < 4; ++q)
+        if (dst[q])
+            mask |= 1 << q;
+    if (mask && n3)
+    {
+        k_state_out<<<nb, kSweepThreads, 0, st>>>(w->dw, w->d_state_stage, w->d_body_rec, w->n_cubes, mask);
+        for (int q = 0; q < 4; ++q)
+            if (dst[q])
+                CK(cudaMemcpyAsync(dst[q], w->d_state_stage + q * n3, n3 * sizeof(float), cudaMemcpyDeviceToHost,
+                                   st));
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(st));
     return NANS_OK;
 }
 

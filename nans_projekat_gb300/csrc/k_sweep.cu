@@ -326,6 +326,49 @@ __global__ void k_pack(DevWorld w, float *rec_cube, float *rec_sphere, float *re
     }
 }
 
+// Dynamic state to and from four float[n][3] arrays in record order (cubes of every scene in
+// upload order, then spheres): stage[0] Position, [1] Angles, [2] V, [3] W. mask bit q selects
+// array q. The radius kept in pos.w is not touched.
+__device__ __forceinline__ size_t state_rec(const int *body_rec, int n_cubes, int b)
+{
+    const int rk = body_rec[b];
+    return (size_t)(rk >= 0 ? rk : n_cubes + (-rk - 1));
+}
+
+__global__ void k_state_in(DevWorld w, const float *stage, const int *body_rec, int n_cubes, int mask)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= w.n_dyn)
+        return;
+    const size_t r = 3 * state_rec(body_rec, n_cubes, b), n3 = 3 * (size_t)w.n_dyn;
+    float4 *dst[4] = {w.pos, w.ang, w.vel, w.omg};
+    for (int q = 0; q < 4; ++q)
+        if (mask & (1 << q))
+        {
+            const float *x = stage + q * n3 + r;
+            const float keep = (q == 0) ? dst[q][b].w : 0.0f;
+            dst[q][b] = make_float4(x[0], x[1], x[2], keep);
+        }
+}
+
+__global__ void k_state_out(DevWorld w, float *stage, const int *body_rec, int n_cubes, int mask)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= w.n_dyn)
+        return;
+    const size_t r = 3 * state_rec(body_rec, n_cubes, b), n3 = 3 * (size_t)w.n_dyn;
+    const float4 *src[4] = {w.pos, w.ang, w.vel, w.omg};
+    for (int q = 0; q < 4; ++q)
+        if (mask & (1 << q))
+        {
+            const float4 v = src[q][b];
+            float *x = stage + q * n3 + r;
+            x[0] = v.x;
+            x[1] = v.y;
+            x[2] = v.z;
+        }
+}
+
 // The project sine/cosine on the device, for comparison with the oracle's host copy.
 __global__ void k_sincos(const float *x, float *s, float *c, int n)
 {

@@ -53,6 +53,8 @@ __global__ void k_pack(DevWorld w, float *rec_cube, float *rec_sphere, float *re
                        const float2 *size_moi, int vertices_valid);
 
 __global__ void k_sincos(const float *x, float *s, float *c, int n);
+__global__ void k_state_in(DevWorld w, const float *stage, const int *body_rec, int n_cubes, int mask);
+__global__ void k_state_out(DevWorld w, float *stage, const int *body_rec, int n_cubes, int mask);
 
 __global__ void k_cull_mask(DevWorld w, int all_pairs);
 __global__ void k_scan_blocks(DevWorld w, int nblocks);

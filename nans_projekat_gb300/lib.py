@@ -39,7 +39,7 @@ EXPORTS = (
     "nans_get_pairs", "nans_world_status", "nans_world_counts", "nans_world_stream",
     "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps",
     "nans_world_epa_stats", "nans_solve_contacts_static", "nans_diff_forward", "nans_diff_backward",
-    "nans_diff_tape_info",
+    "nans_diff_tape_info", "nans_world_set_state_arrays", "nans_world_get_state_arrays",
 )
 
 
@@ -97,6 +97,8 @@ def load(path=LIB_PATH):
     L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
     L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
     L.nans_world_epa_stats.argtypes = [_P, _P, ctypes.c_int]
+    L.nans_world_set_state_arrays.argtypes = [_P, _P, _P, _P, _P]
+    L.nans_world_get_state_arrays.argtypes = [_P, _P, _P, _P, _P]
     L.nans_diff_forward.argtypes = [_P, ctypes.POINTER(StepParams), _F, _U]
     L.nans_diff_backward.argtypes = [_P, ctypes.POINTER(DiffGrads)]
     L.nans_diff_tape_info.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(ctypes.c_uint64)]
@@ -223,6 +225,26 @@ class World:
         _check(self.lib.nans_world_set_state(self.h, _ptr(np.ascontiguousarray(cubes)),
                                              _ptr(np.ascontiguousarray(spheres)),
                                              UPLOAD_KEEP_MODEL if keep_model else 0))
+
+    def set_state_arrays(self, position=None, angles=None, velocity=None, omega=None):
+        """Dynamic state from (n_bodies, 3) float32 arrays in record order (None = keep)."""
+        arrs = []
+        for a in (position, angles, velocity, omega):
+            if a is not None:
+                a = np.ascontiguousarray(a, np.float32)
+                if a.shape != (self.n_bodies, 3):
+                    raise ValueError("state arrays must have shape (%d, 3)" % self.n_bodies)
+            arrs.append(a)
+        self._state_keep = arrs
+        _check(self.lib.nans_world_set_state_arrays(self.h, *[_ptr(a) for a in arrs]))
+
+    def get_state_arrays(self, out=None):
+        """(position, angles, velocity, omega) as (n_bodies, 3) float32 arrays in record order;
+        `out` may supply the four arrays (e.g. in pinned memory)."""
+        if out is None:
+            out = tuple(np.zeros((self.n_bodies, 3), np.float32) for _ in range(4))
+        _check(self.lib.nans_world_get_state_arrays(self.h, *[_ptr(a) for a in out]))
+        return out
 
     def pairs(self, scene=0):
         cnt = _U()

@@ -4,7 +4,7 @@ body state, every contact list and every step."""
 import numpy as np
 import pytest
 
-from helpers import (GOLDEN_CASES, load_golden, step_digest, same_fields, first_difference,
+from helpers import (GOLDEN_CASES, canon, load_golden, step_digest, same_fields, first_difference,
                      STATE_FIELDS, PAIR_FIELDS)
 from nans_projekat_gb300 import scenes
 
@@ -93,6 +93,36 @@ def test_grid_wide_epa_tier_in_graphs(nl):
         cubes, spheres, _ = w.scene_state(i, state)
         assert step_digest(cubes, spheres, w.pairs(i)) == digests[n - 1], LARGE_EPA_CASES[i]
     w.close()
+
+
+def test_state_arrays_match_records(nl):
+    """nans_world_get_state_arrays returns the records' Position / Angles / V / W in record
+    order, and a step after nans_world_set_state_arrays equals a step after the record-based
+    nans_world_set_state (Model rebuilt, no external forces) bit for bit."""
+    batch = scenes.stack_batch(64, seed=9, lo=4, hi=48)
+    dt = np.float32(1 / 60)
+    a = nl.World()
+    a.upload_batch(batch)
+    a.batch_step(dt, 25, graph_steps=10)
+    cubes, spheres, _ = a.download()
+    P, A, V, W = a.get_state_arrays()
+    cat = lambda f: np.concatenate([cubes[f], spheres[f]]).astype(np.float32)
+    for got, f in ((P, "Position"), (A, "Angles"), (V, "V"), (W, "W")):
+        assert canon(got) == canon(cat(f)), f
+    b = nl.World()
+    b.upload_batch(batch)
+    b.set_state_arrays(P, A, V, W)
+    a.set_state(cubes, spheres, keep_model=False)
+    a.step(dt, 5)
+    b.step(dt, 5)
+    ca, sa, _ = a.download()
+    cb, sb, _ = b.download()
+    assert same_fields(ca, cb, STATE_FIELDS + ("Vertices",))[0]
+    assert same_fields(sa, sb, STATE_FIELDS)[0]
+    for i in range(len(batch)):
+        assert same_fields(a.pairs(i), b.pairs(i), PAIR_FIELDS)[0], i
+    a.close()
+    b.close()
 
 
 def test_demo_frames_model_and_vertices(nl):
