@@ -4,7 +4,7 @@
 // stage sequence of the reference's frame function (code/nans.cpp:1758-1762) plus the
 // render code's Model rebuild, as six kernels:
 //   k_sweep        IntegrateVelocities(prev) + rebuild + IntegrateForces + vertices + AABB
-//   k_cull_mask / k_scan_blocks / k_cull_write   ordered candidate pairs
+//   k_cull_mask / k_cull_scan / k_cull_write     ordered candidate pairs
 //   k_narrow / k_narrow_big   GJK + EPA           (DetectCollisions)
 //   k_solve        sequential impulses by waves   (SolveConstraints)
 // The last step's IntegrateVelocities is folded into the next step's sweep, or applied by
@@ -67,7 +67,7 @@ struct nans_world
     int n_scenes = 0, n_dyn = 0, n_all = 0, n_cubes = 0, n_spheres = 0;
     long long pair_total = 0;
     int cand_cap = 0;
-    int cull_blocks = 0;
+    int cull_blocks = 0;    // one thread per pair-mask word
     int max_scene_bodies = 0;
 
     std::vector<void *> allocs;     // per-upload device buffers
@@ -267,7 +267,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     w->n_spheres = (int)ts;
 
     std::vector<int> sc_cube0(S), sc_nc(S), sc_ns(S), sc_iters(S), sc_order(S), body_scene(nall), body_rec(nall);
-    std::vector<long long> sc_pair0(S + 1);
+    std::vector<int> sc_word0(S + 1);
+    long long word_acc = 0;
     std::vector<float> sc_cr(S), sc_cf(S);
     std::vector<int4> shape(nall);
     std::vector<float4> scl(nall);
@@ -282,8 +283,10 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         sc_cube0[s] = b;
         sc_nc[s] = (int)snc[s];
         sc_ns[s] = (int)sns[s];
-        sc_pair0[s] = pair_acc;
-        pair_acc += scene_pair_count(snc[s], sns[s]);
+        sc_word0[s] = (int)word_acc;
+        const long long np = scene_pair_count(snc[s], sns[s]);
+        pair_acc += np;
+        word_acc += (np + 31) / 32;
         max_bodies = std::max(max_bodies, (int)(snc[s] + sns[s]));
         if (sp)
         {
@@ -339,7 +342,9 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
             body_rec[b] = -(sphere_rank++) - 1;
         }
     }
-    sc_pair0[S] = pair_acc;
+    sc_word0[S] = (int)word_acc;
+    if (word_acc > INT32_MAX)
+        return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: more than 2^31 words of pair mask");
     for (int s = 0; s < S; ++s)
     {
         int fb = ndyn + s;
@@ -358,8 +363,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: a scene has more bodies than the solver's wave table holds");
 
     w->pair_total = pair_acc;
-    w->cull_blocks = (int)((pair_acc + kPairsPerBlock - 1) / kPairsPerBlock);
     w->max_scene_bodies = max_bodies;
+    w->cull_blocks = (int)((word_acc + kCullThreads - 1) / kCullThreads);
 
     DevWorld &d = w->dw;
     d = DevWorld{};
@@ -367,14 +372,15 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.n_dyn = ndyn;
     d.n_all = nall;
     d.pair_total = pair_acc;
+    d.n_words = (int)word_acc;
     auto &L = w->allocs;
     int rc;
     int *p_cube0, *p_nc, *p_ns, *p_iters, *p_order, *p_bscene;
-    long long *p_pair0;
+    int *p_word0, *p_wscene;
     float *p_cr, *p_cf, *p_local;
     int4 *p_shape;
     if ((rc = dalloc(w, L, &p_cube0, S)) || (rc = dalloc(w, L, &p_nc, S)) || (rc = dalloc(w, L, &p_ns, S)) ||
-        (rc = dalloc(w, L, &p_iters, S)) || (rc = dalloc(w, L, &p_order, S)) || (rc = dalloc(w, L, &p_pair0, S + 1)) ||
+        (rc = dalloc(w, L, &p_iters, S)) || (rc = dalloc(w, L, &p_order, S)) || (rc = dalloc(w, L, &p_word0, S + 1)) ||
         (rc = dalloc(w, L, &p_cr, S)) || (rc = dalloc(w, L, &p_cf, S)) || (rc = dalloc(w, L, &p_bscene, nall)) ||
         (rc = dalloc(w, L, &w->d_body_rec, nall)) || (rc = dalloc(w, L, &p_shape, nall)) ||
         (rc = dalloc(w, L, &w->d_scl, nall)) || (rc = dalloc(w, L, &w->d_size_moi, nall)) ||
@@ -383,8 +389,9 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.omg, nall)) || (rc = dalloc(w, L, &d.frc, nall)) || (rc = dalloc(w, L, &d.trq, nall)) ||
         (rc = dalloc(w, L, &w->d_prm, nall)) || (rc = dalloc(w, L, &w->d_model_in, (size_t)4 * nall)) ||
         (rc = dalloc(w, L, &d.box_lo, nall)) || (rc = dalloc(w, L, &d.box_hi, nall)) ||
-        (rc = dalloc(w, L, &d.pair_mask, (size_t)((pair_acc + 31) / 32))) ||
-        (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.n_cand, 1)) ||
+        (rc = dalloc(w, L, &d.pair_mask, (size_t)word_acc)) || (rc = dalloc(w, L, &p_wscene, (size_t)word_acc)) ||
+        (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.cull_total, 1)) ||
+        (rc = dalloc(w, L, &d.n_cand, 1)) ||
         (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
         (rc = dalloc(w, L, &d.scene_late, S)) || (rc = dalloc(w, L, &d.late_list, S)) ||
         (rc = dalloc(w, L, &d.work_counter, kWorkCounters)) || (rc = dalloc(w, L, &d.status, 1)) ||
@@ -403,7 +410,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.sc_ns = p_ns;
     d.sc_iters = p_iters;
     d.sc_order = p_order;
-    d.sc_pair0 = p_pair0;
+    d.sc_word0 = p_word0;
+    d.word_scene = p_wscene;
     d.sc_cr = p_cr;
     d.sc_cf = p_cf;
     d.body_scene = p_bscene;
@@ -425,7 +433,15 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     CK(cudaMemcpyAsync(p_ns, sc_ns.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_iters, sc_iters.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_order, sc_order.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(p_pair0, sc_pair0.data(), (S + 1) * sizeof(long long), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(p_word0, sc_word0.data(), (S + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    {
+        std::vector<int> wscene((size_t)word_acc);
+        for (int s = 0; s < S; ++s)
+            std::fill(wscene.begin() + sc_word0[s], wscene.begin() + sc_word0[s + 1], s);
+        if (word_acc)
+            CK(cudaMemcpyAsync(p_wscene, wscene.data(), (size_t)word_acc * sizeof(int), cudaMemcpyHostToDevice, st));
+        CK(cudaStreamSynchronize(st)); // wscene is a local buffer
+    }
     CK(cudaMemcpyAsync(p_cr, sc_cr.data(), S * sizeof(float), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_cf, sc_cf.data(), S * sizeof(float), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_bscene, body_scene.data(), nall * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -474,7 +490,7 @@ void enqueue_cull(nans_world *w)
     int all_pairs = (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0;
     if (w->cull_blocks > 0)
         k_cull_mask<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw, all_pairs);
-    k_scan_blocks<<<1, 1024, 0, st>>>(w->dw, w->cull_blocks);
+    k_cull_scan<<<1, 1024, 0, st>>>(w->dw, w->cull_blocks);
     if (w->cull_blocks > 0)
         k_cull_write<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
 }
@@ -545,21 +561,18 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
         CK(cudaStreamSynchronize(st));
         if (status & ST_CANDIDATES)
         {
-            // count again without the cap: the block offsets hold the exact total
-            long long total = 0;
-            std::vector<int> off(std::max(1, w->cull_blocks));
-            // recount: rerun the mask pass to get per-block counts, then sum on the host
-            int all_pairs = (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0;
-            k_cull_mask<<<w->cull_blocks, kCullThreads, 0, st>>>(d, all_pairs);
-            CK(cudaMemcpyAsync(off.data(), d.block_hits, w->cull_blocks * sizeof(int), cudaMemcpyDeviceToHost, st));
+            // the scan recorded the exact total: grow the candidate buffers and write again
+            int total = 0;
+            CK(cudaMemcpyAsync(&total, d.cull_total, sizeof(int), cudaMemcpyDeviceToHost, st));
             CK(cudaStreamSynchronize(st));
-            for (int v : off)
-                total += v;
-            int rc = alloc_candidates(w, (int)std::min<long long>(total + total / 4 + 1024, INT32_MAX / 16));
+            int rc = alloc_candidates(w, (int)std::min<long long>((long long)total + total / 4 + 1024, INT32_MAX / 16));
             if (rc)
                 return rc;
+            // the block counts were turned into offsets by the scan: count again
             CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
-            k_scan_blocks<<<1, 1024, 0, st>>>(w->dw, w->cull_blocks);
+            const int all_pairs = (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0;
+            k_cull_mask<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw, all_pairs);
+            k_cull_scan<<<1, 1024, 0, st>>>(w->dw, w->cull_blocks);
             k_cull_write<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
             CK(cudaGetLastError());
         }
@@ -1359,8 +1372,8 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
 {
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
-    // sweep, [mask, write], scan, gjk, gjk_long, epa_tiny, epa_medium, block EPA, giant EPA,
-    // solve (two passes)
+    // sweep, [cull mask, cull write], cull scan, gjk, gjk_long, epa_tiny, epa_medium, block
+    // EPA, giant EPA, solve (two passes)
     uint32_t k = 10 + (w->cull_blocks > 0 ? 2u : 0u);
     if (batched)
         *batched = k;

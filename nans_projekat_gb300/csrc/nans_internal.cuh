@@ -55,7 +55,7 @@ struct DevWorld
     const int *sc_cube0;      // global id of the scene's first cube
     const int *sc_nc;         // cubes (incl. hulls)
     const int *sc_ns;         // spheres
-    const long long *sc_pair0; // first index of the scene in the world's pair space
+    const int *sc_word0;      // first pair-mask word of the scene (n_scenes + 1 entries)
     const float *sc_cr;
     const float *sc_cf;
     const int *sc_iters;
@@ -74,8 +74,11 @@ struct DevWorld
     int cand_cap;
     int *cand_a, *cand_b, *cand_meta; // meta = scene << 3 | type
     int *n_cand;                        // device counter
-    unsigned *pair_mask;                // one bit per pair in the pair space
-    int *block_hits;                    // per cull block hit count, then exclusive offsets
+    unsigned *pair_mask;                // one bit per pair, words aligned per scene
+    const int *word_scene;              // scene of each mask word
+    int n_words;
+    int *block_hits;                    // per cull block: culled pairs, then candidate offset
+    int *cull_total;                    // candidates before the capacity clamp
     int *cand_begin, *cand_end;         // per scene candidate range
     int *scene_late;                    // per scene: 1 if a candidate went beyond the per-thread
                                         // EPA tier (solved after those tiers)

@@ -17,8 +17,6 @@ enum SweepFlags
 };
 
 constexpr int kCullThreads = 256;
-constexpr int kPairsPerThread = 32;
-constexpr int kPairsPerBlock = kCullThreads * kPairsPerThread;
 
 // EPA capacities. Vertices: the GJK tetrahedron plus one support per EPA iteration (at most
 // 65, code/nans.cpp:804). Faces grow by two per iteration on a convex polytope, but the
@@ -57,7 +55,7 @@ __global__ void k_state_in(DevWorld w, const float *stage, const int *body_rec, 
 __global__ void k_state_out(DevWorld w, float *stage, const int *body_rec, int n_cubes, int mask);
 
 __global__ void k_cull_mask(DevWorld w, int all_pairs);
-__global__ void k_scan_blocks(DevWorld w, int nblocks);
+__global__ void k_cull_scan(DevWorld w, int nblocks);
 __global__ void k_cull_write(DevWorld w);
 
 int narrow_blocks_per_sm(int warps);

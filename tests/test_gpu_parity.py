@@ -95,6 +95,27 @@ def test_grid_wide_epa_tier_in_graphs(nl):
     w.close()
 
 
+def test_large_scene_cull_equals_all_pairs(nl):
+    """One 6,600-body scene (21.8 M pairs, 680,000 mask words): the culled step must give the
+    all-pairs result."""
+    sc = scenes.random_scene(seed=4, n_boxes=6000, n_spheres=600, extent=150.0)
+    dt = np.float32(1 / 60)
+    a = nl.World()
+    b = nl.World(all_pairs=True)
+    a.upload(sc)
+    b.upload(sc)
+    a.step(dt, 3)
+    b.step(dt, 3)
+    ca, sa, _ = a.download()
+    cb, sb, _ = b.download()
+    assert same_fields(ca, cb, STATE_FIELDS)[0]
+    assert same_fields(sa, sb, STATE_FIELDS)[0]
+    assert same_fields(a.pairs(0), b.pairs(0), PAIR_FIELDS)[0]
+    assert len(a.pairs(0)) > 0
+    a.close()
+    b.close()
+
+
 def test_state_arrays_match_records(nl):
     """nans_world_get_state_arrays returns the records' Position / Angles / V / W in record
     order, and a step after nans_world_set_state_arrays equals a step after the record-based
