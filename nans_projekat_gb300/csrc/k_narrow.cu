@@ -363,15 +363,26 @@ __device__ __forceinline__ void escalate(const DevWorld &w, int c, bool to_big)
 // 12 vertices (8 EPA iterations) and 20 faces hold ~99.7% of the EPAs of the stack workload.
 // ------------------------------------------------------------------------------------
 constexpr int kTinyThreads = 64;
-constexpr int kTinyV = 12;
-constexpr int kTinyF = 20;
+#ifndef NANS_TINY_V
+#define NANS_TINY_V 12
+#endif
+#ifndef NANS_TINY_F
+#define NANS_TINY_F 20
+#endif
+#ifndef NANS_TINY_FD
+#define NANS_TINY_FD 0 // 1: cache each face's distance; 0: recompute it (less shared memory, faster)
+#endif
+constexpr int kTinyV = NANS_TINY_V;
+constexpr int kTinyF = NANS_TINY_F;
 constexpr int kTinyE = 12;
 
 struct TinySmem
 {
     float px[kTinyV][kTinyThreads], py[kTinyV][kTinyThreads], pz[kTinyV][kTinyThreads];
     float fnx[kTinyF][kTinyThreads], fny[kTinyF][kTinyThreads], fnz[kTinyF][kTinyThreads];
+#if NANS_TINY_FD
     float fd[kTinyF][kTinyThreads];
+#endif
     unsigned fidx[kTinyF][kTinyThreads]; // a | b << 8 | c << 16
     unsigned short edge[kTinyE][kTinyThreads]; // a | b << 8
 };
@@ -407,7 +418,20 @@ __device__ __forceinline__ void tiny_face(TinySmem &S, int t, int f, int a, int 
     S.fnx[f][t] = n.x;
     S.fny[f][t] = n.y;
     S.fnz[f][t] = n.z;
+#if NANS_TINY_FD
     S.fd[f][t] = fabsf(dot3(n, pa));
+#endif
+}
+
+// The face's distance |dot(N, A)| (cached, or recomputed from the same operands: bit-equal).
+__device__ __forceinline__ float tiny_fd(const TinySmem &S, int t, int f)
+{
+#if NANS_TINY_FD
+    return S.fd[f][t];
+#else
+    const v3 n = mk3(S.fnx[f][t], S.fny[f][t], S.fnz[f][t]);
+    return fabsf(dot3(n, tiny_p(S, t, S.fidx[f][t] & 0xffu)));
+#endif
 }
 
 // PushEdge (code/nans.cpp:232-266), sequential. Returns false on overflow.
@@ -452,11 +476,11 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
         if (nf == 0 && !stale)
             return EPA_NONE;
         int ci = 0;
-        float cur = S.fd[0][t];
+        float cur = tiny_fd(S, t, 0);
         if (nf > 0 && !isnan(cur))
             for (int f = 1; f < nf; ++f)
             {
-                float d = S.fd[f][t];
+                float d = tiny_fd(S, t, f);
                 if (d < cur)
                 {
                     cur = d;
@@ -514,7 +538,9 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
                     S.fnx[keep][t] = fn.x;
                     S.fny[keep][t] = fn.y;
                     S.fnz[keep][t] = fn.z;
+#if NANS_TINY_FD
                     S.fd[keep][t] = S.fd[f][t];
+#endif
                 }
                 ++keep;
             }
@@ -529,7 +555,9 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
             S.fnx[0][t] = S.fnx[l][t];
             S.fny[0][t] = S.fny[l][t];
             S.fnz[0][t] = S.fnz[l][t];
+#if NANS_TINY_FD
             S.fd[0][t] = S.fd[l][t];
+#endif
             stale = true;
         }
         int sv = nv++;
