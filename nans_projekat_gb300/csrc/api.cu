@@ -164,7 +164,7 @@ size_t solve_smem(const nans_world *w) { return (size_t)std::max(1, w->max_scene
 int solve_grid(nans_world *w)
 {
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve, solve_threads(), solve_smem(w));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve, solve_threads(w->max_scene_bodies), solve_smem(w));
     if (per < 1)
         per = 1;
     if (w->solve_bpsm > 0)
@@ -510,11 +510,11 @@ cudaError_t enqueue_narrow_solve(nans_world *w, float dt)
         return e;
     launch_epa_medium(st2, w->dw);
     e = (cudaError_t)launch_narrow_big(st2, w->dw);
-    k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt, 0);
+    k_solve<<<solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st>>>(w->dw, dt, 0);
     cudaError_t e2 = cudaEventRecord(w->ev_join, st2);
     if (e2 == cudaSuccess)
         e2 = cudaStreamWaitEvent(st, w->ev_join, 0);
-    k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt, 1);
+    k_solve<<<solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st>>>(w->dw, dt, 1);
     return e != cudaSuccess ? e : e2;
 }
 
@@ -1350,8 +1350,8 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[4], st));
         CK((cudaError_t)launch_narrow_big(st, w->dw));
         CK(cudaEventRecord(ev[5], st));
-        k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt, 0);
-        k_solve<<<solve_grid(w), solve_threads(), solve_smem(w), st>>>(w->dw, dt, 1);
+        k_solve<<<solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st>>>(w->dw, dt, 0);
+        k_solve<<<solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st>>>(w->dw, dt, 1);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());
         after_step(w, dt);

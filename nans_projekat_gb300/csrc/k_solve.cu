@@ -18,12 +18,10 @@
 namespace nans
 {
 
-// One scene per block; the waves are latency-bound (a contact's 10-iteration loop per wave),
-// so small blocks let many scenes share an SM.
-#ifndef NANS_SOLVE_THREADS
-#define NANS_SOLVE_THREADS 64
-#endif
-constexpr int kSolveThreads = NANS_SOLVE_THREADS;
+// One scene per block. The waves are latency-bound (a contact's 10-iteration loop per wave),
+// so worlds of small scenes use 64-thread blocks (many scenes share an SM) and worlds with a
+// scene above 512 bodies 256-thread blocks (its waves hold more contacts).
+constexpr int kSolveThreadsMax = 256;
 constexpr int kWaveChunk = 512;
 
 __device__ __forceinline__ int block_scan_excl(int v, int *sh, int *total)
@@ -196,7 +194,7 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
 // pass 0 solves every scene whose contacts are all known after the per-thread EPA tier
 // (largest first); pass 1 the scenes with a candidate in the later EPA tiers, so that pass 0
 // can run while those tiers do.
-__global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt, int pass)
+__global__ void __launch_bounds__(kSolveThreadsMax) k_solve(DevWorld w, float dt, int pass)
 {
     extern __shared__ int s_last[];
     __shared__ int sh[32];
@@ -232,16 +230,22 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(DevWorld w, float dt, i
         const int cb = w.cand_begin[s], ce = w.cand_end[s];
         const int c0 = w.sc_cube0[s];
         const int nb = w.sc_nc[s] + w.sc_ns[s];
-        // (1) ordered compaction of the scene's hits
+        // (1) ordered compaction of the scene's hits, 8 consecutive candidates per thread
         int nh = 0;
-        for (int base = cb; base < ce; base += blockDim.x)
+        for (int base = cb; base < ce; base += blockDim.x * 8)
         {
-            int i = base + tid;
-            int h = (i < ce) ? w.hit[i] : 0;
+            const int i0 = base + tid * 8;
+            unsigned hv = 0u;
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (i0 + k < ce && w.hit[i0 + k])
+                    hv |= 1u << k;
             int tot;
-            int pre = block_scan_excl(h, sh, &tot);
-            if (h)
-                w.s_order[cb + nh + pre] = i;
+            int pos = cb + nh + block_scan_excl(__popc(hv), sh, &tot);
+#pragma unroll
+            for (int k = 0; k < 8; ++k)
+                if (hv & (1u << k))
+                    w.s_order[pos++] = i0 + k;
             nh += tot;
         }
         if (nh == 0)
@@ -398,6 +402,6 @@ __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int 
         *count = n;
 }
 
-int solve_threads() { return kSolveThreads; }
+int solve_threads(int max_scene_bodies) { return max_scene_bodies > 512 ? kSolveThreadsMax : 64; }
 
 } // namespace nans

@@ -68,7 +68,7 @@ int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaErro
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
 __global__ void k_solve(DevWorld w, float dt, int pass);
-int solve_threads();
+int solve_threads(int max_scene_bodies);
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);
 
 // One step of the differentiable rollout's tape. Contact data is stored by solve slot: slot
