@@ -15,6 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(OUT_DIR, "libnans_gb300.so")
+SIM_PATH = os.path.join(OUT_DIR, "libnans_sim.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -39,12 +40,13 @@ def nvcc():
 def _deps():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     files.append(os.path.join(INCLUDE, "nans_gb300.h"))
+    files.append(os.path.join(INCLUDE, "nans_sim.h"))
     files.append(os.path.abspath(__file__))
     return files
 
 
 def up_to_date():
-    if not os.path.exists(LIB_PATH):
+    if not os.path.exists(LIB_PATH) or not os.path.exists(SIM_PATH):
         return False
     t = os.path.getmtime(LIB_PATH)
     return all(os.path.getmtime(f) <= t for f in _deps())
@@ -76,7 +78,23 @@ def build(force=False, verbose=False, extra_flags=()):
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     os.replace(tmp, LIB_PATH)
+    build_sim()
     return LIB_PATH
+
+
+def build_sim():
+    """libnans_sim.so: the headless SimUpdateAndRender (host C++ over libnans_gb300.so)."""
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if cxx is None:
+        raise RuntimeError("g++ not found")
+    tmp = SIM_PATH + ".tmp"
+    cmd = [cxx, "-O2", "-std=c++17", "-fPIC", "-shared", "-ffp-contract=off", "-I", INCLUDE,
+           os.path.join(CSRC, "sim_shim.cpp"), "-L", OUT_DIR, "-lnans_gb300", "-Wl,-rpath,$ORIGIN", "-o", tmp]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("sim shim build failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+    os.replace(tmp, SIM_PATH)
+    return SIM_PATH
 
 
 if __name__ == "__main__":
