@@ -119,6 +119,14 @@ typedef struct nans_contact_pair
                                       not converge) and the event is counted */
 #define NANS_WORLD_TEST_GIANT_TIER 4u /* testing: every EPA beyond the warp tier's 128 faces
                                       runs on the grid-wide tier (results are the same) */
+#define NANS_WORLD_WARM_START 8u   /* warm starting, the reference's TODO at its pair dedupe
+                                      (code/nans.cpp:1386-1389): a pair (type, IndexA,
+                                      IndexB) that was in contact at the previous step starts
+                                      its accumulated impulses from that step's final values
+                                      instead of zero. Changes results (off: the reference's
+                                      behaviour). Costs 16 bytes of device memory per pair of
+                                      the pair space; set_state and upload start it afresh;
+                                      not available with nans_diff_forward. */
 
 typedef struct nans_world_desc
 {

@@ -164,7 +164,7 @@ size_t solve_smem(const nans_world *w) { return (size_t)std::max(1, w->max_scene
 int solve_grid(nans_world *w)
 {
     int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_solve, solve_threads(w->max_scene_bodies), solve_smem(w));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, solve_kernel(w->dw), solve_threads(w->max_scene_bodies), solve_smem(w));
     if (per < 1)
         per = 1;
     if (w->solve_bpsm > 0)
@@ -196,10 +196,29 @@ int alloc_candidates(nans_world *w, int cap)
             return rc;
         d.s_fwd = w->fwd_buf;
     }
+    d.cand_pidx = nullptr;
+    if (w->flags & NANS_WORLD_WARM_START)
+        if ((rc = dalloc(w, L, &d.cand_pidx, cap)))
+            return rc;
     return NANS_OK;
 }
 
 bool finite_pos(float x) { return std::isfinite(x) && x > 0.0f; }
+
+bool flags_world_warm(const nans_world *w) { return (w->flags & NANS_WORLD_WARM_START) != 0; }
+
+// Warm-start entries are valid for one step; a state overwrite moves the counter on by two.
+__global__ void k_warm_bump(int *step) { *step += 2; }
+
+int warm_invalidate(nans_world *w)
+{
+    if (w->dw.warm_step)
+    {
+        k_warm_bump<<<1, 1, 0, w->stream>>>(w->dw.warm_step);
+        CK(cudaGetLastError());
+    }
+    return NANS_OK;
+}
 
 struct SceneIn
 {
@@ -468,11 +487,20 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         d, w->d_rec_cube, w->d_rec_sphere, w->d_rec_floor, w->d_body_rec, mode, w->d_prm, w->d_model_in);
     CK(cudaGetLastError());
 
+    if (flags_world_warm(w))
+    {
+        if (word_acc * 32 > INT32_MAX)
+            return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: warm starting needs fewer than 2^31 pairs");
+        if ((rc = dalloc(w, L, &d.warm, (size_t)word_acc * 32)) || (rc = dalloc(w, L, &d.warm_step, 1)))
+            return rc;
+        CK(cudaMemsetAsync(d.warm, 0, (size_t)word_acc * 32 * sizeof(float4), st));
+        CK(cudaMemsetAsync(d.warm_step, 0, sizeof(int), st));
+    }
     int cap = (int)(w->max_cand_req ? w->max_cand_req : std::min<long long>(16LL * ndyn + 4096, INT32_MAX / 16));
     if ((rc = alloc_candidates(w, std::max(1, cap))))
         return rc;
     if ((size_t)max_bodies * sizeof(int) > 48 * 1024)
-        CK(cudaFuncSetAttribute(k_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)solve_smem(w)));
+        CK(cudaFuncSetAttribute(solve_kernel(d), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)solve_smem(w)));
     CK(cudaStreamSynchronize(st));
     w->uploaded = true;
     w->pending = false;
@@ -510,11 +538,11 @@ cudaError_t enqueue_narrow_solve(nans_world *w, float dt)
         return e;
     launch_epa_medium(st2, w->dw);
     e = (cudaError_t)launch_narrow_big(st2, w->dw);
-    k_solve<<<solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st>>>(w->dw, dt, 0);
+    launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
     cudaError_t e2 = cudaEventRecord(w->ev_join, st2);
     if (e2 == cudaSuccess)
         e2 = cudaStreamWaitEvent(st, w->ev_join, 0);
-    k_solve<<<solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st>>>(w->dw, dt, 1);
+    launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 1);
     return e != cudaSuccess ? e : e2;
 }
 
@@ -994,7 +1022,7 @@ int nans_world_set_state(nans_world *w, const nans_cube *cubes, const nans_spher
     w->model_input = (flags & NANS_UPLOAD_KEEP_MODEL) != 0;
     w->forces_pending = true;
     w->tape_valid = false;
-    return NANS_OK;
+    return warm_invalidate(w);
 }
 
 int nans_diff_forward(nans_world *w, const nans_step_params *params, float dt, uint32_t nsteps)
@@ -1007,6 +1035,8 @@ int nans_diff_forward(nans_world *w, const nans_step_params *params, float dt, u
         return fail(NANS_ERR_INVALID_ARGUMENT, "diff_forward: dt must be finite and positive");
     if (nsteps == 0)
         return fail(NANS_ERR_INVALID_ARGUMENT, "diff_forward: zero steps");
+    if (w->flags & NANS_WORLD_WARM_START)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "diff_forward: not available with NANS_WORLD_WARM_START");
     CK(cudaSetDevice(w->device));
     if (params)
         set_params_all(w, params);
@@ -1163,7 +1193,7 @@ int nans_world_set_state_arrays(nans_world *w, const float *position, const floa
     w->model_input = false;
     w->forces_pending = false;
     w->tape_valid = false;
-    return NANS_OK;
+    return warm_invalidate(w);
 }
 
 int nans_world_get_state_arrays(nans_world *w, float *position, float *angles, float *velocity, float *omega)
@@ -1350,8 +1380,8 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[4], st));
         CK((cudaError_t)launch_narrow_big(st, w->dw));
         CK(cudaEventRecord(ev[5], st));
-        k_solve<<<solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st>>>(w->dw, dt, 0);
-        k_solve<<<solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st>>>(w->dw, dt, 1);
+        launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
+        launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 1);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());
         after_step(w, dt);

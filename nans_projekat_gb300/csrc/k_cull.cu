@@ -238,6 +238,8 @@ __global__ void __launch_bounds__(kCullThreads) k_cull_write(DevWorld w)
                 w.cand_a[pos] = a;
                 w.cand_b[pos] = b;
                 w.cand_meta[pos] = (s << 3) | type;
+                if (w.cand_pidx)
+                    w.cand_pidx[pos] = wi * 32 + bit;
             }
             ++pos;
         }

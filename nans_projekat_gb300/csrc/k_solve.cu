@@ -104,6 +104,7 @@ __device__ __forceinline__ float friction_bound(double c2, float sum) { return (
 // attached (w.s_fwd) it also records, per contact, what the adjoint needs: the relative
 // normal / tangent velocities, the applied impulses and the active set of the closed form
 // (normal impulse max(Ln, 0), tangent impulses clamp(Lt, -mu*Ln, mu*Ln)).
+template <bool WARM>
 __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const float4 *k, float cr, float cf,
                                               double c2, int iters)
 {
@@ -120,6 +121,21 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
     float jdvt2 = dot3(((V1 + cross3(W1, t2)) - V2) - cross3(W2, t2), t2);
     float bias = bias0 + cr * jdvn;
     float sn = 0.0f, st1 = 0.0f, st2 = 0.0f, dn = 0.0f, dt1 = 0.0f, dt2 = 0.0f;
+    int step = 0, pidx = 0;
+    if (WARM)
+    {
+        // warm starting (the reference's TODO at its pair dedupe, code/nans.cpp:1386-1389): a
+        // pair in contact at the previous step starts from that step's accumulators
+        step = *w.warm_step;
+        pidx = w.cand_pidx[c];
+        const float4 e = w.warm[pidx];
+        if (__float_as_int(e.w) == step - 1)
+        {
+            sn = e.x;
+            st1 = e.y;
+            st2 = e.z;
+        }
+    }
     for (int it = 0; it < iters; ++it)
     {
         float ln = (-jdvn + bias) * jn;
@@ -147,6 +163,8 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
             st2 = m2;
         dt2 = st2 - old;
     }
+    if (WARM)
+        w.warm[pidx] = make_float4(sn, st1, st2, __int_as_float(step));
     if (w.s_fwd)
     {
         float ln = (-jdvn + bias) * jn;
@@ -194,7 +212,7 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
 // pass 0 solves every scene whose contacts are all known after the per-thread EPA tier
 // (largest first); pass 1 the scenes with a candidate in the later EPA tiers, so that pass 0
 // can run while those tiers do.
-__global__ void __launch_bounds__(kSolveThreadsMax) k_solve(DevWorld w, float dt, int pass)
+template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve(DevWorld w, float dt, int pass)
 {
     extern __shared__ int s_last[];
     __shared__ int sh[32];
@@ -350,7 +368,7 @@ __global__ void __launch_bounds__(kSolveThreadsMax) k_solve(DevWorld w, float dt
 #pragma unroll
                 for (int q = 0; q < 9; ++q)
                     k[q] = __ldcg(w.s_k + (size_t)9 * c + q);
-                contact_apply(w, c, k, cr, cf, c2, iters);
+                contact_apply<WARM>(w, c, k, cr, cf, c2, iters);
             }
             __syncthreads();
         }
@@ -403,5 +421,19 @@ __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int 
 }
 
 int solve_threads(int max_scene_bodies) { return max_scene_bodies > 512 ? kSolveThreadsMax : 64; }
+
+// Warm starting keeps its own instantiation so that the default solve keeps its registers.
+const void *solve_kernel(const DevWorld &w)
+{
+    return w.warm ? (const void *)k_solve<true> : (const void *)k_solve<false>;
+}
+
+void launch_solve(const DevWorld &w, int grid, int threads, size_t smem, cudaStream_t st, float dt, int pass)
+{
+    if (w.warm)
+        k_solve<true><<<grid, threads, smem, st>>>(w, dt, pass);
+    else
+        k_solve<false><<<grid, threads, smem, st>>>(w, dt, pass);
+}
 
 } // namespace nans

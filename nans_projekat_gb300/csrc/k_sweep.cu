@@ -149,6 +149,8 @@ __global__ void k_sweep(DevWorld w, float pending_dt, float dt, int flags)
     }
     if (!(flags & SW_INTEGRATE))
         return;
+    if (w.warm_step && b == 0)
+        atomicAdd(w.warm_step, 1); // a new step: warm-start entries of the last one stay valid
     if (!is_floor)
     {
         float4 pr = __ldg(w.prm + b);

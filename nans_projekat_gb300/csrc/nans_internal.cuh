@@ -118,6 +118,11 @@ struct DevWorld
                                         // narrowphase the GJK simplex of a hit
     int *s_last;                        // per body: last wave touching it
     float4 *s_fwd;                      // adjoint tape of the solve (2 float4 per slot) or null
+    // warm starting (null when off): per pair of the pair space (index 32 * word + bit) the
+    // accumulators (sn, st1, st2) of its last solve and that solve's step number
+    float4 *warm;
+    int *warm_step;                     // step counter, advanced by the sweep
+    int *cand_pidx;                     // per candidate: its pair-space index
     int *s_maxw;                        // per scene: highest wave of the last solve, or null
     unsigned *status;
 };

@@ -67,8 +67,9 @@ void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
 int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaError_t
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
-__global__ void k_solve(DevWorld w, float dt, int pass);
 int solve_threads(int max_scene_bodies);
+const void *solve_kernel(const DevWorld &w);
+void launch_solve(const DevWorld &w, int grid, int threads, size_t smem, cudaStream_t st, float dt, int pass);
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);
 
 // One step of the differentiable rollout's tape. Contact data is stored by solve slot: slot

@@ -31,6 +31,7 @@ UPLOAD_KEEP_MODEL = 1
 WORLD_ALL_PAIRS = 1
 WORLD_STRICT_EPA = 2
 WORLD_TEST_GIANT_TIER = 4
+WORLD_WARM_START = 8
 
 # Every symbol include/nans_gb300.h declares.
 EXPORTS = (
@@ -134,10 +135,11 @@ class World:
     batch_step(dt, n, g)   the batched path: persistent kernels replayed from a CUDA graph
     """
 
-    def __init__(self, device=0, all_pairs=False, max_candidates=0, strict_epa=False, giant_tier_only=False):
+    def __init__(self, device=0, all_pairs=False, max_candidates=0, strict_epa=False, giant_tier_only=False,
+                 warm_start=False):
         self.lib = load()
         flags = (WORLD_ALL_PAIRS if all_pairs else 0) | (WORLD_STRICT_EPA if strict_epa else 0) | \
-            (WORLD_TEST_GIANT_TIER if giant_tier_only else 0)
+            (WORLD_TEST_GIANT_TIER if giant_tier_only else 0) | (WORLD_WARM_START if warm_start else 0)
         d = WorldDesc(device, flags, max_candidates)
         h = _P()
         _check(self.lib.nans_world_create(ctypes.byref(d), ctypes.byref(h)))

@@ -203,6 +203,7 @@ template <class T> struct Contact
 {
     int type, a, b;
     V3<T> pa, pb, n;
+    T sn, st1, st2; // accumulated impulses: initial values (warm start), then final values
 };
 
 struct Consts
@@ -217,6 +218,8 @@ template <class T> struct Scene
     Body<T> floor;
     std::vector<Contact<T>> pairs;
     Consts k;
+    bool warm = false;                // warm starting: accumulators carried across steps
+    std::vector<Contact<T>> prev;     // the last solve's contacts with their accumulators
 };
 
 // ---------------------------------------------------------------------------------
@@ -759,7 +762,8 @@ template <class T> static void detect(Scene<T> &s)
     s.pairs.clear();
     const int nc = (int)s.cubes.size(), ns = (int)s.spheres.size();
     auto run = [&](int type, int ia, int ib, const Body<T> *A, const Body<T> *B, bool as, bool bs) {
-        Contact<T> c{type, ia, ib, mk(T(0), T(0), T(0)), mk(T(0), T(0), T(0)), mk(T(0), T(0), T(0))};
+        Contact<T> c{type, ia, ib, mk(T(0), T(0), T(0)), mk(T(0), T(0), T(0)), mk(T(0), T(0), T(0)), T(0), T(0),
+                     T(0)};
         PairCtx<T> p{A, B, as, bs};
         if (check_collision(p, c))
             s.pairs.push_back(c);
@@ -782,7 +786,7 @@ template <class T> static void detect(Scene<T> &s)
 // ---------------------------------------------------------------------------------
 // sequential impulses (code/nans.cpp:1020-1329, 1538-1548)
 // ---------------------------------------------------------------------------------
-template <class T> static void constraint(Scene<T> &s, const Contact<T> &c, T dt)
+template <class T> static void constraint(Scene<T> &s, Contact<T> &c, T dt)
 {
     Body<T> *A, *B;
     switch (c.type)
@@ -825,7 +829,7 @@ template <class T> static void constraint(Scene<T> &s, const Contact<T> &c, T dt
     T jdvt1 = dot(sub(sub(add(v1, cross(w1, t1)), v2), cross(w2, t1)), t1);
     T jdvt2 = dot(sub(sub(add(v1, cross(w1, t2)), v2), cross(w2, t2)), t2);
 
-    T sn = 0, st1 = 0, st2 = 0, dn = 0, dt1 = 0, dt2 = 0;
+    T sn = c.sn, st1 = c.st1, st2 = c.st2, dn = 0, dt1 = 0, dt2 = 0;
     for (int it = 0; it < s.k.iters; ++it)
     {
         T ln = (-jdvn + bias) * jn;
@@ -853,6 +857,9 @@ template <class T> static void constraint(Scene<T> &s, const Contact<T> &c, T dt
             st2 = m2;
         dt2 = st2 - old;
     }
+    c.sn = sn;
+    c.st1 = st1;
+    c.st2 = st2;
     V3<T> li = mul(dn, n), lt1 = mul(dt1, t1), lt2 = mul(dt2, t2);
     V3<T> ai1 = mul(dn, rn1), ai2 = mul(dn, rn2);
     V3<T> ai1t1 = mul(dt1, r1t1), ai2t1 = mul(dt1, r2t1);
@@ -872,10 +879,27 @@ template <class T> static void constraint(Scene<T> &s, const Contact<T> &c, T dt
     if (writes_b) B->W = sub(B->W, mul(invi2, ai2t2));
 }
 
+// With warm starting (the reference's TODO at its pair dedupe, code/nans.cpp:1386-1389) a
+// contact whose pair (type, IndexA, IndexB) was in contact at the previous solve starts its
+// accumulators from that solve's final values instead of zero.
 template <class T> static void solve(Scene<T> &s, T dt)
 {
-    for (const auto &c : s.pairs)
+    for (auto &c : s.pairs)
+    {
+        c.sn = c.st1 = c.st2 = T(0);
+        if (s.warm)
+            for (const auto &p : s.prev)
+                if (p.type == c.type && p.a == c.a && p.b == c.b)
+                {
+                    c.sn = p.sn;
+                    c.st1 = p.st1;
+                    c.st2 = p.st2;
+                    break;
+                }
         constraint(s, c, dt);
+    }
+    if (s.warm)
+        s.prev = s.pairs;
 }
 
 template <class T> static void stage(Scene<T> &s, int st, T dt)
@@ -1234,6 +1258,22 @@ void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
 
 // Turns the EPA / GJK statistics on or off (off by default).
 void nanso_stats_enable(int on) { g_stats = on != 0; }
+
+// Warm starting for every scene of the world (off by default: the reference's behaviour).
+void nanso_set_warm(void *h, int on)
+{
+    World *w = (World *)h;
+    for (auto &s : w->sf)
+    {
+        s.warm = on != 0;
+        s.prev.clear();
+    }
+    for (auto &s : w->sd)
+    {
+        s.warm = on != 0;
+        s.prev.clear();
+    }
+}
 
 // EPA size statistics since the last reset: out[0] max faces, [1] max edges,
 // [2] max iteration index, [3] EPA calls, [4..7] EPAs whose face list exceeded

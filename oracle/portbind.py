@@ -45,6 +45,7 @@ def lib():
         L.nanso_step_range.argtypes = [_P, _I, _I, _F, _I, _I]
         L.nanso_store.argtypes = [_P, _I, _P, _P, _P]
         L.nanso_state_f64.argtypes = [_P, _I, _P]
+        L.nanso_set_warm.argtypes = [_P, _I]
         L.nanso_pairs.argtypes = [_P, _I, _P, _U]
         L.nanso_pairs.restype = _U
         L.nanso_set_constants.argtypes = [_P, _I, _F, _F, _I]
@@ -84,6 +85,10 @@ class OracleWorld:
         if getattr(self, "h", None):
             self.lib.nanso_destroy(self.h)
             self.h = None
+
+    def set_warm(self, on=True):
+        """Warm starting: accumulators carried across steps for pairs that stay in contact."""
+        self.lib.nanso_set_warm(self.h, 1 if on else 0)
 
     def step(self, dt, n=1, threads=1):
         self.lib.nanso_step(self.h, dt, n, threads)

@@ -116,6 +116,37 @@ def test_large_scene_cull_equals_all_pairs(nl):
     b.close()
 
 
+def test_warm_start_matches_oracle(nl, oracle_lib):
+    """NANS_WORLD_WARM_START against the oracle's warm starting (accumulators carried across
+    steps for pairs that stay in contact), bit for bit, on the batched and the plain path; and
+    it does change the result."""
+    batch = scenes.stack_batch(64, seed=15, lo=4, hi=64)
+    dt = np.float32(1 / 60)
+    n = 60
+    o = _oracle_states(batch, 0, dt)
+    o.set_warm(True)
+    o.step(dt, n, 8)
+    w = nl.World(warm_start=True)
+    w.upload_batch(batch)
+    w.batch_step(dt, n, graph_steps=20)
+    state = w.download()
+    for i in range(len(batch)):
+        cubes, spheres, _ = w.scene_state(i, state)
+        oc, os_, _ = o.state(i)
+        assert same_fields(oc, cubes, STATE_FIELDS)[0], (i, first_difference(oc, cubes, STATE_FIELDS))
+        assert same_fields(os_, spheres, STATE_FIELDS)[0], i
+    p = nl.World(warm_start=True)
+    p.upload(batch[3])
+    p.step(dt, n)
+    assert same_fields(p.download()[0], w.scene_state(3, state)[0], STATE_FIELDS)[0]
+    cold = nl.World()
+    cold.upload_batch(batch)
+    cold.batch_step(dt, n, graph_steps=20)
+    assert not same_fields(cold.download()[0], state[0], STATE_FIELDS)[0]
+    for x in (w, p, cold):
+        x.close()
+
+
 def test_state_arrays_match_records(nl):
     """nans_world_get_state_arrays returns the records' Position / Angles / V / W in record
     order, and a step after nans_world_set_state_arrays equals a step after the record-based
