@@ -457,14 +457,20 @@ __device__ __forceinline__ bool tiny_edge(TinySmem &S, int t, int &ne, int u, in
 }
 
 // ResolveCollision (code/nans.cpp:787-904) by one thread; same results as epa_run.
-__device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, const Shape &B, const GV &s0,
-                        const GV &s1, const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n)
+// `simp` is the GJK simplex as the GJK pass stored it (4 x (P, SupA, SupB), 36 floats).
+__device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, const Shape &B, const float *simp,
+                        v3 &out_pa, v3 &out_pb, v3 &out_n)
 {
     TinyLocal L;
-    tiny_put(S, L, t, 0, s0);
-    tiny_put(S, L, t, 1, s1);
-    tiny_put(S, L, t, 2, s2);
-    tiny_put(S, L, t, 3, s3);
+    for (int i = 0; i < 4; ++i)
+    {
+        const float *q = simp + 9 * i;
+        GV g;
+        g.p = mk3(q[0], q[1], q[2]);
+        g.sa = mk3(q[3], q[4], q[5]);
+        g.sb = mk3(q[6], q[7], q[8]);
+        tiny_put(S, L, t, i, g);
+    }
     tiny_face(S, t, 0, 0, 1, 2);
     tiny_face(S, t, 1, 0, 2, 3);
     tiny_face(S, t, 2, 0, 3, 1);
@@ -592,24 +598,6 @@ __device__ __forceinline__ void store_simplex(const DevWorld &w, int c, const GV
     o[8] = make_float4(s3.sa.z, s3.sb.x, s3.sb.y, s3.sb.z);
 }
 
-__device__ __forceinline__ void load_simplex(const DevWorld &w, int c, GV &s0, GV &s1, GV &s2, GV &s3)
-{
-    const float4 *o = w.s_k + 9 * (size_t)c;
-    const float4 q0 = o[0], q1 = o[1], q2 = o[2], q3 = o[3], q4 = o[4], q5 = o[5], q6 = o[6], q7 = o[7], q8 = o[8];
-    s0.p = mk3(q0.x, q0.y, q0.z);
-    s0.sa = mk3(q0.w, q1.x, q1.y);
-    s0.sb = mk3(q1.z, q1.w, q2.x);
-    s1.p = mk3(q2.y, q2.z, q2.w);
-    s1.sa = mk3(q3.x, q3.y, q3.z);
-    s1.sb = mk3(q3.w, q4.x, q4.y);
-    s2.p = mk3(q4.z, q4.w, q5.x);
-    s2.sa = mk3(q5.y, q5.z, q5.w);
-    s2.sb = mk3(q6.x, q6.y, q6.z);
-    s3.p = mk3(q6.w, q7.x, q7.y);
-    s3.sa = mk3(q7.z, q7.w, q8.x);
-    s3.sb = mk3(q8.y, q8.z, q8.w);
-}
-
 // Appends c to the EPA queue when `hit` (one atomic per warp).
 __device__ __forceinline__ void enqueue_epa(const DevWorld &w, int c, bool hit)
 {
@@ -698,10 +686,8 @@ __global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
             continue;
         const int c = w.s_order[i];
         const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
-        GV s0, s1, s2, s3;
-        load_simplex(w, c, s0, s1, s2, s3);
         v3 pa, pb, nn;
-        const int r = epa_tiny(w, S, t, A, B, s0, s1, s2, s3, pa, pb, nn);
+        const int r = epa_tiny(w, S, t, A, B, reinterpret_cast<const float *>(w.s_k + 9 * (size_t)c), pa, pb, nn);
         if (r == EPA_OVERFLOW)
             escalate(w, c, false);
         else
