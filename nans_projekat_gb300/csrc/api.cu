@@ -765,9 +765,10 @@ int diff_step(nans_world *w, float dt)
     nc = std::max(0, std::min(nc, w->cand_cap));
     if ((rc = tape_alloc(w, &t.a, nc)) || (rc = tape_alloc(w, &t.b, nc)) || (rc = tape_alloc(w, &t.type, nc)) ||
         (rc = tape_alloc(w, &t.k, (size_t)9 * nc)) || (rc = tape_alloc(w, &t.fwd, (size_t)2 * nc)) ||
-        (rc = tape_alloc(w, &t.wend, (size_t)nc + 1)) || (rc = tape_alloc(w, &t.cand_begin, S)) ||
+        (rc = tape_alloc(w, &t.wend, (size_t)nc)) || (rc = tape_alloc(w, &t.cand_begin, S)) ||
         (rc = tape_alloc(w, &t.maxw, S)))
         return rc;
+    t.n = nc;
     const int grid = std::max(1, std::min((std::max(nc, S) + 255) / 256, 8 * w->sm_count));
     k_tape_copy<<<grid, 256, 0, st>>>(d, t);
     CK(cudaGetLastError());
@@ -1083,7 +1084,7 @@ int nans_diff_backward(nans_world *w, const nans_diff_grads *g)
     const int S = w->n_scenes;
     int rc;
     if (!w->d_adj4 && ((rc = dalloc(w, w->allocs, &w->d_adj4, 4 * nd)) ||
-                       (rc = dalloc(w, w->allocs, &w->d_adj1, 5 * nd + 2 * (size_t)S)) ||
+                       (rc = dalloc(w, w->allocs, &w->d_adj1, 5 * nd + 2 * (size_t)S + 4)) ||
                        (rc = dalloc(w, w->allocs, &w->d_stage, 3 * nd))))
         return rc;
     const size_t nst = w->tape.size();
@@ -1097,7 +1098,7 @@ int nans_diff_backward(nans_world *w, const nans_diff_grads *g)
         w->d_tape_cap = nst;
     }
     CK(cudaMemcpyAsync(w->d_tape, w->tape.data(), nst * sizeof(TapeStep), cudaMemcpyHostToDevice, st));
-    CK(cudaMemsetAsync(w->d_adj1, 0, (5 * nd + 2 * (size_t)S) * sizeof(float), st));
+    CK(cudaMemsetAsync(w->d_adj1, 0, (5 * nd + 2 * (size_t)S + 4) * sizeof(float), st));
     float4 *gP = w->d_adj4, *gA = gP + nd, *gV = gA + nd, *gW = gV + nd;
     const int nb = (int)((nd + kSweepThreads - 1) / kSweepThreads);
     const float *ins[4] = {g->dl_position, g->dl_angles, g->dl_velocity, g->dl_omega};
@@ -1122,6 +1123,7 @@ int nans_diff_backward(nans_world *w, const nans_diff_grads *g)
     b.g_mass = b.g_zw + nd;
     b.g_cr = b.g_mass + nd;
     b.g_cf = b.g_cr + S;
+    b.err = reinterpret_cast<int *>(b.g_cf + S);
     const int grid = std::max(1, std::min(S, 16 * w->sm_count));
     k_adjoint<<<grid, adjoint_threads(), 0, st>>>(w->dw, w->d_tape, (int)nst, w->tape_dt, b);
     CK(cudaGetLastError());
@@ -1144,8 +1146,14 @@ int nans_diff_backward(nans_world *w, const nans_diff_grads *g)
         CK(cudaMemcpyAsync(g->restitution, b.g_cr, S * sizeof(float), cudaMemcpyDeviceToHost, st));
     if (g->friction)
         CK(cudaMemcpyAsync(g->friction, b.g_cf, S * sizeof(float), cudaMemcpyDeviceToHost, st));
+    int err[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(err, b.err, sizeof(err), cudaMemcpyDeviceToHost, st));
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(st));
+    if (err[0])
+        return fail(NANS_ERR_CUDA, "diff_backward: inconsistent tape (check " + std::to_string(err[0]) + ": " +
+                                       std::to_string(err[1]) + ", " + std::to_string(err[2]) + ", " +
+                                       std::to_string(err[3]) + ")");
     return NANS_OK;
 }
 

@@ -38,7 +38,7 @@ __global__ void k_tape_copy(DevWorld w, TapeStep t)
         t.wend[j] = w.s_wcnt[j];
         const int s = w.cand_meta[j] >> 3;
         const int cb = w.cand_begin[s], mw = w.s_maxw[s];
-        const int nh = mw > 0 ? w.s_wcnt[cb + mw] : 0;
+        const int nh = mw > 0 ? w.s_wcnt[cb + mw - 1] : 0;
         if (j - cb >= nh)
             continue;
         const int c = w.s_perm[j];
@@ -51,8 +51,6 @@ __global__ void k_tape_copy(DevWorld w, TapeStep t)
         t.fwd[2 * (size_t)j] = w.s_fwd[2 * (size_t)c];
         t.fwd[2 * (size_t)j + 1] = w.s_fwd[2 * (size_t)c + 1];
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0)
-        t.wend[n] = w.s_wcnt[n];
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < w.n_scenes; s += stride)
     {
         t.cand_begin[s] = w.cand_begin[s];
@@ -60,12 +58,28 @@ __global__ void k_tape_copy(DevWorld w, TapeStep t)
     }
 }
 
+// Records the first inconsistency met (the tape is checked before it is followed).
+__device__ __forceinline__ void adj_error(const AdjointBufs &g, int kind, int x, int y, int z)
+{
+    if (atomicCAS(g.err, 0, kind) == 0)
+    {
+        g.err[1] = x;
+        g.err[2] = y;
+        g.err[3] = z;
+    }
+}
+
 // Adjoint of one contact's solve (contact_apply in k_solve.cu) on the closed form.
-__device__ __forceinline__ void contact_adjoint(const TapeStep &t, int j, float cr, float mu, AdjointBufs &g,
-                                                float &gcr, float &gmu)
+__device__ __forceinline__ void contact_adjoint(const DevWorld &w, const TapeStep &t, int j, float cr, float mu,
+                                                AdjointBufs &g, float &gcr, float &gmu)
 {
     const int a = t.a[j], b = t.b[j];
     const bool wb = !type_b_is_floor(t.type[j]);
+    if (a < 0 || a >= w.n_dyn || (wb && (b < 0 || b >= w.n_dyn)))
+    {
+        adj_error(g, 3, j, a, b);
+        return;
+    }
     const float4 *k = t.k + (size_t)9 * j;
     const float4 k0 = k[0], k1 = k[1], k2 = k[2], k3 = k[3], k4 = k[4], k5 = k[5], k6 = k[6], k7 = k[7], k8 = k[8];
     const v3 n = xyz(k0), t1 = xyz(k1), t2 = xyz(k2);
@@ -206,12 +220,25 @@ __global__ void __launch_bounds__(kAdjointThreads) k_adjoint(DevWorld w, const T
         for (int k = nsteps - 1; k >= 0; --k)
         {
             const TapeStep t = steps[k];
-            const int cb = t.cand_begin[s], maxw = t.maxw[s];
+            const int cb = t.cand_begin[s];
+            int maxw = t.maxw[s];
+            if (cb < 0 || cb > t.n || maxw < 0 || maxw > t.n - cb)
+            {
+                if (tid == 0)
+                    adj_error(g, 1, k, s, maxw);
+                maxw = 0;
+            }
             for (int wv = maxw; wv >= 1; --wv)
             {
-                const int lo = cb + t.wend[cb + wv - 1], hi = cb + t.wend[cb + wv];
-                for (int j = lo + tid; j < hi; j += blockDim.x)
-                    contact_adjoint(t, j, cr, mu, g, gcr, gmu);
+                const int lo = cb + ((wv == 1) ? 0 : t.wend[cb + wv - 2]), hi = cb + t.wend[cb + wv - 1];
+                if (lo < cb || hi > t.n || lo > hi)
+                {
+                    if (tid == 0)
+                        adj_error(g, 2, k, s, wv);
+                }
+                else
+                    for (int j = lo + tid; j < hi; j += blockDim.x)
+                        contact_adjoint(w, t, j, cr, mu, g, gcr, gmu);
                 __syncthreads();
             }
             for (int i = tid; i < nb; i += blockDim.x)

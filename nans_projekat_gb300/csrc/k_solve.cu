@@ -316,22 +316,24 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
         const int maxw = s_maxw;
         if (tid == 0 && w.s_maxw)
             w.s_maxw[s] = maxw;
-        // (3) counting sort by wave: s_wcnt[cb + wave] (waves 1..maxw, maxw <= nh)
-        for (int i = tid; i <= maxw; i += blockDim.x)
+        // (3) counting sort by wave. Wave v (1..maxw) counts at s_wcnt[cb + v - 1]: maxw entries,
+        // and maxw <= nh <= the scene's candidate slots, so scenes never share an entry. After
+        // the placement s_wcnt[cb + v - 1] is the end of wave v (wave 1 starts at 0).
+        for (int i = tid; i < maxw; i += blockDim.x)
             w.s_wcnt[cb + i] = 0;
         __syncthreads();
         for (int i = tid; i < nh; i += blockDim.x)
-            atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i], 1);
+            atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i] - 1, 1);
         __syncthreads();
         {
             int carry = 0;
-            for (int base = 0; base <= maxw; base += blockDim.x)
+            for (int base = 0; base < maxw; base += blockDim.x)
             {
                 int i = base + tid;
-                int v = (i <= maxw) ? w.s_wcnt[cb + i] : 0;
+                int v = (i < maxw) ? w.s_wcnt[cb + i] : 0;
                 int tot;
                 int pre = block_scan_excl(v, sh, &tot);
-                if (i <= maxw)
+                if (i < maxw)
                     w.s_wcnt[cb + i] = carry + pre;
                 carry += tot;
                 __syncthreads();
@@ -339,7 +341,7 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
         }
         for (int i = tid; i < nh; i += blockDim.x)
         {
-            int pos = atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i], 1);
+            int pos = atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i] - 1, 1);
             w.s_perm[cb + pos] = w.s_order[cb + i];
         }
         // (4) velocity-independent constants
@@ -360,7 +362,7 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
         const int iters = w.sc_iters[s];
         for (int wv = 1; wv <= maxw; ++wv)
         {
-            int lo = __ldcg(w.s_wcnt + cb + wv - 1), hi = __ldcg(w.s_wcnt + cb + wv);
+            int lo = (wv == 1) ? 0 : __ldcg(w.s_wcnt + cb + wv - 2), hi = __ldcg(w.s_wcnt + cb + wv - 1);
             for (int i = lo + tid; i < hi; i += blockDim.x)
             {
                 int c = __ldcg(w.s_perm + cb + i);

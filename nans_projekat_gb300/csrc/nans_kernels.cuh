@@ -73,17 +73,18 @@ void launch_solve(const DevWorld &w, int grid, int threads, size_t smem, cudaStr
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);
 
 // One step of the differentiable rollout's tape. Contact data is stored by solve slot: slot
-// cand_begin[s] + i holds the i-th contact of scene s in wave order, so one wave is a
-// contiguous slot range [wend[cb + w - 1], wend[cb + w]) offset by cb.
+// cand_begin[s] + i holds the i-th contact of scene s in wave order, so wave v is the
+// contiguous slot range cb + [v == 1 ? 0 : wend[cb + v - 2], wend[cb + v - 1]).
 struct TapeStep
 {
     int *a, *b, *type;        // per slot: bodies and pair type
     float4 *k;                // per slot: 9 float4 of contact constants (k_solve layout)
     float4 *fwd;              // per slot: (JdVn, JdVt1, JdVt2, flags), (dn, dt1, dt2, Ln)
-    int *wend;                // per slot index: end of each wave (k_solve's s_wcnt)
+    int *wend;                // per scene, from its first slot: end of each wave (k_solve's s_wcnt)
     int *cand_begin, *maxw;   // per scene
     float4 *v_pre, *w_pre;    // per dynamic body: V, W before this step's RK4
     float4 *f_ext, *t_ext;    // per dynamic body: external force / torque of this step, or null
+    int n;                    // slots (candidate pairs of the step)
 };
 
 // Adjoint accumulators, per dynamic body (float4 xyz) / per scene.
@@ -95,6 +96,7 @@ struct AdjointBufs
     float *g_z, *g_zw;        // accumulated dL/dz, dL/dzw of the RK4 closed form
     float *g_mass;            // out: dL/dm (moment of inertia proportional to mass)
     float *g_cr, *g_cf;       // out, per scene: dL/d restitution, dL/d friction
+    int *err;                 // [0] first inconsistency found (0 none), [1..3] its indices
 };
 
 int adjoint_threads();

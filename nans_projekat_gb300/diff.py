@@ -73,13 +73,23 @@ def final_state(world):
     return cat("Position"), cat("Angles"), cat("V"), cat("W")
 
 
+def _start(world, scenes, position0, angles0, velocity0, omega0, mass, restitution, friction):
+    """Puts the initial state into the world: a full upload when the masses or the solver
+    constants changed since the last rollout on this world, else the four state arrays only."""
+    key = (tuple(id(s) for s in scenes), mass.tobytes(), restitution.tobytes(), friction.tobytes())
+    if getattr(world, "_diff_key", None) != key:
+        world.upload_batch(with_state(scenes, position0, angles0, velocity0, omega0, mass, restitution, friction))
+        world._diff_key = key
+    else:
+        world.set_state_arrays(position0, angles0, velocity0, omega0)
+
+
 class _Rollout(torch.autograd.Function):
     @staticmethod
     def forward(ctx, world, scenes, dt, nsteps, position0, angles0, velocity0, omega0, mass, restitution, friction):
-        host = lambda t: t.detach().to("cpu", torch.float32).numpy()
-        sc = with_state(scenes, host(position0), host(angles0), host(velocity0), host(omega0), host(mass),
-                        host(restitution), host(friction))
-        world.upload_batch(sc)
+        host = lambda t: np.ascontiguousarray(t.detach().to("cpu", torch.float32).numpy())
+        _start(world, scenes, host(position0), host(angles0), host(velocity0), host(omega0), host(mass),
+               host(restitution), host(friction))
         world.diff_forward(dt, nsteps)
         ctx.world = world
         ctx.device = velocity0.device

@@ -116,6 +116,41 @@ def test_large_scene_cull_equals_all_pairs(nl):
     b.close()
 
 
+def _single_box_scenes(n):
+    from nans_projekat_gb300.types import SPHERE_DTYPE
+    out = []
+    for k in range(n):
+        pos = np.array([[0.01 * (k % 5), 0.49 + 0.002 * (k % 3), 0.0]])
+        m = np.ones(1)
+        cubes = scenes._cubes(pos, None, m, m / 12.0 * 2.0, vel=[[0.3 * ((k % 4) - 1.5), -0.5, 0.0]])
+        out.append(scenes.Scene(cubes, np.zeros(0, SPHERE_DTYPE), scenes.ground(20.0), name="box1"))
+    return out
+
+
+def test_one_wave_per_contact_scenes(nl, oracle_lib):
+    """Scenes whose every candidate is a contact in a wave of its own (one box on the ground:
+    one candidate, one contact, one wave) use all of their solver slots; 512 of them solved side
+    by side must still match the oracle."""
+    batch = _single_box_scenes(512)
+    dt = np.float32(1 / 60)
+    n = 30
+    o = _oracle_states(batch, n, dt)
+    for graph in (False, True):
+        w = nl.World()
+        w.upload_batch(batch)
+        if graph:
+            w.batch_step(dt, n, graph_steps=10)
+        else:
+            w.step(dt, n)
+        state = w.download()
+        for i in range(len(batch)):
+            cubes, _, _ = w.scene_state(i, state)
+            assert same_fields(o.state(i)[0], cubes, STATE_FIELDS)[0], (graph, i)
+            assert same_fields(o.pairs(i), w.pairs(i), PAIR_FIELDS)[0], (graph, i)
+        assert sum(len(w.pairs(i)) for i in range(0, 512, 16)) > 0
+        w.close()
+
+
 def test_warm_start_matches_oracle(nl, oracle_lib):
     """NANS_WORLD_WARM_START against the oracle's warm starting (accumulators carried across
     steps for pairs that stay in contact), bit for bit, on the batched and the plain path; and
