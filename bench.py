@@ -43,6 +43,21 @@ def _jsonable(o):
     raise TypeError(type(o).__name__)
 
 
+def _strict(o):
+    """Strict JSON: a non-finite float (never a headline figure) becomes its string form."""
+    if isinstance(o, dict):
+        return {k: _strict(v) for k, v in o.items()}
+    if isinstance(o, (list, tuple)):
+        return [_strict(v) for v in o]
+    if isinstance(o, (float, np.floating)) and not np.isfinite(o):
+        return str(float(o))
+    return o
+
+
+def emit(line):
+    print(json.dumps(_strict(line), default=_jsonable, allow_nan=False))
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -215,7 +230,7 @@ def cpu_sample_rate(scenes_list, seconds, threads, kind):
     t0 = time.perf_counter()
     run(1)
     t1 = time.perf_counter() - t0
-    n = max(1, min(200, int(seconds / max(t1, 1e-6))))
+    n = max(1, min(3000, int(seconds / max(t1, 1e-6))))
     t0 = time.perf_counter()
     run(n)
     t = time.perf_counter() - t0
@@ -271,7 +286,7 @@ def run_reference_arm(args):
                          "sample": "%d scenes (every %dth) per step, %d bodies" % (len(sample), stride, bodies)},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line, default=_jsonable))
+    emit(line)
 
 
 def secondary_measurements(lib, batch, device):
@@ -541,7 +556,7 @@ def run_ours(args):
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
-        print(json.dumps(line, default=_jsonable))
+        emit(line)
     w.close()
     if dist is not None:
         dist.destroy_process_group()

@@ -273,6 +273,17 @@ int nans_diff_backward(nans_world *world, const nans_diff_grads *grads);
 /* Steps and device bytes held by the current tape. */
 int nans_diff_tape_info(nans_world *world, uint32_t *steps, uint64_t *bytes);
 
+/* ---- headless rendering ------------------------------------------------------------ */
+
+/* A picture of one scene for visual debugging, without a graphics API (the reference draws with
+ * OpenGL, code/nans.cpp:1853-2025): CUDA kernels rasterise the boxes from the step's world
+ * vertices and ray-cast the spheres and the ground's top face; convex hulls appear as their
+ * bounding spheres. Camera at `eye` looking at `target`, vertical field of view fov_deg.
+ * rgb receives width * height * 3 bytes, rows top to bottom. Shows the state as of the last
+ * step (the Model rebuild of the step); not meant for per-frame use (it allocates). */
+int nans_render_scene(nans_world *world, uint32_t scene, const float eye[3], const float target[3], float fov_deg,
+                      uint32_t width, uint32_t height, uint8_t *rgb);
+
 /* ---- allocation-free solve -------------------------------------------------------- */
 
 /* No counterpart in the reference: an extra entry point for callers that must not allocate

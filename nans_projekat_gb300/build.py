@@ -26,8 +26,8 @@ NVCC_FLAGS = ARCH + [
     "-I", CSRC, "-I", INCLUDE,
 ]
 
-SOURCES = ["k_sweep.cu", "k_cull.cu", "k_narrow.cu", "k_epa_large.cu", "k_solve.cu", "k_adjoint.cu", "api.cu",
-           "noalloc.cu"]
+SOURCES = ["k_sweep.cu", "k_cull.cu", "k_narrow.cu", "k_epa_large.cu", "k_solve.cu", "k_adjoint.cu", "k_render.cu",
+           "api.cu", "noalloc.cu"]
 
 
 def nvcc():

@@ -424,6 +424,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &w->d_rec_floor, (size_t)61 * S)) || (rc = dalloc(w, L, &w->d_small, 2)) ||
         (rc = dalloc(w, L, &d.s_last, 1)))
         return rc;
+    // world vertices are written by the first step; zero until then (the renderer reads them)
+    CK(cudaMemset(d.verts, 0, (size_t)std::max(1LL, vert_floats) * sizeof(float)));
     d.sc_cube0 = p_cube0;
     d.sc_nc = p_nc;
     d.sc_ns = p_ns;
@@ -1154,6 +1156,38 @@ int nans_diff_backward(nans_world *w, const nans_diff_grads *g)
         return fail(NANS_ERR_CUDA, "diff_backward: inconsistent tape (check " + std::to_string(err[0]) + ": " +
                                        std::to_string(err[1]) + ", " + std::to_string(err[2]) + ", " +
                                        std::to_string(err[3]) + ")");
+    return NANS_OK;
+}
+
+int nans_render_scene(nans_world *w, uint32_t scene, const float eye[3], const float target[3], float fov_deg,
+                      uint32_t width, uint32_t height, uint8_t *rgb)
+{
+    if (!w || !eye || !target || !rgb)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "render: null argument");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "render: no scene uploaded");
+    if (scene >= (uint32_t)w->n_scenes)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "render: scene index out of range");
+    if (width < 1 || height < 1 || width > 8192 || height > 8192 || !(fov_deg > 1.0f && fov_deg < 179.0f))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "render: image size outside [1, 8192] or field of view outside (1, 179)");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    const size_t n = (size_t)width * height;
+    unsigned long long *fb = nullptr;
+    unsigned char *img = nullptr;
+    CK(cudaMalloc(&fb, n * sizeof(unsigned long long)));
+    cudaError_t e = cudaMalloc(&img, 3 * n);
+    if (e == cudaSuccess)
+        e = (cudaError_t)render_scene(w->dw, (int)scene, eye, target, fov_deg, (int)width, (int)height, fb, img, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(rgb, img, 3 * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
+    cudaFree(fb);
+    if (img)
+        cudaFree(img);
+    if (e != cudaSuccess)
+        return fail(NANS_ERR_CUDA, std::string("render: ") + cudaGetErrorString(e));
     return NANS_OK;
 }
 

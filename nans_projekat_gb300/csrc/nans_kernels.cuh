@@ -68,6 +68,8 @@ int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaErro
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
 int solve_threads(int max_scene_bodies);
+int render_scene(const DevWorld &w, int scene, const float eye[3], const float target[3], float fov_deg, int width,
+                 int height, unsigned long long *fb, unsigned char *rgb, cudaStream_t st);
 const void *solve_kernel(const DevWorld &w);
 void launch_solve(const DevWorld &w, int grid, int threads, size_t smem, cudaStream_t st, float dt, int pass);
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);

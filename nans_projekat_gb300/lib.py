@@ -40,7 +40,7 @@ EXPORTS = (
     "nans_get_pairs", "nans_world_status", "nans_world_counts", "nans_world_stream",
     "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps",
     "nans_world_epa_stats", "nans_solve_contacts_static", "nans_diff_forward", "nans_diff_backward",
-    "nans_diff_tape_info", "nans_world_set_state_arrays", "nans_world_get_state_arrays",
+    "nans_diff_tape_info", "nans_world_set_state_arrays", "nans_world_get_state_arrays", "nans_render_scene",
 )
 
 
@@ -99,6 +99,7 @@ def load(path=LIB_PATH):
     L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
     L.nans_world_epa_stats.argtypes = [_P, _P, ctypes.c_int]
     L.nans_world_set_state_arrays.argtypes = [_P, _P, _P, _P, _P]
+    L.nans_render_scene.argtypes = [_P, _U, _P, _P, _F, _U, _U, _P]
     L.nans_world_get_state_arrays.argtypes = [_P, _P, _P, _P, _P]
     L.nans_diff_forward.argtypes = [_P, ctypes.POINTER(StepParams), _F, _U]
     L.nans_diff_backward.argtypes = [_P, ctypes.POINTER(DiffGrads)]
@@ -248,6 +249,14 @@ class World:
         _check(self.lib.nans_world_get_state_arrays(self.h, *[_ptr(a) for a in out]))
         return out
 
+    def render(self, scene=0, eye=(6.0, 4.0, 8.0), target=(0.0, 0.5, 0.0), fov=45.0, width=640, height=480):
+        """(height, width, 3) uint8 picture of one scene (headless CUDA rasteriser)."""
+        img = np.zeros((height, width, 3), np.uint8)
+        e = np.asarray(eye, np.float32)
+        t = np.asarray(target, np.float32)
+        _check(self.lib.nans_render_scene(self.h, scene, _ptr(e), _ptr(t), fov, width, height, _ptr(img)))
+        return img
+
     def pairs(self, scene=0):
         cnt = _U()
         _check(self.lib.nans_get_pairs(self.h, scene, None, 0, ctypes.byref(cnt)))
@@ -331,6 +340,14 @@ class World:
     @property
     def stream(self):
         return self.lib.nans_world_stream(self.h)
+
+
+def save_ppm(path, img):
+    """Writes a (height, width, 3) uint8 image as binary PPM."""
+    h, w = img.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(img, np.uint8).tobytes())
 
 
 def solve_contacts_static(nbodies, ncubes, d_position, d_mass, d_moi, d_velocity, d_angular_velocity, floor,

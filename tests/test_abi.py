@@ -43,3 +43,13 @@ def test_last_error_is_empty_string_initially():
     from nans_projekat_gb300 import lib
     L = lib.load()
     assert isinstance(L.nans_last_error(), bytes)
+
+
+def test_save_ppm(tmp_path):
+    import numpy as np
+    from nans_projekat_gb300 import lib
+    img = np.arange(2 * 3 * 3, dtype=np.uint8).reshape(2, 3, 3)
+    p = tmp_path / "a.ppm"
+    lib.save_ppm(str(p), img)
+    raw = p.read_bytes()
+    assert raw.startswith(b"P6\n3 2\n255\n") and raw[-18:] == img.tobytes()
