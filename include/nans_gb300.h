@@ -224,6 +224,12 @@ void *nans_world_stream(nans_world *world);
  * [3] warp-tier EPA, [4] large-polytope EPA, [5] solver. */
 int nans_profile_steps(nans_world *world, float dt, uint32_t nsteps, float *stage_ms);
 
+/* Runs nsteps eager steps with the production stream overlap and adds to t_ms[0..6] the time
+ * from the step's start at which each stage ended: [0] sweep, [1] cull, [2] GJK + per-thread
+ * EPA, [3] warp-tier EPA (second stream), [4] large-polytope EPA (second stream), [5] solve of
+ * the scenes without escalated EPAs, [6] solve of the rest (the step's end). */
+int nans_profile_timeline(nans_world *world, float dt, uint32_t nsteps, float *t_ms);
+
 /* Kernel launches per step on the batched path and on the plain path. */
 int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain);
 

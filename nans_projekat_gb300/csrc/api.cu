@@ -529,22 +529,34 @@ void enqueue_cull(nans_world *w)
 // while the first solve pass handles every scene they do not touch; the second pass solves
 // the rest after them. Both streams are joined before the function returns (also under
 // stream capture).
-cudaError_t enqueue_narrow_solve(nans_world *w, float dt)
+// tl (timeline profiling only, else null): events recorded after the per-thread EPA (stream 1),
+// the warp tier and the large tiers (stream 2), solve pass 0 and pass 1 (stream 1).
+cudaError_t enqueue_narrow_solve(nans_world *w, float dt, cudaEvent_t *tl)
 {
     cudaStream_t st = w->stream, st2 = w->stream2;
     launch_narrow_tiny(narrow_grid(w), st, w->dw);
+    if (tl)
+        cudaEventRecord(tl[0], st);
     cudaError_t e = cudaEventRecord(w->ev_fork, st);
     if (e == cudaSuccess)
         e = cudaStreamWaitEvent(st2, w->ev_fork, 0);
     if (e != cudaSuccess)
         return e;
     launch_epa_medium(st2, w->dw);
+    if (tl)
+        cudaEventRecord(tl[1], st2);
     e = (cudaError_t)launch_narrow_big(st2, w->dw);
+    if (tl)
+        cudaEventRecord(tl[2], st2);
     launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
+    if (tl)
+        cudaEventRecord(tl[3], st);
     cudaError_t e2 = cudaEventRecord(w->ev_join, st2);
     if (e2 == cudaSuccess)
         e2 = cudaStreamWaitEvent(st, w->ev_join, 0);
     launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 1);
+    if (tl)
+        cudaEventRecord(tl[4], st);
     return e != cudaSuccess ? e : e2;
 }
 
@@ -607,7 +619,7 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
             CK(cudaGetLastError());
         }
     }
-    CK(enqueue_narrow_solve(w, dt));
+    CK(enqueue_narrow_solve(w, dt, nullptr));
     CK(cudaGetLastError());
     after_step(w, dt);
     return NANS_OK;
@@ -660,7 +672,7 @@ int ensure_graph(nans_world *w, float dt, int gsteps)
         k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, dt, dt,
                                                                                            SW_INTEGRATE | SW_APPLY_VEL);
         enqueue_cull(w);
-        enqueue_narrow_solve(w, dt);
+        enqueue_narrow_solve(w, dt, nullptr);
     }
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess)
@@ -1409,7 +1421,6 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
         CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
         CK(cudaMemsetAsync(d.scene_late, 0, w->n_scenes * sizeof(int), st));
-    CK(cudaMemsetAsync(d.scene_late, 0, w->n_scenes * sizeof(int), st));
         CK(cudaEventRecord(ev[0], st));
         k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
                                                                                            sweep_flags(w));
@@ -1436,6 +1447,50 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         }
     }
     for (int i = 0; i < 7; ++i)
+        cudaEventDestroy(ev[i]);
+    return check_status(w);
+}
+
+int nans_profile_timeline(nans_world *w, float dt, uint32_t nsteps, float *t_ms)
+{
+    if (!w || !t_ms)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "timeline: null argument");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "timeline: no scene uploaded");
+    if (!valid_dt(dt))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "timeline: dt must be finite and positive");
+    CK(cudaSetDevice(w->device));
+    cudaStream_t st = w->stream;
+    cudaEvent_t ev[8];
+    for (int i = 0; i < 8; ++i)
+        CK(cudaEventCreate(&ev[i]));
+    for (int i = 0; i < 7; ++i)
+        t_ms[i] = 0.0f;
+    DevWorld &d = w->dw;
+    for (uint32_t k = 0; k < nsteps; ++k)
+    {
+        CK(cudaEventRecord(ev[0], st));
+        CK(cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st));
+        CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
+        CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
+        CK(cudaMemsetAsync(d.scene_late, 0, w->n_scenes * sizeof(int), st));
+        k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, w->pending_dt, dt,
+                                                                                           sweep_flags(w));
+        CK(cudaEventRecord(ev[1], st));
+        enqueue_cull(w);
+        CK(cudaEventRecord(ev[2], st));
+        CK(enqueue_narrow_solve(w, dt, ev + 3));
+        CK(cudaGetLastError());
+        after_step(w, dt);
+        CK(cudaEventSynchronize(ev[7]));
+        for (int i = 0; i < 7; ++i)
+        {
+            float ms = 0.0f;
+            CK(cudaEventElapsedTime(&ms, ev[0], ev[i + 1]));
+            t_ms[i] += ms;
+        }
+    }
+    for (int i = 0; i < 8; ++i)
         cudaEventDestroy(ev[i]);
     return check_status(w);
 }

@@ -6,9 +6,9 @@
 // words are contiguous and start on a word boundary (scene s owns words [sc_word0[s],
 // sc_word0[s+1]); word_scene maps a word back to its scene). Three passes keep the order while
 // skipping pairs whose inflated AABBs are disjoint:
-//   k_cull_mask   one thread per word: the word's bits, a count per block
+//   k_cull_mask   one warp per word, one lane per pair: the word's bits, a count per block
 //   k_cull_scan   exclusive scan of the block counts -> candidate offsets, total, capacity
-//   k_cull_write  each thread writes its word's pairs at its prefix position
+//   k_cull_write  the pairs of each word at its prefix position, one lane per pair
 // all_pairs != 0 keeps every pair (the reference's exact all-pairs behaviour).
 #include "nans_kernels.cuh"
 
@@ -122,56 +122,100 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int *total)
     return warp_prefix + x - v;
 }
 
-// Box test of the pairs of one mask word: word wi of scene s covers the scene's pairs
-// 32*(wi - sc_word0[s]) onward. Body ids are global (pair_bodies); the box of body a is kept in
-// registers while consecutive pairs share it.
-__device__ __forceinline__ unsigned word_mask(const DevWorld &w, int wi, int all_pairs)
+// (type, i, j) of the pair `off` places after (type0, i0, j0), the pair at scene-local index
+// p0: for cube-cube pairs the same row or the next one directly, otherwise a full decode.
+__device__ __forceinline__ void pair_after(long long p0, int nc, int ns, int type0, int i0, int j0, int off,
+                                           int &type, int &i, int &j)
 {
-    const int s = w.word_scene[wi];
-    const int nc = __ldg(w.sc_nc + s), ns = __ldg(w.sc_ns + s);
-    const long long npair = scene_pair_count(nc, ns);
-    const long long p0 = (long long)(wi - __ldg(w.sc_word0 + s)) * 32;
-    const int cnt = (int)min(32ll, npair - p0);
-    int type, i, j;
-    decode_pair(p0, nc, ns, type, i, j);
-    unsigned mask = 0u;
-    int last_a = -1;
-    float4 la = make_float4(0.f, 0.f, 0.f, 0.f), ha = la;
-    for (int bit = 0; bit < cnt; ++bit)
+    if (type0 == T_CC)
     {
-        int a, b;
-        pair_bodies(w, s, type, i, j, a, b);
-        if (all_pairs)
-            mask |= 1u << bit;
-        else
+        const int r0 = nc - j0; // pairs (i0, j0 .. nc-1)
+        if (off < r0)
         {
-            if (a != last_a)
-            {
-                la = __ldg(w.box_lo + a);
-                ha = __ldg(w.box_hi + a);
-                last_a = a;
-            }
-            const float4 lb = __ldg(w.box_lo + b), hb = __ldg(w.box_hi + b);
-            if (la.x <= hb.x && lb.x <= ha.x && la.y <= hb.y && lb.y <= ha.y && la.z <= hb.z && lb.z <= ha.z)
-                mask |= 1u << bit;
+            type = T_CC;
+            i = i0;
+            j = j0 + off;
+            return;
         }
-        advance_local(nc, ns, type, i, j);
+        if (off - r0 < nc - i0 - 2) // pairs (i0+1, i0+2 .. nc-1)
+        {
+            type = T_CC;
+            i = i0 + 1;
+            j = i0 + 2 + (off - r0);
+            return;
+        }
     }
-    return mask;
+    decode_pair(p0 + off, nc, ns, type, i, j);
 }
 
-// One thread per mask word; per block, the number of culled pairs.
+// Global body ids of pair (type, i, j) of scene s whose cubes start at c0 (nc cubes).
+__device__ __forceinline__ void pair_ids(const DevWorld &w, int s, int c0, int nc, int type, int i, int j, int &a,
+                                         int &b)
+{
+    const int s0 = c0 + nc;
+    a = type_a_is_sphere(type) ? s0 + i : c0 + i;
+    if (type_b_is_floor(type))
+        b = w.n_dyn + s;
+    else
+        b = type_b_is_sphere(type) ? s0 + j : c0 + j;
+}
+
+// One warp per mask word, one lane per pair (bit = lane): the pairs' second boxes are read
+// coalesced and the word is a ballot. Lane q first loads the scene data of word w0 + q and
+// decodes its first pair (32 decodes side by side); the warp then walks the 32 words with
+// that data broadcast by shuffles. A block covers kCullThreads words, as the scan and the
+// write expect. Per block, the number of culled pairs.
 __global__ void __launch_bounds__(kCullThreads) k_cull_mask(DevWorld w, int all_pairs)
 {
     __shared__ int sh[32];
-    const int wi = blockIdx.x * blockDim.x + threadIdx.x;
-    unsigned mask = 0u;
-    if (wi < w.n_words)
+    const int lane = threadIdx.x & 31;
+    const int wo = blockIdx.x * kCullThreads + threadIdx.x;
+    const int w0 = wo - lane;
+    int s = 0, nc = 0, ns = 0, c0 = 0, t0 = 0, i0 = 0, j0 = 0, cnt = 0;
+    long long p0 = 0;
+    if (wo < w.n_words)
     {
-        mask = word_mask(w, wi, all_pairs);
-        w.pair_mask[wi] = mask;
+        s = __ldg(w.word_scene + wo);
+        nc = __ldg(w.sc_nc + s);
+        ns = __ldg(w.sc_ns + s);
+        c0 = __ldg(w.sc_cube0 + s);
+        p0 = (long long)(wo - __ldg(w.sc_word0 + s)) * 32;
+        cnt = (int)min(32ll, scene_pair_count(nc, ns) - p0);
+        decode_pair(p0, nc, ns, t0, i0, j0);
     }
-    const int total = block_sum(__popc(mask), sh);
+    unsigned keep = 0u; // lane q keeps word w0 + q
+    const int nq = min(32, w.n_words - w0);
+    for (int q = 0; q < nq; ++q)
+    {
+        const int qcnt = __shfl_sync(0xffffffffu, cnt, q);
+        const int qs = __shfl_sync(0xffffffffu, s, q);
+        const int qnc = __shfl_sync(0xffffffffu, nc, q), qns = __shfl_sync(0xffffffffu, ns, q);
+        const int qc0 = __shfl_sync(0xffffffffu, c0, q);
+        const int qt = __shfl_sync(0xffffffffu, t0, q), qi = __shfl_sync(0xffffffffu, i0, q);
+        const int qj = __shfl_sync(0xffffffffu, j0, q);
+        const long long qp0 = __shfl_sync(0xffffffffu, p0, q);
+        bool hit = false;
+        if (lane < qcnt)
+        {
+            if (all_pairs)
+                hit = true;
+            else
+            {
+                int type, i, j, a, b;
+                pair_after(qp0, qnc, qns, qt, qi, qj, lane, type, i, j);
+                pair_ids(w, qs, qc0, qnc, type, i, j, a, b);
+                const float4 la = __ldg(w.box_lo + a), ha = __ldg(w.box_hi + a);
+                const float4 lb = __ldg(w.box_lo + b), hb = __ldg(w.box_hi + b);
+                hit = la.x <= hb.x && lb.x <= ha.x && la.y <= hb.y && lb.y <= ha.y && la.z <= hb.z && lb.z <= ha.z;
+            }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (lane == q)
+            keep = m;
+    }
+    if (wo < w.n_words)
+        w.pair_mask[wo] = keep;
+    const int total = block_sum(__popc(keep), sh);
     if (threadIdx.x == 0)
         w.block_hits[blockIdx.x] = total;
 }
@@ -211,43 +255,58 @@ __global__ void __launch_bounds__(1024) k_cull_scan(DevWorld w, int nblocks)
     }
 }
 
-// Each thread writes its word's culled pairs at its prefix position (scene-major order).
+// The culled pairs at their prefix positions (scene-major order). Thread t of the block owns
+// word blockIdx.x * kCullThreads + t: its scan position, scene data and first pair; each warp
+// then walks its non-empty words, one lane per pair, so that a word's candidates are written
+// by consecutive lanes.
 __global__ void __launch_bounds__(kCullThreads) k_cull_write(DevWorld w)
 {
     __shared__ int sh[32];
-    const int wi = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned mask = (wi < w.n_words) ? w.pair_mask[wi] : 0u;
+    const int lane = threadIdx.x & 31;
+    const int wo = blockIdx.x * kCullThreads + threadIdx.x;
+    const unsigned own = (wo < w.n_words) ? w.pair_mask[wo] : 0u;
     int total;
-    int pos = w.block_hits[blockIdx.x] + block_exclusive_scan(__popc(mask), sh, &total);
-    if (mask == 0u)
-        return;
-    const int s = w.word_scene[wi];
-    const int nc = __ldg(w.sc_nc + s), ns = __ldg(w.sc_ns + s);
-    const long long p0 = (long long)(wi - __ldg(w.sc_word0 + s)) * 32;
-    int type, i, j;
-    decode_pair(p0, nc, ns, type, i, j);
-    const int cap = w.cand_cap;
-    for (int bit = 0; bit < 32; ++bit)
+    const int own_pos = w.block_hits[blockIdx.x] + block_exclusive_scan(__popc(own), sh, &total);
+    const int w0 = wo - lane;
+    int s = 0, nc = 0, ns = 0, c0 = 0, t0 = 0, i0 = 0, j0 = 0;
+    long long p0 = 0;
+    if (own)
     {
-        if (mask & (1u << bit))
-        {
-            if (pos < cap)
-            {
-                int a, b;
-                pair_bodies(w, s, type, i, j, a, b);
-                w.cand_a[pos] = a;
-                w.cand_b[pos] = b;
-                w.cand_meta[pos] = (s << 3) | type;
-                if (w.cand_pidx)
-                    w.cand_pidx[pos] = wi * 32 + bit;
-            }
-            ++pos;
-        }
-        if ((mask >> bit) <= 1u)
-            break;
-        advance_local(nc, ns, type, i, j);
+        s = __ldg(w.word_scene + wo);
+        nc = __ldg(w.sc_nc + s);
+        ns = __ldg(w.sc_ns + s);
+        c0 = __ldg(w.sc_cube0 + s);
+        p0 = (long long)(wo - __ldg(w.sc_word0 + s)) * 32;
+        decode_pair(p0, nc, ns, t0, i0, j0);
+    }
+    const int cap = w.cand_cap;
+    unsigned todo = __ballot_sync(0xffffffffu, own != 0u);
+    while (todo)
+    {
+        const int q = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        const unsigned m = __shfl_sync(0xffffffffu, own, q);
+        const int pos0 = __shfl_sync(0xffffffffu, own_pos, q);
+        const int qs = __shfl_sync(0xffffffffu, s, q);
+        const int qnc = __shfl_sync(0xffffffffu, nc, q), qns = __shfl_sync(0xffffffffu, ns, q);
+        const int qc0 = __shfl_sync(0xffffffffu, c0, q);
+        const int qt = __shfl_sync(0xffffffffu, t0, q), qi = __shfl_sync(0xffffffffu, i0, q);
+        const int qj = __shfl_sync(0xffffffffu, j0, q);
+        const long long qp0 = __shfl_sync(0xffffffffu, p0, q);
+        if (!(m & (1u << lane)))
+            continue;
+        const int pos = pos0 + __popc(m & ((1u << lane) - 1u));
+        if (pos >= cap)
+            continue;
+        int type, i, j, a, b;
+        pair_after(qp0, qnc, qns, qt, qi, qj, lane, type, i, j);
+        pair_ids(w, qs, qc0, qnc, type, i, j, a, b);
+        w.cand_a[pos] = a;
+        w.cand_b[pos] = b;
+        w.cand_meta[pos] = (qs << 3) | type;
+        if (w.cand_pidx)
+            w.cand_pidx[pos] = (w0 + q) * 32 + lane;
     }
 }
-
 
 } // namespace nans

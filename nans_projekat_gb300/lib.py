@@ -38,7 +38,7 @@ EXPORTS = (
     "nans_world_create", "nans_world_destroy", "nans_world_upload", "nans_batch_upload", "nans_step",
     "nans_batch_step", "nans_batch_autotune", "nans_world_download", "nans_world_set_state",
     "nans_get_pairs", "nans_world_status", "nans_world_counts", "nans_world_stream",
-    "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps",
+    "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps", "nans_profile_timeline",
     "nans_world_epa_stats", "nans_solve_contacts_static", "nans_diff_forward", "nans_diff_backward",
     "nans_diff_tape_info", "nans_world_set_state_arrays", "nans_world_get_state_arrays", "nans_render_scene",
 )
@@ -97,6 +97,7 @@ def load(path=LIB_PATH):
     L.nans_launches_per_step.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(_U)]
     L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
     L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
+    L.nans_profile_timeline.argtypes = [_P, _F, _U, _P]
     L.nans_world_epa_stats.argtypes = [_P, _P, ctypes.c_int]
     L.nans_world_set_state_arrays.argtypes = [_P, _P, _P, _P, _P]
     L.nans_render_scene.argtypes = [_P, _U, _P, _P, _F, _U, _U, _P]
@@ -286,6 +287,14 @@ class World:
         ms = np.zeros(6, np.float32)
         _check(self.lib.nans_profile_steps(self.h, dt, n, _ptr(ms)))
         return ms
+
+    def timeline(self, dt, n):
+        """Mean milliseconds from a step's start to the end of each stage over n eager steps
+        with the stream overlap: sweep, cull, GJK + per-thread EPA, warp tier, large tiers
+        (second stream), solve pass 0, solve pass 1 (the step's end)."""
+        ms = np.zeros(7, np.float32)
+        _check(self.lib.nans_profile_timeline(self.h, dt, n, _ptr(ms)))
+        return ms / max(1, n)
 
     def epa_stats(self, reset=False):
         out = np.zeros(8, np.uint32)
