@@ -369,22 +369,18 @@ constexpr int kTinyThreads = 64;
 #ifndef NANS_TINY_F
 #define NANS_TINY_F 20
 #endif
-#ifndef NANS_TINY_FD
-#define NANS_TINY_FD 0 // 1: cache each face's distance; 0: recompute it (less shared memory, faster)
-#endif
 constexpr int kTinyV = NANS_TINY_V;
 constexpr int kTinyF = NANS_TINY_F;
 constexpr int kTinyE = 12;
+constexpr unsigned kNoCanon = 15u; // a vertex with a NaN coordinate: equal to no vertex
+static_assert(kTinyV < 15, "vertex and canonical indices are packed in 4 bits");
 
 struct TinySmem
 {
     float px[kTinyV][kTinyThreads], py[kTinyV][kTinyThreads], pz[kTinyV][kTinyThreads];
     float fnx[kTinyF][kTinyThreads], fny[kTinyF][kTinyThreads], fnz[kTinyF][kTinyThreads];
-#if NANS_TINY_FD
-    float fd[kTinyF][kTinyThreads];
-#endif
-    unsigned fidx[kTinyF][kTinyThreads]; // a | b << 8 | c << 16
-    unsigned short edge[kTinyE][kTinyThreads]; // a | b << 8
+    unsigned fidx[kTinyF][kTinyThreads];       // a | b << 8 | c << 16
+    unsigned short edge[kTinyE][kTinyThreads]; // u | v << 4 | canon(u) << 8 | canon(v) << 12
 };
 
 struct TinyLocal
@@ -394,7 +390,11 @@ struct TinyLocal
 
 __device__ __forceinline__ v3 tiny_p(const TinySmem &S, int t, int i) { return mk3(S.px[i][t], S.py[i][t], S.pz[i][t]); }
 
-__device__ __forceinline__ void tiny_put(TinySmem &S, TinyLocal &L, int t, int i, const GV &g)
+// Stores vertex i and returns its canonical index: the first vertex whose P equals it (P
+// equality is what the reference's edge matching compares), kNoCanon when P has a NaN.
+// `canon` holds the canonical indices of vertices 0..i-1, 4 bits each.
+__device__ __forceinline__ unsigned tiny_put(TinySmem &S, TinyLocal &L, int t, int i, const GV &g,
+                                             unsigned long long canon)
 {
     S.px[i][t] = g.p.x;
     S.py[i][t] = g.p.y;
@@ -405,10 +405,17 @@ __device__ __forceinline__ void tiny_put(TinySmem &S, TinyLocal &L, int t, int i
     L.sb[i][0] = g.sb.x;
     L.sb[i][1] = g.sb.y;
     L.sb[i][2] = g.sb.z;
+    if (isnan(g.p.x) || isnan(g.p.y) || isnan(g.p.z))
+        return kNoCanon;
+    for (int j = 0; j < i; ++j)
+        if (eq3(tiny_p(S, t, j), g.p))
+            return (unsigned)(canon >> (4 * j)) & 15u;
+    return (unsigned)i;
 }
 
-// PushTriangle (code/nans.cpp:292-322) with the face distance cached.
-__device__ __forceinline__ void tiny_face(TinySmem &S, int t, int f, int a, int b, int c)
+// PushTriangle (code/nans.cpp:292-322); returns the face's distance |dot(N, A)|, which the
+// reference recomputes from the same operands in its closest-face search (bit-equal).
+__device__ __forceinline__ float tiny_face(TinySmem &S, int t, int f, int a, int b, int c)
 {
     v3 pa = tiny_p(S, t, a), pb = tiny_p(S, t, b), pc = tiny_p(S, t, c);
     v3 n = normalize3(cross3(pb - pa, pc - pa));
@@ -418,50 +425,46 @@ __device__ __forceinline__ void tiny_face(TinySmem &S, int t, int f, int a, int 
     S.fnx[f][t] = n.x;
     S.fny[f][t] = n.y;
     S.fnz[f][t] = n.z;
-#if NANS_TINY_FD
-    S.fd[f][t] = fabsf(dot3(n, pa));
-#endif
+    return fabsf(dot3(n, pa));
 }
 
-// The face's distance |dot(N, A)| (cached, or recomputed from the same operands: bit-equal).
-__device__ __forceinline__ float tiny_fd(const TinySmem &S, int t, int f)
+// PushEdge (code/nans.cpp:232-266), sequential. The stored edge (x, y) is the reverse of (u, v)
+// when P(x) == P(v) and P(y) == P(u): equal canonical indices (a NaN vertex matches nothing).
+// Returns false on overflow.
+__device__ __forceinline__ bool tiny_edge(TinySmem &S, int t, unsigned long long canon, int &ne, int u, int v)
 {
-#if NANS_TINY_FD
-    return S.fd[f][t];
-#else
-    const v3 n = mk3(S.fnx[f][t], S.fny[f][t], S.fnz[f][t]);
-    return fabsf(dot3(n, tiny_p(S, t, S.fidx[f][t] & 0xffu)));
-#endif
-}
-
-// PushEdge (code/nans.cpp:232-266), sequential. Returns false on overflow.
-__device__ __forceinline__ bool tiny_edge(TinySmem &S, int t, int &ne, int u, int v)
-{
-    v3 pu = tiny_p(S, t, u), pv = tiny_p(S, t, v);
-    for (int e = 0; e < ne; ++e)
+    const unsigned cu = (unsigned)(canon >> (4 * u)) & 15u, cv = (unsigned)(canon >> (4 * v)) & 15u;
+    if (cu != kNoCanon && cv != kNoCanon)
     {
-        unsigned ed = S.edge[e][t];
-        if (eq3(tiny_p(S, t, ed & 0xffu), pv) && eq3(tiny_p(S, t, ed >> 8), pu))
+        const unsigned want = cv | (cu << 4);
+        for (int e = 0; e < ne; ++e)
         {
-            for (int k = e + 1; k < ne; ++k)
-                S.edge[k - 1][t] = S.edge[k][t];
-            --ne;
-            return true;
+            if ((unsigned)(S.edge[e][t] >> 8) == want)
+            {
+                for (int k = e + 1; k < ne; ++k)
+                    S.edge[k - 1][t] = S.edge[k][t];
+                --ne;
+                return true;
+            }
         }
     }
     if (ne >= kTinyE)
         return false;
-    S.edge[ne][t] = (unsigned short)(u | (v << 8));
+    S.edge[ne][t] = (unsigned short)(u | (v << 4) | (cu << 8) | (cv << 12));
     ++ne;
     return true;
 }
 
 // ResolveCollision (code/nans.cpp:787-904) by one thread; same results as epa_run.
 // `simp` is the GJK simplex as the GJK pass stored it (4 x (P, SupA, SupB), 36 floats).
+// The closest-face search of the next iteration is folded into the removal pass and the face
+// creation: a running minimum with strict '<' over the kept faces, then the new ones, in list
+// order, is the reference's scan (a NaN first distance keeps face 0, as its scan does).
 __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, const Shape &B, const float *simp,
                         v3 &out_pa, v3 &out_pb, v3 &out_n)
 {
     TinyLocal L;
+    unsigned long long canon = 0ull;
     for (int i = 0; i < 4; ++i)
     {
         const float *q = simp + 9 * i;
@@ -469,30 +472,36 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
         g.p = mk3(q[0], q[1], q[2]);
         g.sa = mk3(q[3], q[4], q[5]);
         g.sb = mk3(q[6], q[7], q[8]);
-        tiny_put(S, L, t, i, g);
+        canon |= (unsigned long long)tiny_put(S, L, t, i, g, canon) << (4 * i);
     }
-    tiny_face(S, t, 0, 0, 1, 2);
-    tiny_face(S, t, 1, 0, 2, 3);
-    tiny_face(S, t, 2, 0, 3, 1);
-    tiny_face(S, t, 3, 1, 3, 2);
+    float cur = tiny_face(S, t, 0, 0, 1, 2);
+    int ci = 0;
+    {
+        const float d1 = tiny_face(S, t, 1, 0, 2, 3);
+        if (d1 < cur)
+        {
+            cur = d1;
+            ci = 1;
+        }
+        const float d2 = tiny_face(S, t, 2, 0, 3, 1);
+        if (d2 < cur)
+        {
+            cur = d2;
+            ci = 2;
+        }
+        const float d3 = tiny_face(S, t, 3, 1, 3, 2);
+        if (d3 < cur)
+        {
+            cur = d3;
+            ci = 3;
+        }
+    }
     int nf = 4, nv = 4;
     bool stale = false;
     for (int it = 0; it <= 64; ++it)
     {
         if (nf == 0 && !stale)
             return EPA_NONE;
-        int ci = 0;
-        float cur = tiny_fd(S, t, 0);
-        if (nf > 0 && !isnan(cur))
-            for (int f = 1; f < nf; ++f)
-            {
-                float d = tiny_fd(S, t, f);
-                if (d < cur)
-                {
-                    cur = d;
-                    ci = f;
-                }
-            }
         const v3 n = mk3(S.fnx[ci][t], S.fny[ci][t], S.fnz[ci][t]);
         const GV ns = minkowski_support(w.verts, A, B, n);
         if (dot3(n, ns.p) - cur < 0.001f)
@@ -523,8 +532,10 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
         }
         if (nf == 0)
             return EPA_NONE; // the stale read repeats identically until the iteration cap
-        // visible faces -> horizon edges, the others compacted in place (code/nans.cpp:869-891)
-        int ne = 0, keep = 0;
+        // visible faces -> horizon edges, the others compacted in place (code/nans.cpp:869-891),
+        // with the running closest-face search over the kept ones
+        int ne = 0, keep = 0, nci = 0;
+        float ncur = 0.0f;
         for (int f = 0; f < nf; ++f)
         {
             unsigned fi = S.fidx[f][t];
@@ -533,7 +544,8 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
             if (dot3(fn, ns.p - fa) > 0.0f)
             {
                 int a = fi & 0xffu, b = (fi >> 8) & 0xffu, c = fi >> 16;
-                if (!(tiny_edge(S, t, ne, a, b) && tiny_edge(S, t, ne, b, c) && tiny_edge(S, t, ne, c, a)))
+                if (!(tiny_edge(S, t, canon, ne, a, b) && tiny_edge(S, t, canon, ne, b, c) &&
+                      tiny_edge(S, t, canon, ne, c, a)))
                     return EPA_OVERFLOW;
             }
             else
@@ -544,9 +556,12 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
                     S.fnx[keep][t] = fn.x;
                     S.fny[keep][t] = fn.y;
                     S.fnz[keep][t] = fn.z;
-#if NANS_TINY_FD
-                    S.fd[keep][t] = S.fd[f][t];
-#endif
+                }
+                const float d = fabsf(dot3(fn, fa));
+                if (keep == 0 || d < ncur)
+                {
+                    ncur = d;
+                    nci = keep;
                 }
                 ++keep;
             }
@@ -557,23 +572,31 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
         {
             // every face removed: slot 0 keeps the last face of the list (nothing was moved)
             int l = nf - 1;
-            S.fidx[0][t] = S.fidx[l][t];
-            S.fnx[0][t] = S.fnx[l][t];
-            S.fny[0][t] = S.fny[l][t];
-            S.fnz[0][t] = S.fnz[l][t];
-#if NANS_TINY_FD
-            S.fd[0][t] = S.fd[l][t];
-#endif
+            const unsigned fi = S.fidx[l][t];
+            const v3 fn = mk3(S.fnx[l][t], S.fny[l][t], S.fnz[l][t]);
+            S.fidx[0][t] = fi;
+            S.fnx[0][t] = fn.x;
+            S.fny[0][t] = fn.y;
+            S.fnz[0][t] = fn.z;
+            ncur = fabsf(dot3(fn, tiny_p(S, t, fi & 0xffu)));
+            nci = 0;
             stale = true;
         }
         int sv = nv++;
-        tiny_put(S, L, t, sv, ns);
+        canon |= (unsigned long long)tiny_put(S, L, t, sv, ns, canon) << (4 * sv);
         for (int j = 0; j < ne; ++j)
         {
-            unsigned ed = S.edge[j][t];
-            tiny_face(S, t, keep + j, sv, ed & 0xffu, ed >> 8);
+            const unsigned ed = S.edge[j][t];
+            const float d = tiny_face(S, t, keep + j, sv, ed & 15u, (ed >> 4) & 15u);
+            if (keep + j == 0 || d < ncur)
+            {
+                ncur = d;
+                nci = keep + j;
+            }
         }
         nf = keep + ne;
+        cur = ncur;
+        ci = nci;
     }
     return EPA_NONE;
 }
