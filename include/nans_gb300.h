@@ -117,7 +117,7 @@ typedef struct nans_contact_pair
                                       NANS_ERR_EPA_CAPACITY; default: that pair gets no
                                       contact (the reference's result for every EPA that does
                                       not converge) and the event is counted */
-#define NANS_WORLD_TEST_GIANT_TIER 4u /* testing: every EPA beyond the warp tier's 128 faces
+#define NANS_WORLD_TEST_GIANT_TIER 4u /* testing: every EPA beyond the warp tier's 256 faces
                                       runs on the grid-wide tier (results are the same) */
 #define NANS_WORLD_WARM_START 8u   /* warm starting, the reference's TODO at its pair dedupe
                                       (code/nans.cpp:1386-1389): a pair (type, IndexA,

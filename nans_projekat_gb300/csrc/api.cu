@@ -677,7 +677,7 @@ int ensure_graph(nans_world *w, float dt, int gsteps)
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess)
         return fail(NANS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&w->gexec, graph, 0);
+    e = cudaGraphInstantiate(&w->gexec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess)
     {
@@ -812,7 +812,7 @@ int nans_world_create(const nans_world_desc *desc, nans_world **out)
     if (e == cudaSuccess)
         e = cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess)
-        e = cudaStreamCreateWithFlags(&w->stream2, cudaStreamNonBlocking);
+        e = cudaStreamCreateWithPriority(&w->stream2, cudaStreamNonBlocking, tier_priority());
     if (e == cudaSuccess)
         e = cudaEventCreateWithFlags(&w->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess)

@@ -1,4 +1,4 @@
-// Tiers 3 and 4 of the narrowphase: EPA on polytopes beyond the warp tier's 128 faces.
+// Tiers 3 and 4 of the narrowphase: EPA on polytopes beyond the warp tier's 256 faces.
 //
 // ResolveCollision (code/nans.cpp:787-904) with the polytope in global memory, run by a team
 // of threads: one block per EPA in tier 3 (arenas of 32,768 faces, two blocks per SM), the
@@ -733,9 +733,21 @@ int launch_narrow_big(cudaStream_t st, const DevWorld &w)
         cudaFuncSetAttribute(k_epa_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupTable));
         attrs = true;
     }
-    k_epa_block<<<w.blk_blocks, kLargeThreads, sizeof(GroupTable), st>>>(w);
+    cudaLaunchAttribute prio;
+    prio.id = cudaLaunchAttributePriority;
+    prio.val.priority = tier_priority();
+    cudaLaunchConfig_t bcfg = {};
+    bcfg.gridDim = dim3(w.blk_blocks);
+    bcfg.blockDim = dim3(kLargeThreads);
+    bcfg.dynamicSmemBytes = sizeof(GroupTable);
+    bcfg.stream = st;
+    bcfg.attrs = &prio;
+    bcfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&bcfg, k_epa_block, w);
+    if (e != cudaSuccess)
+        return (int)e;
     GiantScratch *S = reinterpret_cast<GiantScratch *>(w.giant_scratch);
-    cudaError_t e = cudaMemsetAsync(&S->bar, 0, sizeof(GridBarrier), st);
+    e = cudaMemsetAsync(&S->bar, 0, sizeof(GridBarrier), st);
     if (e != cudaSuccess)
         return (int)e;
     cudaLaunchConfig_t cfg = {};
@@ -743,11 +755,12 @@ int launch_narrow_big(cudaStream_t st, const DevWorld &w)
     cfg.blockDim = dim3(kLargeThreads);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
+    attr[1] = prio;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     e = cudaLaunchKernelEx(&cfg, k_epa_giant, w);
     return (int)e;
 }

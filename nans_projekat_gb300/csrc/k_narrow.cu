@@ -12,7 +12,8 @@
 //     the visible faces is a stable compaction, new faces are appended in edge order -- the
 //     same order vector::erase / push_back produce;
 //   * horizon edges are pushed in the order of the visible faces, each push cancelling the
-//     FIRST stored edge that is its reverse (vertex equality compares P, code/nans.h:251-254).
+//     FIRST stored edge that is its reverse (vertex equality compares P, code/nans.h:251-254);
+//     the warp tier decides every push's fate in parallel from its group of equal edges.
 // A face's "recomputed" normal in the closest-face search and the removal test equals its
 // stored normal bit for bit (same operands, same operations, the flip is an exact negation),
 // so each face's distance |dot(N, A)| is computed once when the face is created.
@@ -34,14 +35,19 @@ template <int FMAX, int EMAX> struct EpaBuf
 {
     static constexpr int kFaces = FMAX;
     static constexpr int kEdges = EMAX;
+    static constexpr int kPushes = 3 * FMAX;
     float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
     float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
     float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
+    unsigned char vid[kEpaMaxVerts]; // canonical vertex id (first vertex with an equal P), 0xff: NaN
     float fnx[FMAX], fny[FMAX], fnz[FMAX], fd[FMAX];
     unsigned char fa[FMAX], fb[FMAX], fc[FMAX];
     unsigned char ea[EMAX], eb[EMAX];
     unsigned vis[FMAX / 32];
+    unsigned pkey[kPushes];      // horizon push: group lo | hi << 8, orientation << 16, self-loop << 17
+    unsigned short puv[kPushes]; // horizon push: u | v << 8
 };
+constexpr unsigned kNanPush = 0xffffffffu; // a push with a NaN vertex: it equals no edge
 using EpaFast = EpaBuf<kEpaFastFaces, kEpaFastEdges>; // shared memory, one per warp
 
 
@@ -77,58 +83,69 @@ template <class B> __device__ __forceinline__ void face_put(B &E, int f, int a, 
     E.fd[f] = fabsf(dot3(n, pa));
 }
 
-// PushEdge (code/nans.cpp:232-266), warp-cooperative: cancels the first stored edge that is the
-// reverse of (u, v) (vertex equality compares P), else appends. Returns false on overflow.
-template <class B> __device__ __forceinline__ bool push_edge(B &E, int &ne, int u, int v, int lane)
+// Canonical id of pool vertex i (written by lane 0 before the call): the first vertex whose P
+// equals it, which is its own canonical id; 0xff when P has a NaN (it equals nothing).
+template <class B> __device__ __forceinline__ void pool_canon(B &E, int i, int lane)
 {
-    v3 pu = pool_p(E, u), pv = pool_p(E, v);
-    int found = -1;
-    for (int base = 0; base < ne; base += 32)
-    {
-        int e = base + lane;
-        bool m = false;
-        if (e < ne)
-            m = eq3(pool_p(E, E.ea[e]), pv) && eq3(pool_p(E, E.eb[e]), pu);
-        unsigned bal = __ballot_sync(0xffffffffu, m);
-        if (bal)
+    const v3 p = pool_p(E, i);
+    int id = i;
+    if (isnan(p.x) || isnan(p.y) || isnan(p.z))
+        id = 0xff;
+    else
+        for (int base = 0; base < i; base += 32)
         {
-            found = base + __ffs(bal) - 1;
-            break;
-        }
-    }
-    if (found >= 0)
-    {
-        // erase: shift the tail down by one, chunk by chunk (each chunk read before written)
-        for (int base = found + 1; base < ne; base += 32)
-        {
-            int e = base + lane;
-            unsigned char ta = 0, tb = 0;
-            if (e < ne)
+            const int j = base + lane;
+            const unsigned bal = __ballot_sync(0xffffffffu, j < i && eq3(pool_p(E, j), p));
+            if (bal)
             {
-                ta = E.ea[e];
-                tb = E.eb[e];
+                id = base + __ffs(bal) - 1;
+                break;
             }
-            __syncwarp();
-            if (e < ne)
-            {
-                E.ea[e - 1] = ta;
-                E.eb[e - 1] = tb;
-            }
-            __syncwarp();
         }
-        --ne;
-        return true;
-    }
-    if (ne >= B::kEdges)
-        return false;
     if (lane == 0)
-    {
-        E.ea[ne] = (unsigned char)u;
-        E.eb[ne] = (unsigned char)v;
-    }
+        E.vid[i] = (unsigned char)id;
     __syncwarp();
-    ++ne;
-    return true;
+}
+
+// Horizon push k = (u, v): its group is the unordered pair of canonical ids.
+template <class B> __device__ __forceinline__ void push_put(B &E, int k, int u, int v)
+{
+    const unsigned cu = E.vid[u], cv = E.vid[v];
+    unsigned key = kNanPush;
+    if (cu != 0xffu && cv != 0xffu)
+        key = min(cu, cv) | (max(cu, cv) << 8) | ((cu > cv ? 1u : 0u) << 16) | ((cu == cv ? 1u : 0u) << 17);
+    E.pkey[k] = key;
+    E.puv[k] = (unsigned short)(u | (v << 8));
+}
+
+// Whether push k of np is on the horizon after PushEdge (code/nans.cpp:232-266) has run over
+// all pushes in order. A push cancels the FIRST stored edge that is its reverse, so a group's
+// stored edges always run one way and leave in push order: the survivors are the last
+// (#majority - #minority) pushes of the majority orientation; in a self-loop group (P(u) ==
+// P(v): every push reverses every other) the last push survives iff the count is odd.
+template <class B> __device__ __forceinline__ bool push_survives(const B &E, int k, int np)
+{
+    const unsigned key = E.pkey[k];
+    if (key == kNanPush)
+        return true;
+    const unsigned g = key & 0xffffu, dir = (key >> 16) & 1u;
+    int same = 0, opp = 0, after = 0;
+    for (int j = 0; j < np; ++j)
+    {
+        const unsigned kj = E.pkey[j];
+        if ((kj & 0xffffu) != g || kj == kNanPush)
+            continue;
+        if (((kj >> 16) & 1u) == dir)
+        {
+            ++same;
+            after += j > k;
+        }
+        else
+            ++opp;
+    }
+    if ((key >> 17) & 1u)
+        return after == 0 && (same & 1);
+    return same > opp && after < same - opp;
 }
 
 // ResolveCollision (code/nans.cpp:787-904) on one warp. Returns EPA_CONTACT with the contact
@@ -145,6 +162,8 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         pool_put(E, 3, s3);
     }
     __syncwarp();
+    for (int i = 0; i < 4; ++i)
+        pool_canon(E, i, lane);
     // ABC, ACD, ADB, BDC (code/nans.cpp:799-802)
     if (lane == 0)
         face_put(E, 0, 0, 1, 2);
@@ -240,24 +259,47 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
                 E.vis[ch] = bal;
         }
         __syncwarp();
-        // horizon edges in face order
+        // horizon: the pushes (A,B), (B,C), (C,A) of the visible faces in face order, decided
+        // in parallel; the survivors keep push order
         int ne = 0;
         {
-            bool ok = true;
-            for (int ch = 0; ch < nchunks && ok; ++ch)
+            int nvis = 0;
+            for (int ch = 0; ch < nchunks; ++ch)
             {
-                unsigned m = E.vis[ch];
-                while (m && ok)
+                const unsigned m = E.vis[ch];
+                if ((m >> lane) & 1u)
                 {
-                    int f = ch * 32 + __ffs(m) - 1;
-                    m &= m - 1;
-                    int a = E.fa[f], b = E.fb[f], c = E.fc[f];
-                    ok = push_edge(E, ne, a, b, lane) && push_edge(E, ne, b, c, lane) &&
-                         push_edge(E, ne, c, a, lane);
+                    const int f = ch * 32 + lane;
+                    const int r = nvis + __popc(m & ((1u << lane) - 1u));
+                    const int a = E.fa[f], b = E.fb[f], c = E.fc[f];
+                    push_put(E, 3 * r, a, b);
+                    push_put(E, 3 * r + 1, b, c);
+                    push_put(E, 3 * r + 2, c, a);
                 }
+                nvis += __popc(m);
             }
-            if (!ok)
+            __syncwarp();
+            const int np = 3 * nvis;
+            for (int base = 0; base < np; base += 32)
+            {
+                const int k = base + lane;
+                const bool alive = k < np && push_survives(E, k, np);
+                const unsigned bal = __ballot_sync(0xffffffffu, alive);
+                if (alive)
+                {
+                    const int dst = ne + __popc(bal & ((1u << lane) - 1u));
+                    if (dst < B::kEdges)
+                    {
+                        const unsigned uv = E.puv[k];
+                        E.ea[dst] = (unsigned char)(uv & 0xffu);
+                        E.eb[dst] = (unsigned char)(uv >> 8);
+                    }
+                }
+                ne += __popc(bal);
+            }
+            if (ne > B::kEdges)
                 return EPA_OVERFLOW;
+            __syncwarp();
         }
         // stable removal of the visible faces
         int keep = 0;
@@ -320,6 +362,7 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
             pool_put(E, sv, ns);
         ++nv;
         __syncwarp();
+        pool_canon(E, sv, lane);
         for (int j = lane; j < ne; j += 32)
             face_put(E, keep + j, sv, E.ea[j], E.eb[j]);
         __syncwarp();
@@ -718,7 +761,7 @@ __global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
     }
 }
 
-// Tier 2: one warp per queued candidate, polytope of up to 128 faces in shared memory.
+// Tier 2: one warp per queued candidate, polytope of up to 256 faces in shared memory.
 // Dynamic shared memory: one EpaFast per warp.
 template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(DevWorld w)
 {
@@ -794,10 +837,35 @@ void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w)
     k_epa_tiny<<<epa_tiny_grid(), kTinyThreads, 0, st>>>(w);
 }
 
+int tier_priority()
+{
+    static int prio = 1;
+    if (prio > 0)
+    {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        prio = greatest;
+    }
+    return prio;
+}
+
+// The escalation tiers are latency-bound chains on the step's critical path; they are
+// launched at the greatest priority so that their blocks are placed before those of the
+// solve pass that becomes ready at the same time.
 void launch_epa_medium(cudaStream_t st, const DevWorld &w)
 {
     narrow_attrs();
-    k_epa_medium<4><<<w.medium_blocks, 128, medium_smem(4), st>>>(w);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(w.medium_blocks);
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = medium_smem(4);
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = tier_priority();
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_epa_medium<4>, w);
 }
 
 void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)

@@ -23,17 +23,18 @@ constexpr int kCullThreads = 256;
 // reference's polytope is not always convex: with bodies flung to large coordinates the
 // supports repeat existing vertices, faces degenerate (NaN normals, never removed) and the
 // list keeps growing, at times geometrically, for all 65 iterations. On the 16,384-scene
-// stack workload ~2 EPAs in a thousand outgrow 12 vertices / 20 faces, ~4 in a million exceed
-// 128 faces, and the largest met so far (scene 10198, step 135) reaches 485,688 faces and a
-// 139,111-edge horizon (the reference's own algorithm needs 334 s of one CPU core for it).
-// Tier 1 runs EPA per thread (12 vertices, 20 faces, 12 edges); tier 2 per warp in shared
-// memory (128 faces, 32 edges); tier 3 per block in a global-memory arena of 32,768 faces,
-// two blocks per SM; tier 4 on the whole grid (cooperative launch) in an arena of 8,388,608
-// faces and 4,194,304 horizon edges. Beyond that the pair gets no contact and the event is
-// counted (NANS_ERR_EPA_CAPACITY in strict worlds).
+// stack workload ~1.3 EPAs in a thousand outgrow 12 vertices / 20 faces, ~14 in a million
+// exceed 128 faces (nearly all of them stay within 256), and the largest met so far (scene
+// 10198, step 135) reaches 485,688 faces and a 139,111-edge horizon (the reference's own
+// algorithm needs 334 s of one CPU core for it). Tier 1 runs EPA per thread (12 vertices, 20
+// faces, 12 edges); tier 2 per warp in shared memory (256 faces, a 64-edge horizon); tier 3
+// per block in a global-memory arena of 32,768 faces, two blocks per SM; tier 4 on the whole
+// grid (cooperative launch) in an arena of 8,388,608 faces and 4,194,304 horizon edges.
+// Beyond that the pair gets no contact and the event is counted (NANS_ERR_EPA_CAPACITY in
+// strict worlds).
 constexpr int kEpaMaxVerts = 72;
-constexpr int kEpaFastFaces = 128;
-constexpr int kEpaFastEdges = 32;
+constexpr int kEpaFastFaces = 256;
+constexpr int kEpaFastEdges = 64;
 constexpr int kBlockFaces = 1 << 15;   // tier 3 arena (two blocks per SM)
 constexpr int kBlockEdges = 1 << 15;
 constexpr int kBlockPerSm = 2;
@@ -67,6 +68,7 @@ void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
 int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaError_t
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
+int tier_priority(); // the device's greatest stream priority
 int solve_threads(int max_scene_bodies);
 int render_scene(const DevWorld &w, int scene, const float eye[3], const float target[3], float fov_deg, int width,
                  int height, unsigned long long *fb, unsigned char *rgb, cudaStream_t st);

@@ -68,7 +68,7 @@ LARGE_EPA_CASES = [c for c in GOLDEN_CASES if "bigepa" in c or "emptied" in c]
 
 @pytest.mark.parametrize("case", LARGE_EPA_CASES)
 def test_grid_wide_epa_tier_reproduces_reference_golden(nl, case):
-    """The same reference fixtures with every EPA beyond the warp tier's 128 faces routed to the
+    """The same reference fixtures with every EPA beyond the warp tier's 256 faces routed to the
     grid-wide tier (cooperative launch) instead of the per-block tier."""
     scene, meta, digests, _ = load_golden(case)
     res = _run_plain_digests(nl, scene, meta["nsteps"], giant_tier_only=True)
