@@ -548,7 +548,7 @@ cudaError_t enqueue_narrow_solve(nans_world *w, float dt, cudaEvent_t *tl)
     e = (cudaError_t)launch_narrow_big(st2, w->dw);
     if (tl)
         cudaEventRecord(tl[2], st2);
-    launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
+    launch_solve(w->dw, w->n_scenes, solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
     if (tl)
         cudaEventRecord(tl[3], st);
     cudaError_t e2 = cudaEventRecord(w->ev_join, st2);
@@ -1433,7 +1433,7 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[4], st));
         CK((cudaError_t)launch_narrow_big(st, w->dw));
         CK(cudaEventRecord(ev[5], st));
-        launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
+        launch_solve(w->dw, w->n_scenes, solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
         launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 1);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());

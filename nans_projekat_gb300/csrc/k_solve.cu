@@ -210,8 +210,8 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
 
 // Dynamic shared memory: int last[max_scene_bodies] (wave of the last contact per body).
 // pass 0 solves every scene whose contacts are all known after the per-thread EPA tier
-// (largest first); pass 1 the scenes with a candidate in the later EPA tiers, so that pass 0
-// can run while those tiers do.
+// (largest first, a block per scene); pass 1 the scenes with a candidate in the later EPA
+// tiers (a persistent grid over the late list), so that pass 0 can run while those tiers do.
 template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve(DevWorld w, float dt, int pass)
 {
     extern __shared__ int s_last[];
@@ -219,13 +219,16 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
     __shared__ int s_scene, s_maxw;
     __shared__ int s_la[kWaveChunk], s_lb[kWaveChunk];
     const int tid = threadIdx.x;
-    for (;;)
+    for (int round = 0;; ++round)
     {
         if (tid == 0)
         {
             if (pass == 0)
             {
-                int q = atomicAdd(w.work_counter + 1, 1);
+                // one block per scene (the grid covers the scenes; blocks start in index order,
+                // so the largest scenes start first), so that blocks retire continuously and
+                // the escalation tiers' blocks, launched at a higher priority, find room early
+                const int q = blockIdx.x + round * gridDim.x;
                 s_scene = (q < w.n_scenes) ? w.sc_order[q] : -1;
                 if (s_scene >= 0 && w.scene_late[s_scene])
                     s_scene = -2;
