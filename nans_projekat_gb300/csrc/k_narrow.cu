@@ -46,6 +46,8 @@ template <int FMAX, int EMAX> struct EpaBuf
     unsigned vis[FMAX / 32];
     unsigned pkey[kPushes];      // horizon push: group lo | hi << 8, orientation << 16, self-loop << 17
     unsigned short puv[kPushes]; // horizon push: u | v << 8
+    static constexpr int kShapeCache = 64;
+    float sva[3 * kShapeCache], svb[3 * kShapeCache]; // the two shapes' world vertices
 };
 constexpr unsigned kNanPush = 0xffffffffu; // a push with a NaN vertex: it equals no edge
 using EpaFast = EpaBuf<kEpaFastFaces, kEpaFastEdges>; // shared memory, one per warp
@@ -81,6 +83,47 @@ template <class B> __device__ __forceinline__ void face_put(B &E, int f, int a, 
     E.fny[f] = n.y;
     E.fnz[f] = n.z;
     E.fd[f] = fabsf(dot3(n, pa));
+}
+
+// The support of one shape from its vertices cached in shared memory (hull_support's order
+// and comparisons: the same vertex, bit for bit).
+__device__ __forceinline__ v3 cached_hull_support(const float *v, int npts, v3 d)
+{
+    float best = -FLT_MAX;
+    v3 r = mk3(0.0f, 0.0f, 0.0f);
+    for (int t = 0; t < npts; ++t)
+    {
+        const v3 p = mk3(v[3 * t], v[3 * t + 1], v[3 * t + 2]);
+        const float dist = dot3(p, d);
+        if (dist > best)
+        {
+            best = dist;
+            r = p;
+        }
+    }
+    return r;
+}
+
+// minkowski_support with each hull of at most kShapeCache vertices read from the cache.
+template <class B>
+__device__ __forceinline__ GV cached_support(const DevWorld &w, const B &E, const Shape &A, const Shape &Bs, v3 d)
+{
+    GV r;
+    if (A.npts == 0)
+        r.sa = sphere_support(A.p, A.radius, d);
+    else if (A.npts <= B::kShapeCache)
+        r.sa = cached_hull_support(E.sva, A.npts, d);
+    else
+        r.sa = hull_support(w.verts, A.off, A.npts, d);
+    const v3 nd = -1.0f * d;
+    if (Bs.npts == 0)
+        r.sb = sphere_support(Bs.p, Bs.radius, nd);
+    else if (Bs.npts <= B::kShapeCache)
+        r.sb = cached_hull_support(E.svb, Bs.npts, nd);
+    else
+        r.sb = hull_support(w.verts, Bs.off, Bs.npts, nd);
+    r.p = r.sa - r.sb;
+    return r;
 }
 
 // Canonical id of pool vertex i (written by lane 0 before the call): the first vertex whose P
@@ -161,6 +204,12 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         pool_put(E, 2, s2);
         pool_put(E, 3, s3);
     }
+    if (A.npts > 0 && A.npts <= B::kShapeCache)
+        for (int i = lane; i < 3 * A.npts; i += 32)
+            E.sva[i] = w.verts[A.off + i];
+    if (Bs.npts > 0 && Bs.npts <= B::kShapeCache)
+        for (int i = lane; i < 3 * Bs.npts; i += 32)
+            E.svb[i] = w.verts[Bs.off + i];
     __syncwarp();
     for (int i = 0; i < 4; ++i)
         pool_canon(E, i, lane);
@@ -213,7 +262,7 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         }
         const float cur = E.fd[ci];
         const v3 n = mk3(E.fnx[ci], E.fny[ci], E.fnz[ci]);
-        const GV ns = minkowski_support(w.verts, A, Bs, n);
+        const GV ns = cached_support(w, E, A, Bs, n);
         if (dot3(n, ns.p) - cur < 0.001f)
         {
             // Barycentric (code/nans.cpp:771-785) of N*dist on the closest face

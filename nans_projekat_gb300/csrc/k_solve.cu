@@ -19,7 +19,7 @@ namespace nans
 {
 
 // One scene per block. The waves are latency-bound (a contact's 10-iteration loop per wave),
-// so worlds of small scenes use 64-thread blocks (many scenes share an SM) and worlds with a
+// so worlds of small scenes use 32-thread blocks (many scenes share an SM) and worlds with a
 // scene above 512 bodies 256-thread blocks (its waves hold more contacts).
 constexpr int kSolveThreadsMax = 256;
 constexpr int kWaveChunk = 512;
@@ -425,7 +425,7 @@ __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int 
         *count = n;
 }
 
-int solve_threads(int max_scene_bodies) { return max_scene_bodies > 512 ? kSolveThreadsMax : 64; }
+int solve_threads(int max_scene_bodies) { return max_scene_bodies > 512 ? kSolveThreadsMax : 32; }
 
 // Warm starting keeps its own instantiation so that the default solve keeps its registers.
 const void *solve_kernel(const DevWorld &w)
