@@ -126,6 +126,48 @@ __device__ __forceinline__ GV cached_support(const DevWorld &w, const B &E, cons
     return r;
 }
 
+// The same supports with the vertices spread over the warp when both shapes are cached hulls
+// of at most 16 vertices: lanes 0-15 evaluate A's vertices against d, lanes 16-31 B's against
+// -d, and each half reduces to the first maximum (larger distance, then lower index; NaN and
+// distances not above -FLT_MAX never win), which is the sequential scan's vertex.
+template <class B>
+__device__ __forceinline__ GV warp_support(const DevWorld &w, const B &E, const Shape &A, const Shape &Bs, v3 d,
+                                           int lane)
+{
+    if (A.npts == 0 || Bs.npts == 0 || A.npts > 16 || Bs.npts > 16)
+        return cached_support(w, E, A, Bs, d);
+    const int half = lane >> 4, t = lane & 15;
+    const float *v = half ? E.svb : E.sva;
+    const v3 dd = half ? -1.0f * d : d;
+    float best = -FLT_MAX;
+    int bi = -1;
+    if (t < (half ? Bs.npts : A.npts))
+    {
+        const float dist = dot3(mk3(v[3 * t], v[3 * t + 1], v[3 * t + 2]), dd);
+        if (dist > best)
+        {
+            best = dist;
+            bi = t;
+        }
+    }
+    for (int o = 8; o > 0; o >>= 1)
+    {
+        const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (oi >= 0 && (bi < 0 || ob > best || (ob == best && oi < bi)))
+        {
+            best = ob;
+            bi = oi;
+        }
+    }
+    const int ia = __shfl_sync(0xffffffffu, bi, 0), ib = __shfl_sync(0xffffffffu, bi, 16);
+    GV r;
+    r.sa = ia >= 0 ? mk3(E.sva[3 * ia], E.sva[3 * ia + 1], E.sva[3 * ia + 2]) : mk3(0.0f, 0.0f, 0.0f);
+    r.sb = ib >= 0 ? mk3(E.svb[3 * ib], E.svb[3 * ib + 1], E.svb[3 * ib + 2]) : mk3(0.0f, 0.0f, 0.0f);
+    r.p = r.sa - r.sb;
+    return r;
+}
+
 // Canonical id of pool vertex i (written by lane 0 before the call): the first vertex whose P
 // equals it, which is its own canonical id; 0xff when P has a NaN (it equals nothing).
 template <class B> __device__ __forceinline__ void pool_canon(B &E, int i, int lane)
@@ -262,7 +304,7 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         }
         const float cur = E.fd[ci];
         const v3 n = mk3(E.fnx[ci], E.fny[ci], E.fnz[ci]);
-        const GV ns = cached_support(w, E, A, Bs, n);
+        const GV ns = warp_support(w, E, A, Bs, n, lane);
         if (dot3(n, ns.p) - cur < 0.001f)
         {
             // Barycentric (code/nans.cpp:771-785) of N*dist on the closest face
@@ -810,8 +852,9 @@ __global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
     }
 }
 
-// Tier 2: one warp per queued candidate, polytope of up to 256 faces in shared memory.
-// Dynamic shared memory: one EpaFast per warp.
+// Tier 2: one warp per queued candidate, polytope of up to 256 faces in shared memory, from
+// the GJK simplex the GJK pass stored with the candidate. Dynamic shared memory: one EpaFast
+// per warp.
 template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(DevWorld w)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -829,10 +872,16 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(
             break;
         const int cc = w.med_cand[q];
         const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
-        GV s0, s1, s2, s3;
-        gjk(w.verts, A, B, s0, s1, s2, s3); // every lane: same inputs, same simplex
+        const float *sq = reinterpret_cast<const float *>(w.s_k + 9 * (size_t)cc);
+        GV g[4];
+        for (int i = 0; i < 4; ++i)
+        {
+            g[i].p = mk3(sq[9 * i], sq[9 * i + 1], sq[9 * i + 2]);
+            g[i].sa = mk3(sq[9 * i + 3], sq[9 * i + 4], sq[9 * i + 5]);
+            g[i].sb = mk3(sq[9 * i + 6], sq[9 * i + 7], sq[9 * i + 8]);
+        }
         v3 pa, pb, nn;
-        int r = epa_run(w, E, A, B, s0, s1, s2, s3, pa, pb, nn, lane);
+        int r = epa_run(w, E, A, B, g[0], g[1], g[2], g[3], pa, pb, nn, lane);
         __syncwarp();
         if (lane == 0)
         {
