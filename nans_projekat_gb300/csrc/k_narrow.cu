@@ -770,17 +770,19 @@ __device__ __forceinline__ void enqueue_epa(const DevWorld &w, int c, bool hit)
     w.s_order[base + __popc(bal & ((1u << lane) - 1u))] = c;
 }
 
-// GJK of candidate c; with a budget below 65, a GJK still evolving is queued for the long pass.
-__device__ __forceinline__ void gjk_one(const DevWorld &w, int c, int budget)
+// GJK of candidate c from call `it` with the simplex (s0..s3, n points). With a budget below
+// 65, a GJK still evolving is queued for the long pass with its state (the simplex in the
+// candidate's s_k slot, n and it in the queue), which resumes it.
+__device__ __forceinline__ void gjk_one(const DevWorld &w, int c, int budget, GV &s0, GV &s1, GV &s2, GV &s3, int n,
+                                        int it)
 {
     const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
-    GV s0, s1, s2, s3;
-    const int g = gjk(w.verts, A, B, s0, s1, s2, s3, budget);
-    if (g == G_FOUND)
+    const int g = gjk_from(w.verts, A, B, s0, s1, s2, s3, n, it, budget);
+    if (g == G_FOUND || g == G_BUDGET)
         store_simplex(w, c, s0, s1, s2, s3);
-    else if (g == G_BUDGET)
-        w.long_cand[atomicAdd(w.work_counter + 7, 1)] = c;
-    else
+    if (g == G_BUDGET)
+        w.long_cand[atomicAdd(w.work_counter + 7, 1)] = make_int2(c, n | (it << 8));
+    else if (g != G_FOUND)
         w.hit[c] = 0;
     enqueue_epa(w, c, g == G_FOUND);
 }
@@ -811,16 +813,36 @@ __global__ void __launch_bounds__(kGjkThreads, 6) k_gjk(DevWorld w)
             w.cand_begin[sc] = c;
         if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
             w.cand_end[sc] = c + 1;
-        gjk_one(w, c, kGjkShort);
+        GV s0 = {}, s1 = {}, s2 = {}, s3 = {};
+        gjk_one(w, c, kGjkShort, s0, s1, s2, s3, 0, 0);
     }
 }
 
-// The long pass: candidates whose GJK needed more than kGjkShort calls, rerun in full.
+// The long pass: candidates whose GJK needed more than kGjkShort calls, resumed where the
+// first pass stopped.
 __global__ void __launch_bounds__(kGjkThreads, 6) k_gjk_long(DevWorld w)
 {
     const int n = w.work_counter[7];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        gjk_one(w, w.long_cand[i], 65);
+    {
+        const int2 q = w.long_cand[i];
+        const float4 *o = w.s_k + 9 * (size_t)q.x;
+        const float4 k0 = o[0], k1 = o[1], k2 = o[2], k3 = o[3], k4 = o[4], k5 = o[5], k6 = o[6], k7 = o[7], k8 = o[8];
+        GV s0, s1, s2, s3;
+        s0.p = mk3(k0.x, k0.y, k0.z);
+        s0.sa = mk3(k0.w, k1.x, k1.y);
+        s0.sb = mk3(k1.z, k1.w, k2.x);
+        s1.p = mk3(k2.y, k2.z, k2.w);
+        s1.sa = mk3(k3.x, k3.y, k3.z);
+        s1.sb = mk3(k3.w, k4.x, k4.y);
+        s2.p = mk3(k4.z, k4.w, k5.x);
+        s2.sa = mk3(k5.y, k5.z, k5.w);
+        s2.sb = mk3(k6.x, k6.y, k6.z);
+        s3.p = mk3(k6.w, k7.x, k7.y);
+        s3.sa = mk3(k7.z, k7.w, k8.x);
+        s3.sb = mk3(k8.y, k8.z, k8.w);
+        gjk_one(w, q.x, 65, s0, s1, s2, s3, q.y & 0xff, q.y >> 8);
+    }
 }
 
 // Tier 1 EPA: one thread per hit from the queue; EPAs that outgrow the per-thread polytope

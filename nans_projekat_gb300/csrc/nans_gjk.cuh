@@ -16,16 +16,15 @@ enum
 // TripleCross (code/nans.cpp:564-569): (A x B) x C = B * dot(C, A) - A * dot(C, B)
 __device__ __forceinline__ v3 triple_cross(v3 a, v3 b, v3 c) { return (dot3(c, a) * b) - (dot3(c, b) * a); }
 
-// CheckCollision's GJK loop (at most 65 EvolveSimplex calls). With budget < 65 it stops after
-// `budget` calls and returns G_BUDGET if the simplex is still evolving; rerunning with the
-// full budget reproduces the same sequence from the start.
-__device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,
-                                   GV &s3, int budget = 65)
+// CheckCollision's GJK loop (at most 65 EvolveSimplex calls) from call `it` with the simplex
+// (s0..s3, n points). With budget < 65 it stops before call `budget` and returns G_BUDGET if
+// the simplex is still evolving; (simplex, n, it) then resume it exactly.
+__device__ __forceinline__ int gjk_from(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,
+                                        GV &s3, int &n, int &it, int budget)
 {
     const v3 dir0 = normalize3(B.p - A.p);
-    int n = 0;
     int res = G_EVOLVING;
-    for (int it = 0; it <= 64; ++it)
+    for (; it <= 64; ++it)
     {
         if (it >= budget)
             return G_BUDGET;
@@ -160,6 +159,13 @@ __device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Sha
             return res;
     }
     return G_NOHIT; // iteration cap reached while still evolving: no collision
+}
+
+__device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,
+                                   GV &s3, int budget = 65)
+{
+    int n = 0, it = 0;
+    return gjk_from(verts, A, B, s0, s1, s2, s3, n, it, budget);
 }
 
 enum

@@ -95,7 +95,7 @@ struct DevWorld
                                         // [13] late-scene count
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
-    int *long_cand;                     // candidates whose GJK needs the long pass
+    int2 *long_cand;                    // candidates whose GJK needs the long pass: (c, n | it << 8)
     int medium_blocks;                  // warp-tier grid
     int ovf_cap;                        // block-EPA queue capacity
     int *ovf_cand;                      // candidates queued for the block tier
