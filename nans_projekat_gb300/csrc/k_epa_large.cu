@@ -359,6 +359,8 @@ __device__ int epa_large(const DevWorld &w, const T &team, A &E, GroupTable &G, 
         int vis_before = 0, nvis = 0;
         if (!team_prefix(team, team.c1, wvis, vis_before, nvis))
             return EPA_ABORT;
+        if (nvis == 0)
+            return EPA_NONE; // nothing changes: every later iteration repeats this one
         const int m = 3 * nvis;
         // pushes of the visible faces (edges AB, BC, CA at 3*rank), the other faces to the
         // other bank in order

@@ -335,6 +335,7 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
             return EPA_NONE; // the stale read repeats identically until the iteration cap
         // faces that see the new support point (code/nans.cpp:869-891)
         const int nchunks = (nf + 31) >> 5;
+        int nseen = 0;
         for (int ch = 0; ch < nchunks; ++ch)
         {
             int f = ch * 32 + lane;
@@ -348,8 +349,11 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
             unsigned bal = __ballot_sync(0xffffffffu, vis);
             if (lane == 0)
                 E.vis[ch] = bal;
+            nseen += __popc(bal);
         }
         __syncwarp();
+        if (nseen == 0)
+            return EPA_NONE; // nothing changes: every later iteration repeats this one
         // horizon: the pushes (A,B), (B,C), (C,A) of the visible faces in face order, decided
         // in parallel; the survivors keep push order
         int ne = 0;
@@ -700,6 +704,8 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
                 ++keep;
             }
         }
+        if (keep == nf)
+            return EPA_NONE; // no face sees the support: every later iteration repeats this one
         if (keep + ne > kTinyF || nv >= kTinyV)
             return EPA_OVERFLOW;
         if (keep == 0 && ne == 0)
