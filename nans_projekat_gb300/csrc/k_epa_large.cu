@@ -251,14 +251,24 @@ template <class T> __device__ __forceinline__ bool team_prefix(const T &team, in
     return true;
 }
 
+// Resumable EPA state at the start of an iteration: (unused, it | bank << 8 | stale << 9,
+// face count, vertex count); the faces are those of the bank, the vertices the pool's first.
+__device__ __forceinline__ int4 epa_state(int it, int cb, bool stale, int nf, int nv)
+{
+    return make_int4(0, it | (cb << 8) | ((stale ? 1 : 0) << 9), nf, nv);
+}
+
+// ResolveCollision on a team's polytope, from the GJK simplex, or (resume != null) from an
+// iteration's starting state already in the arena. On EPA_OVERFLOW, *ovf (rank 0 writes it)
+// holds the state at the start of the iteration that overflowed, which the next tier resumes.
 template <class T, class A>
 __device__ int epa_large(const DevWorld &w, const T &team, A &E, GroupTable &G, int face_limit, const Shape &SA,
                          const Shape &SB, const GV &s0, const GV &s1, const GV &s2, const GV &s3, v3 &out_pa,
-                         v3 &out_pb, v3 &out_n)
+                         v3 &out_pb, v3 &out_n, const int4 *resume = nullptr, int4 *ovf = nullptr)
 {
     const int r = team.rank(), nt = team.size(), lane = threadIdx.x & 31, gw = team.warp(), W = team.warps();
     const unsigned full = 0xffffffffu;
-    if (r == 0)
+    if (r == 0 && !resume)
     {
         lpool_put(E, 0, s0);
         lpool_put(E, 1, s1);
@@ -275,19 +285,30 @@ __device__ int epa_large(const DevWorld &w, const T &team, A &E, GroupTable &G, 
     }
     if (!team.sync())
         return EPA_ABORT;
-    if (r == 0)
-        lface_put(E, 0, 0, 0, 1, 2);
-    else if (r == 1)
-        lface_put(E, 0, 1, 0, 2, 3);
-    else if (r == 2)
-        lface_put(E, 0, 2, 0, 3, 1);
-    else if (r == 3)
-        lface_put(E, 0, 3, 1, 3, 2);
-    if (!team.sync())
-        return EPA_ABORT;
-    int nf = 4, nv = 4, cb = 0;
+    int nf = 4, nv = 4, cb = 0, it0 = 0;
     bool stale = false;
-    for (int it = 0; it <= 64; ++it)
+    if (resume)
+    {
+        it0 = resume->y & 0xff;
+        cb = (resume->y >> 8) & 1;
+        stale = ((resume->y >> 9) & 1) != 0;
+        nf = resume->z;
+        nv = resume->w;
+    }
+    else
+    {
+        if (r == 0)
+            lface_put(E, 0, 0, 0, 1, 2);
+        else if (r == 1)
+            lface_put(E, 0, 1, 0, 2, 3);
+        else if (r == 2)
+            lface_put(E, 0, 2, 0, 3, 1);
+        else if (r == 3)
+            lface_put(E, 0, 3, 1, 3, 2);
+        if (!team.sync())
+            return EPA_ABORT;
+    }
+    for (int it = it0; it <= 64; ++it)
     {
         if (nf == 0 && !stale)
             return EPA_NONE;
@@ -558,7 +579,11 @@ __device__ int epa_large(const DevWorld &w, const T &team, A &E, GroupTable &G, 
         if (!team_prefix(team, team.c2, wal, al_before, ne))
             return EPA_ABORT;
         if (ne > A::kEdges)
+        {
+            if (ovf && r == 0)
+                *ovf = epa_state(it, cb, stale, nf, nv);
             return EPA_OVERFLOW;
+        }
         {
             int er = al_before;
             const unsigned below = (1u << lane) - 1u;
@@ -578,7 +603,11 @@ __device__ int epa_large(const DevWorld &w, const T &team, A &E, GroupTable &G, 
             atomicMax(w.epa_stats + 1, (unsigned)ne);
         }
         if (keep + ne > face_limit)
+        {
+            if (ovf && r == 0)
+                *ovf = epa_state(it, cb, stale, nf, nv);
             return EPA_OVERFLOW;
+        }
         const int sv = nv++;
         if (r == 0)
         {
@@ -622,13 +651,15 @@ __device__ __forceinline__ void epa_beyond_capacity(const DevWorld &w, int cc)
 }
 
 // Tier 3: one block per queued candidate. An EPA that outgrows the block arena is queued for
-// tier 4. Dynamic shared memory: the group table.
+// tier 4 with the state of its last iteration, which stays in this block's arena (the block
+// takes no further candidate) for tier 4 to resume. Dynamic shared memory: the group table.
 __global__ void __launch_bounds__(kLargeThreads) k_epa_block(DevWorld w)
 {
     extern __shared__ unsigned char s_dyn[];
     GroupTable &G = *reinterpret_cast<GroupTable *>(s_dyn);
     __shared__ float s_af[32];
-    __shared__ int s_ai[32], s_c1[32], s_c2[32], s_flag, s_q;
+    __shared__ int s_ai[32], s_c1[32], s_c2[32], s_flag, s_q, s_stop;
+    __shared__ int4 s_ovf;
     const BlockTeam team{s_af, s_ai, s_c1, s_c2, &s_flag};
     BlockArena &E = *reinterpret_cast<BlockArena *>(w.blk_arena + (size_t)blockIdx.x * sizeof(BlockArena));
     const int n = min(w.work_counter[3], w.ovf_cap);
@@ -647,10 +678,11 @@ __global__ void __launch_bounds__(kLargeThreads) k_epa_block(DevWorld w)
         gjk(w.verts, A, B, s0, s1, s2, s3); // every thread: same inputs, same simplex
         v3 pa, pb, nn;
         int r = epa_large(w, team, E, G, min(w.blk_face_limit, BlockArena::kFaces), A, B, s0, s1, s2, s3, pa, pb,
-                          nn);
+                          nn, nullptr, &s_ovf);
         __syncthreads();
         if (threadIdx.x == 0)
         {
+            s_stop = 0;
             atomicAdd(w.epa_stats + 2, 1u);
             bool done = true;
             if (r == EPA_OVERFLOW)
@@ -658,10 +690,11 @@ __global__ void __launch_bounds__(kLargeThreads) k_epa_block(DevWorld w)
                 int g = atomicAdd(w.work_counter + 8, 1);
                 if (g < w.giant_cap)
                 {
-                    w.giant_cand[g] = cc;
+                    w.giant_cand[g] = make_int4(cc, s_ovf.y | ((int)blockIdx.x << 10), s_ovf.z, s_ovf.w);
                     atomicAdd(w.epa_stats + 7, 1u);
                     w.hit[cc] = 0;
                     done = false;
+                    s_stop = 1;
                 }
                 else
                 {
@@ -673,6 +706,8 @@ __global__ void __launch_bounds__(kLargeThreads) k_epa_block(DevWorld w)
                 write_result(w, cc, r, pa, pb, nn);
         }
         __syncthreads();
+        if (s_stop)
+            break;
     }
 }
 
@@ -685,12 +720,38 @@ __global__ void __launch_bounds__(kLargeThreads) k_epa_giant(DevWorld w)
     const int n = min(w.work_counter[8], w.giant_cap);
     for (int q = 0; q < n; ++q)
     {
-        const int cc = w.giant_cand[q];
+        const int4 gq = w.giant_cand[q];
+        const int cc = gq.x;
         const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
-        GV s0, s1, s2, s3;
-        gjk(w.verts, A, B, s0, s1, s2, s3);
+        // the block tier's polytope at the start of the iteration that outgrew it
+        const BlockArena &src =
+            *reinterpret_cast<const BlockArena *>(w.blk_arena + (size_t)(gq.y >> 10) * sizeof(BlockArena));
+        const int cb = (gq.y >> 8) & 1, nf = gq.z, nv = gq.w;
+        for (int i = team.rank(); i < nv; i += team.size())
+        {
+            E.px[i] = src.px[i];
+            E.py[i] = src.py[i];
+            E.pz[i] = src.pz[i];
+            E.ax[i] = src.ax[i];
+            E.ay[i] = src.ay[i];
+            E.az[i] = src.az[i];
+            E.bx[i] = src.bx[i];
+            E.by[i] = src.by[i];
+            E.bz[i] = src.bz[i];
+            E.vid[i] = src.vid[i];
+        }
+        for (int f = team.rank(); f < nf; f += team.size())
+        {
+            E.fidx[cb][f] = src.fidx[cb][f];
+            E.fnx[cb][f] = src.fnx[cb][f];
+            E.fny[cb][f] = src.fny[cb][f];
+            E.fnz[cb][f] = src.fnz[cb][f];
+            E.fd[cb][f] = src.fd[cb][f];
+        }
+        const int4 resume = make_int4(0, gq.y & 0x3ff, nf, nv);
+        GV s0 = {}, s1 = {}, s2 = {}, s3 = {};
         v3 pa, pb, nn;
-        int r = epa_large(w, team, E, S.table, GiantArena::kFaces, A, B, s0, s1, s2, s3, pa, pb, nn);
+        int r = epa_large(w, team, E, S.table, GiantArena::kFaces, A, B, s0, s1, s2, s3, pa, pb, nn, &resume);
         if (r == EPA_ABORT)
         {
             if (team.rank() == 0)

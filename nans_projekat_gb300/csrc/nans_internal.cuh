@@ -103,7 +103,8 @@ struct DevWorld
     int blk_blocks;                     // block-tier grid
     int blk_face_limit;                 // block-tier face capacity (lowered only by a test flag)
     int giant_cap;                      // giant-EPA queue capacity
-    int *giant_cand;                    // candidates queued for the giant tier
+    int4 *giant_cand;                   // queued for the giant tier: candidate, state (it | bank << 8 |
+                                        // stale << 9 | block << 10), faces, vertices
     unsigned char *epa_arena;           // giant-tier polytope buffers (one, grid-wide)
     unsigned char *giant_scratch;       // giant-tier group table, team scratch and barrier
     int giant_blocks;                   // giant-tier grid (cooperative launch)
