@@ -418,7 +418,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.epa_arena, epa_big_bytes())) ||
         (rc = dalloc(w, L, &d.giant_scratch, epa_giant_scratch_bytes())) ||
         (rc = dalloc(w, L, &d.blk_arena, epa_block_bytes() * (size_t)(kBlockPerSm * w->sm_count))) ||
-        (rc = dalloc(w, L, &d.giant_cand, kGiantQueueCap)) ||
+        (rc = dalloc(w, L, &d.giant_cand, kGiantQueueCap)) || (rc = dalloc(w, L, &d.handover, kHandoverSlots)) ||
         (rc = dalloc(w, L, &d.epa_stats, 8)) ||
         (rc = dalloc(w, L, &w->d_rec_cube, (size_t)61 * tc)) || (rc = dalloc(w, L, &w->d_rec_sphere, (size_t)37 * ts)) ||
         (rc = dalloc(w, L, &w->d_rec_floor, (size_t)61 * S)) || (rc = dalloc(w, L, &w->d_small, 2)) ||

@@ -674,11 +674,41 @@ __global__ void __launch_bounds__(kLargeThreads) k_epa_block(DevWorld w)
             break;
         const int cc = w.ovf_cand[q];
         const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
-        GV s0, s1, s2, s3;
-        gjk(w.verts, A, B, s0, s1, s2, s3); // every thread: same inputs, same simplex
+        GV s0 = {}, s1 = {}, s2 = {}, s3 = {};
+        int4 resume = make_int4(0, 0, -1, 0);
+        if (q < kHandoverSlots && w.handover[q].hdr[2] >= 0)
+        {
+            // the warp tier's polytope at the start of the iteration that outgrew it (bank 0)
+            const EpaHandover &H = w.handover[q];
+            const int nf = H.hdr[2], nv = H.hdr[3];
+            for (int i = threadIdx.x; i < nv; i += blockDim.x)
+            {
+                E.px[i] = H.px[i];
+                E.py[i] = H.py[i];
+                E.pz[i] = H.pz[i];
+                E.ax[i] = H.ax[i];
+                E.ay[i] = H.ay[i];
+                E.az[i] = H.az[i];
+                E.bx[i] = H.bx[i];
+                E.by[i] = H.by[i];
+                E.bz[i] = H.bz[i];
+                E.vid[i] = H.vid[i];
+            }
+            for (int f = threadIdx.x; f < nf; f += blockDim.x)
+            {
+                E.fidx[0][f] = H.fidx[f];
+                E.fnx[0][f] = H.fnx[f];
+                E.fny[0][f] = H.fny[f];
+                E.fnz[0][f] = H.fnz[f];
+                E.fd[0][f] = H.fd[f];
+            }
+            resume = epa_state(H.hdr[0], 0, H.hdr[1] != 0, nf, nv);
+        }
+        else
+            gjk(w.verts, A, B, s0, s1, s2, s3); // every thread: same inputs, same simplex
         v3 pa, pb, nn;
         int r = epa_large(w, team, E, G, min(w.blk_face_limit, BlockArena::kFaces), A, B, s0, s1, s2, s3, pa, pb,
-                          nn, nullptr, &s_ovf);
+                          nn, resume.z >= 0 ? &resume : nullptr, &s_ovf);
         __syncthreads();
         if (threadIdx.x == 0)
         {

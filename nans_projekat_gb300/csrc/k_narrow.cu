@@ -234,10 +234,11 @@ template <class B> __device__ __forceinline__ bool push_survives(const B &E, int
 }
 
 // ResolveCollision (code/nans.cpp:787-904) on one warp. Returns EPA_CONTACT with the contact
-// written, EPA_NONE, or EPA_OVERFLOW when the polytope outgrows B.
+// written, EPA_NONE, or EPA_OVERFLOW when the polytope outgrows B; then ovf = (iteration,
+// stale, faces, vertices) describes the polytope at the start of that iteration, still in E.
 template <class B>
 __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs, const GV &s0, const GV &s1,
-                       const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n, int lane)
+                       const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n, int lane, int4 &ovf)
 {
     if (lane == 0)
     {
@@ -392,8 +393,11 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
                 }
                 ne += __popc(bal);
             }
-            if (ne > B::kEdges)
+            if (ne > B::kEdges || nf - nseen + ne > B::kFaces)
+            {
+                ovf = make_int4(it, stale ? 1 : 0, nf, nv);
                 return EPA_OVERFLOW;
+            }
             __syncwarp();
         }
         // stable removal of the visible faces
@@ -431,8 +435,6 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
             __syncwarp();
             keep += __popc(sm);
         }
-        if (keep + ne > B::kFaces)
-            return EPA_OVERFLOW;
         if (keep == 0 && ne == 0)
         {
             // every face removed: slot 0 keeps the last face of the list (still intact, the
@@ -470,7 +472,8 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
 // Queues a candidate whose EPA outgrew the current tier: the warp tier (capacity med_cap),
 // then the large-polytope tier (capacity ovf_cap). The next tier reruns GJK (deterministic,
 // so it sees the same simplex) and EPA from scratch.
-__device__ __forceinline__ void escalate(const DevWorld &w, int c, bool to_big)
+// Returns the tier-3 queue index (the caller may leave its state in handover[q]), or -1.
+__device__ __forceinline__ int escalate(const DevWorld &w, int c, bool to_big)
 {
     w.hit[c] = 0;
     const int sc = w.cand_meta[c] >> 3;
@@ -483,14 +486,56 @@ __device__ __forceinline__ void escalate(const DevWorld &w, int c, bool to_big)
         if (q < w.med_cap)
         {
             w.med_cand[q] = c;
-            return;
+            return -1;
         }
     }
     int q = atomicAdd(w.work_counter + 3, 1);
     if (q < w.ovf_cap)
+    {
         w.ovf_cand[q] = c;
-    else
-        atomicOr(w.status, (unsigned)ST_EPA_FACES);
+        if (q < kHandoverSlots)
+            w.handover[q].hdr[2] = -1; // no state unless the warp tier leaves one
+        return q;
+    }
+    atomicOr(w.status, (unsigned)ST_EPA_FACES);
+    return -1;
+}
+
+// The warp tier's polytope (state ovf) into handover slot q, for the block tier to resume.
+__device__ __forceinline__ void handover_put(const DevWorld &w, const EpaFast &E, int q, int4 ovf, int lane)
+{
+    EpaHandover &H = w.handover[q];
+    const int nf = ovf.z, nv = ovf.w;
+    for (int i = lane; i < nv; i += 32)
+    {
+        H.px[i] = E.px[i];
+        H.py[i] = E.py[i];
+        H.pz[i] = E.pz[i];
+        H.ax[i] = E.ax[i];
+        H.ay[i] = E.ay[i];
+        H.az[i] = E.az[i];
+        H.bx[i] = E.bx[i];
+        H.by[i] = E.by[i];
+        H.bz[i] = E.bz[i];
+        H.vid[i] = E.vid[i] == 0xffu ? -1 : (int)E.vid[i];
+    }
+    for (int f = lane; f < nf; f += 32)
+    {
+        H.fidx[f] = (unsigned)E.fa[f] | ((unsigned)E.fb[f] << 8) | ((unsigned)E.fc[f] << 16);
+        H.fnx[f] = E.fnx[f];
+        H.fny[f] = E.fny[f];
+        H.fnz[f] = E.fnz[f];
+        H.fd[f] = E.fd[f];
+    }
+    __syncwarp();
+    if (lane == 0)
+    {
+        H.hdr[0] = ovf.x;
+        H.hdr[1] = ovf.y;
+        H.hdr[3] = nv;
+        __threadfence();
+        H.hdr[2] = nf;
+    }
 }
 
 // ------------------------------------------------------------------------------------
@@ -909,15 +954,21 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(
             g[i].sb = mk3(sq[9 * i + 6], sq[9 * i + 7], sq[9 * i + 8]);
         }
         v3 pa, pb, nn;
-        int r = epa_run(w, E, A, B, g[0], g[1], g[2], g[3], pa, pb, nn, lane);
+        int4 ovf;
+        int r = epa_run(w, E, A, B, g[0], g[1], g[2], g[3], pa, pb, nn, lane, ovf);
         __syncwarp();
+        int qo = -1;
         if (lane == 0)
         {
             if (r == EPA_OVERFLOW)
-                escalate(w, cc, true);
+                qo = escalate(w, cc, true);
             else
                 write_result(w, cc, r, pa, pb, nn);
         }
+        qo = __shfl_sync(0xffffffffu, qo, 0);
+        if (qo >= 0 && qo < kHandoverSlots)
+            handover_put(w, E, qo, ovf, lane);
+        __syncwarp();
     }
 }
 

@@ -46,6 +46,8 @@ enum StatusBits
     ST_EPA_TIMEOUT = 1u << 5,    // a giant-tier grid barrier timed out (pair: no contact)
 };
 
+struct EpaHandover; // nans_kernels.cuh
+
 struct DevWorld
 {
     int n_scenes;
@@ -103,6 +105,7 @@ struct DevWorld
     int blk_blocks;                     // block-tier grid
     int blk_face_limit;                 // block-tier face capacity (lowered only by a test flag)
     int giant_cap;                      // giant-EPA queue capacity
+    EpaHandover *handover;              // warp-tier states for the block tier (kHandoverSlots)
     int4 *giant_cand;                   // queued for the giant tier: candidate, state (it | bank << 8 |
                                         // stale << 9 | block << 10), faces, vertices
     unsigned char *epa_arena;           // giant-tier polytope buffers (one, grid-wide)

@@ -41,6 +41,21 @@ constexpr int kBlockPerSm = 2;
 constexpr int kGiantFaces = 1 << 23;   // tier 4 arena (one, the whole grid per EPA)
 constexpr int kGiantEdges = 1 << 22;
 constexpr int kEpaOverflowCap = 65536; // tier-3 EPAs queued per step
+constexpr int kHandoverSlots = 1024;   // tier-3 queue entries that can carry the warp tier's state
+
+// The warp tier's polytope at the start of the iteration that outgrew it, for the block tier to
+// resume (queue entry q < kHandoverSlots of the tier-3 queue): hdr = (iteration, stale, face
+// count or -1 when there is no state, vertex count).
+struct EpaHandover
+{
+    int hdr[4];
+    float px[kEpaMaxVerts], py[kEpaMaxVerts], pz[kEpaMaxVerts];
+    float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
+    float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
+    int vid[kEpaMaxVerts];
+    unsigned fidx[kEpaFastFaces];
+    float fnx[kEpaFastFaces], fny[kEpaFastFaces], fnz[kEpaFastFaces], fd[kEpaFastFaces];
+};
 constexpr int kGiantQueueCap = 4096;   // tier-4 EPAs queued per step
 constexpr int kWorkCounters = 16;
 constexpr int kEpaMediumCap = 1 << 20; // tier-2 EPAs queued per step
