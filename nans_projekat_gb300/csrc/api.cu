@@ -161,16 +161,6 @@ int narrow_grid(nans_world *w)
 
 size_t solve_smem(const nans_world *w) { return (size_t)std::max(1, w->max_scene_bodies) * sizeof(int); }
 
-int solve_grid(nans_world *w)
-{
-    int per = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, solve_kernel(w->dw), solve_threads(w->max_scene_bodies), solve_smem(w));
-    if (per < 1)
-        per = 1;
-    if (w->solve_bpsm > 0)
-        per = std::min(per, w->solve_bpsm);
-    return std::max(1, std::min(w->n_scenes, per * w->sm_count));
-}
 
 int alloc_candidates(nans_world *w, int cap)
 {
@@ -554,7 +544,9 @@ cudaError_t enqueue_narrow_solve(nans_world *w, float dt, cudaEvent_t *tl)
     cudaError_t e2 = cudaEventRecord(w->ev_join, st2);
     if (e2 == cudaSuccess)
         e2 = cudaStreamWaitEvent(st, w->ev_join, 0);
-    launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 1);
+    // the late scenes (few, and mostly the larger ones) solve with wider blocks: their waves
+    // are on the step's critical path
+    launch_solve(w->dw, std::min(w->n_scenes, 2 * w->sm_count), kSolveLateThreads, solve_smem(w), st, dt, 1);
     if (tl)
         cudaEventRecord(tl[4], st);
     return e != cudaSuccess ? e : e2;
@@ -1434,7 +1426,7 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK((cudaError_t)launch_narrow_big(st, w->dw));
         CK(cudaEventRecord(ev[5], st));
         launch_solve(w->dw, w->n_scenes, solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
-        launch_solve(w->dw, solve_grid(w), solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 1);
+        launch_solve(w->dw, std::min(w->n_scenes, 2 * w->sm_count), kSolveLateThreads, solve_smem(w), st, dt, 1);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());
         after_step(w, dt);

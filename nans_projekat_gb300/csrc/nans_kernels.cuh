@@ -17,6 +17,7 @@ enum SweepFlags
 };
 
 constexpr int kCullThreads = 256;
+constexpr int kSolveLateThreads = 128; // solver blocks of the second pass (late scenes)
 
 // EPA capacities. Vertices: the GJK tetrahedron plus one support per EPA iteration (at most
 // 65, code/nans.cpp:804). Faces grow by two per iteration on a convex polytope, but the
