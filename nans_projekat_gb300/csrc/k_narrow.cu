@@ -40,10 +40,9 @@ template <int FMAX, int EMAX> struct EpaBuf
     float ax[kEpaMaxVerts], ay[kEpaMaxVerts], az[kEpaMaxVerts];
     float bx[kEpaMaxVerts], by[kEpaMaxVerts], bz[kEpaMaxVerts];
     unsigned char vid[kEpaMaxVerts]; // canonical vertex id (first vertex with an equal P), 0xff: NaN
-    float fnx[FMAX], fny[FMAX], fnz[FMAX], fd[FMAX];
-    unsigned char fa[FMAX], fb[FMAX], fc[FMAX];
+    float fnx[2][FMAX], fny[2][FMAX], fnz[2][FMAX], fd[2][FMAX]; // two banks: the list and its successor
+    unsigned char fa[2][FMAX], fb[2][FMAX], fc[2][FMAX];
     unsigned char ea[EMAX], eb[EMAX];
-    unsigned vis[FMAX / 32];
     unsigned pkey[kPushes];      // horizon push: group lo | hi << 8, orientation << 16, self-loop << 17
     unsigned short puv[kPushes]; // horizon push: u | v << 8
     static constexpr int kShapeCache = 64;
@@ -68,21 +67,24 @@ template <class B> __device__ __forceinline__ void pool_put(B &E, int i, const G
     E.bz[i] = g.sb.z;
 }
 
-// PushTriangle (code/nans.cpp:292-322): N = normalize(cross(B-A, C-A)), flipped to face away
-// from the origin; the face's distance to the origin |dot(N, A)| is cached with it.
-template <class B> __device__ __forceinline__ void face_put(B &E, int f, int a, int b, int c)
+// PushTriangle (code/nans.cpp:292-322) into bank k: N = normalize(cross(B-A, C-A)), flipped to
+// face away from the origin; the face's distance to the origin |dot(N, A)| is cached with it
+// and returned.
+template <class B> __device__ __forceinline__ float face_put(B &E, int k, int f, int a, int b, int c)
 {
     v3 pa = pool_p(E, a), pb = pool_p(E, b), pc = pool_p(E, c);
     v3 n = normalize3(cross3(pb - pa, pc - pa));
     if (dot3(pa, n) < 0.0f)
         n = -1.0f * n;
-    E.fa[f] = (unsigned char)a;
-    E.fb[f] = (unsigned char)b;
-    E.fc[f] = (unsigned char)c;
-    E.fnx[f] = n.x;
-    E.fny[f] = n.y;
-    E.fnz[f] = n.z;
-    E.fd[f] = fabsf(dot3(n, pa));
+    E.fa[k][f] = (unsigned char)a;
+    E.fb[k][f] = (unsigned char)b;
+    E.fc[k][f] = (unsigned char)c;
+    E.fnx[k][f] = n.x;
+    E.fny[k][f] = n.y;
+    E.fnz[k][f] = n.z;
+    const float d = fabsf(dot3(n, pa));
+    E.fd[k][f] = d;
+    return d;
 }
 
 // The support of one shape from its vertices cached in shared memory (hull_support's order
@@ -233,13 +235,48 @@ template <class B> __device__ __forceinline__ bool push_survives(const B &E, int
     return same > opp && after < same - opp;
 }
 
-// ResolveCollision (code/nans.cpp:787-904) on one warp. Returns EPA_CONTACT with the contact
-// written, EPA_NONE, or EPA_OVERFLOW when the polytope outgrows B; then ovf = (iteration,
-// stale, faces, vertices) describes the polytope at the start of that iteration, still in E.
+// Candidate (d, f) for the closest face: the first minimum of the list's distances, NaN
+// distances never winning.
+__device__ __forceinline__ void closest_step(float &bd, int &bi, float d, int f)
+{
+    if (d < bd || (d == bd && f < bi))
+    {
+        bd = d;
+        bi = f;
+    }
+}
+
+// The reference's closest-face scan (CurrentDistance starts at face 0, strict '<'): the first
+// minimum over the faces, except that a NaN face 0 stays the closest. (bd, bi) are each lane's
+// candidates; returns the face and writes its distance.
+template <class B>
+__device__ __forceinline__ int closest_face(const B &E, int k, int nf, float bd, int bi, float &cur)
+{
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const float od = __shfl_xor_sync(0xffffffffu, bd, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        closest_step(bd, bi, od, oi);
+    }
+    int ci = bi;
+    if (nf == 0 || isnan(E.fd[k][0]) || ci >= nf)
+        ci = 0;
+    cur = E.fd[k][ci];
+    return ci;
+}
+
+// ResolveCollision (code/nans.cpp:787-904) on one warp, the face list in one of two banks.
+// One pass over the list tests each face against the new support point, writes the pushes of
+// the visible ones and moves the others to the other bank in order (the stable removal); the
+// closest face of the next list is reduced from the kept and the new faces as they are
+// written. Returns EPA_CONTACT with the contact written, EPA_NONE, or EPA_OVERFLOW when the
+// polytope outgrows B; then ovf = (iteration, stale | bank << 1, faces, vertices) describes the
+// polytope at the start of that iteration, still in E.
 template <class B>
 __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs, const GV &s0, const GV &s1,
                        const GV &s2, const GV &s3, v3 &out_pa, v3 &out_pb, v3 &out_n, int lane, int4 &ovf)
 {
+    const unsigned full = 0xffffffffu;
     if (lane == 0)
     {
         pool_put(E, 0, s0);
@@ -257,16 +294,17 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
     for (int i = 0; i < 4; ++i)
         pool_canon(E, i, lane);
     // ABC, ACD, ADB, BDC (code/nans.cpp:799-802)
-    if (lane == 0)
-        face_put(E, 0, 0, 1, 2);
-    else if (lane == 1)
-        face_put(E, 1, 0, 2, 3);
-    else if (lane == 2)
-        face_put(E, 2, 0, 3, 1);
-    else if (lane == 3)
-        face_put(E, 3, 1, 3, 2);
+    float bd = INFINITY;
+    int bi = 0x7fffffff;
+    if (lane < 4)
+    {
+        const int a = lane == 3 ? 1 : 0, b = lane == 0 ? 1 : (lane == 1 ? 2 : 3), c = lane == 0 ? 2 : (lane == 1 ? 3 : (lane == 2 ? 1 : 2));
+        closest_step(bd, bi, face_put(E, 0, lane, a, b, c), lane);
+    }
     __syncwarp();
-    int nf = 4, nv = 4;
+    int cb = 0, nf = 4, nv = 4;
+    float cur;
+    int ci = closest_face(E, cb, nf, bd, bi, cur);
     // When every face is removed and the horizon cancels out, the reference reads Triangle[0]
     // of the empty vector (code/nans.cpp:807, 824); with libstdc++ that slot still holds the
     // face erased last, the last face of the list before removal. It is kept at index 0.
@@ -275,41 +313,12 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
     {
         if (nf == 0 && !stale)
             return EPA_NONE;
-        // closest face: CurrentDistance starts at face 0; strict '<' keeps the first minimum
-        int ci = 0;
-        float d0 = E.fd[0];
-        if (nf > 0 && !isnan(d0))
-        {
-            float bd = d0;
-            int bi = 0;
-            for (int f = lane; f < nf; f += 32)
-            {
-                float d = E.fd[f];
-                if (d < bd || (d == bd && f < bi))
-                {
-                    bd = d;
-                    bi = f;
-                }
-            }
-            for (int o = 16; o > 0; o >>= 1)
-            {
-                float od = __shfl_xor_sync(0xffffffffu, bd, o);
-                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-                if (od < bd || (od == bd && oi < bi))
-                {
-                    bd = od;
-                    bi = oi;
-                }
-            }
-            ci = bi;
-        }
-        const float cur = E.fd[ci];
-        const v3 n = mk3(E.fnx[ci], E.fny[ci], E.fnz[ci]);
+        const v3 n = mk3(E.fnx[cb][ci], E.fny[cb][ci], E.fnz[cb][ci]);
         const GV ns = warp_support(w, E, A, Bs, n, lane);
         if (dot3(n, ns.p) - cur < 0.001f)
         {
             // Barycentric (code/nans.cpp:771-785) of N*dist on the closest face
-            int ia = E.fa[ci], ib = E.fb[ci], ic = E.fc[ci];
+            int ia = E.fa[cb][ci], ib = E.fb[cb][ci], ic = E.fc[cb][ci];
             v3 pa = pool_p(E, ia), pb = pool_p(E, ib), pc = pool_p(E, ic);
             v3 p = cur * n;
             v3 v0 = pb - pa, v1 = pc - pa, v2 = p - pa;
@@ -334,144 +343,117 @@ __device__ int epa_run(const DevWorld &w, B &E, const Shape &A, const Shape &Bs,
         }
         if (nf == 0)
             return EPA_NONE; // the stale read repeats identically until the iteration cap
-        // faces that see the new support point (code/nans.cpp:869-891)
-        const int nchunks = (nf + 31) >> 5;
-        int nseen = 0;
-        for (int ch = 0; ch < nchunks; ++ch)
+        // faces that see the new support point (code/nans.cpp:869-891): pushes of the visible
+        // ones, the others into the other bank in order
+        const int nb = cb ^ 1;
+        int nseen = 0, keep = 0;
+        bd = INFINITY;
+        bi = 0x7fffffff;
+        for (int base = 0; base < nf; base += 32)
         {
-            int f = ch * 32 + lane;
+            const int f = base + lane;
+            const bool in = f < nf;
             bool vis = false;
-            if (f < nf)
+            unsigned char a = 0, b = 0, c = 0;
+            v3 fn = mk3(0.0f, 0.0f, 0.0f);
+            float d = 0.0f;
+            if (in)
             {
-                v3 fa = pool_p(E, E.fa[f]);
-                v3 fn = mk3(E.fnx[f], E.fny[f], E.fnz[f]);
-                vis = dot3(fn, ns.p - fa) > 0.0f;
+                a = E.fa[cb][f];
+                b = E.fb[cb][f];
+                c = E.fc[cb][f];
+                fn = mk3(E.fnx[cb][f], E.fny[cb][f], E.fnz[cb][f]);
+                d = E.fd[cb][f];
+                vis = dot3(fn, ns.p - pool_p(E, a)) > 0.0f;
             }
-            unsigned bal = __ballot_sync(0xffffffffu, vis);
-            if (lane == 0)
-                E.vis[ch] = bal;
-            nseen += __popc(bal);
+            const unsigned bv = __ballot_sync(full, vis), bk = __ballot_sync(full, in && !vis);
+            const unsigned below = (1u << lane) - 1u;
+            if (vis)
+            {
+                const int r = nseen + __popc(bv & below);
+                push_put(E, 3 * r, a, b);
+                push_put(E, 3 * r + 1, b, c);
+                push_put(E, 3 * r + 2, c, a);
+            }
+            else if (in)
+            {
+                const int dst = keep + __popc(bk & below);
+                E.fa[nb][dst] = a;
+                E.fb[nb][dst] = b;
+                E.fc[nb][dst] = c;
+                E.fnx[nb][dst] = fn.x;
+                E.fny[nb][dst] = fn.y;
+                E.fnz[nb][dst] = fn.z;
+                E.fd[nb][dst] = d;
+                closest_step(bd, bi, d, dst);
+            }
+            nseen += __popc(bv);
+            keep += __popc(bk);
         }
         __syncwarp();
         if (nseen == 0)
             return EPA_NONE; // nothing changes: every later iteration repeats this one
-        // horizon: the pushes (A,B), (B,C), (C,A) of the visible faces in face order, decided
-        // in parallel; the survivors keep push order
+        // horizon: the pushes decided in parallel; the survivors keep push order
+        const int np = 3 * nseen;
         int ne = 0;
+        for (int base = 0; base < np; base += 32)
         {
-            int nvis = 0;
-            for (int ch = 0; ch < nchunks; ++ch)
+            const int k = base + lane;
+            const bool alive = k < np && push_survives(E, k, np);
+            const unsigned bal = __ballot_sync(full, alive);
+            if (alive)
             {
-                const unsigned m = E.vis[ch];
-                if ((m >> lane) & 1u)
+                const int dst = ne + __popc(bal & ((1u << lane) - 1u));
+                if (dst < B::kEdges)
                 {
-                    const int f = ch * 32 + lane;
-                    const int r = nvis + __popc(m & ((1u << lane) - 1u));
-                    const int a = E.fa[f], b = E.fb[f], c = E.fc[f];
-                    push_put(E, 3 * r, a, b);
-                    push_put(E, 3 * r + 1, b, c);
-                    push_put(E, 3 * r + 2, c, a);
+                    const unsigned uv = E.puv[k];
+                    E.ea[dst] = (unsigned char)(uv & 0xffu);
+                    E.eb[dst] = (unsigned char)(uv >> 8);
                 }
-                nvis += __popc(m);
             }
-            __syncwarp();
-            const int np = 3 * nvis;
-            for (int base = 0; base < np; base += 32)
-            {
-                const int k = base + lane;
-                const bool alive = k < np && push_survives(E, k, np);
-                const unsigned bal = __ballot_sync(0xffffffffu, alive);
-                if (alive)
-                {
-                    const int dst = ne + __popc(bal & ((1u << lane) - 1u));
-                    if (dst < B::kEdges)
-                    {
-                        const unsigned uv = E.puv[k];
-                        E.ea[dst] = (unsigned char)(uv & 0xffu);
-                        E.eb[dst] = (unsigned char)(uv >> 8);
-                    }
-                }
-                ne += __popc(bal);
-            }
-            if (ne > B::kEdges || nf - nseen + ne > B::kFaces)
-            {
-                ovf = make_int4(it, stale ? 1 : 0, nf, nv);
-                return EPA_OVERFLOW;
-            }
-            __syncwarp();
+            ne += __popc(bal);
         }
-        // stable removal of the visible faces
-        int keep = 0;
-        for (int ch = 0; ch < nchunks; ++ch)
+        if (ne > B::kEdges || keep + ne > B::kFaces)
         {
-            int f = ch * 32 + lane;
-            unsigned vm = E.vis[ch];
-            bool stay = (f < nf) && !((vm >> lane) & 1u);
-            unsigned sm = __ballot_sync(0xffffffffu, stay);
-            int dst = keep + __popc(sm & ((1u << lane) - 1u));
-            float nx = 0.f, ny = 0.f, nz = 0.f, d = 0.f;
-            unsigned char a = 0, b = 0, c = 0;
-            if (stay)
-            {
-                nx = E.fnx[f];
-                ny = E.fny[f];
-                nz = E.fnz[f];
-                d = E.fd[f];
-                a = E.fa[f];
-                b = E.fb[f];
-                c = E.fc[f];
-            }
-            __syncwarp();
-            if (stay)
-            {
-                E.fnx[dst] = nx;
-                E.fny[dst] = ny;
-                E.fnz[dst] = nz;
-                E.fd[dst] = d;
-                E.fa[dst] = a;
-                E.fb[dst] = b;
-                E.fc[dst] = c;
-            }
-            __syncwarp();
-            keep += __popc(sm);
+            ovf = make_int4(it, (stale ? 1 : 0) | (cb << 1), nf, nv);
+            return EPA_OVERFLOW;
         }
+        __syncwarp();
         if (keep == 0 && ne == 0)
         {
-            // every face removed: slot 0 keeps the last face of the list (still intact, the
-            // compaction wrote nothing)
+            // every face removed: slot 0 keeps the last face of the list
             if (lane == 0)
             {
-                int l = nf - 1;
-                E.fa[0] = E.fa[l];
-                E.fb[0] = E.fb[l];
-                E.fc[0] = E.fc[l];
-                E.fnx[0] = E.fnx[l];
-                E.fny[0] = E.fny[l];
-                E.fnz[0] = E.fnz[l];
-                E.fd[0] = E.fd[l];
+                const int l = nf - 1;
+                E.fa[nb][0] = E.fa[cb][l];
+                E.fb[nb][0] = E.fb[cb][l];
+                E.fc[nb][0] = E.fc[cb][l];
+                E.fnx[nb][0] = E.fnx[cb][l];
+                E.fny[nb][0] = E.fny[cb][l];
+                E.fnz[nb][0] = E.fnz[cb][l];
+                E.fd[nb][0] = E.fd[cb][l];
             }
             __syncwarp();
             stale = true;
         }
         // the new support joins the vertex pool; new faces (S, e.A, e.B) in edge order
-        int sv = nv;
+        const int sv = nv;
         if (lane == 0)
             pool_put(E, sv, ns);
         ++nv;
         __syncwarp();
         pool_canon(E, sv, lane);
         for (int j = lane; j < ne; j += 32)
-            face_put(E, keep + j, sv, E.ea[j], E.eb[j]);
+            closest_step(bd, bi, face_put(E, nb, keep + j, sv, E.ea[j], E.eb[j]), keep + j);
         __syncwarp();
+        cb = nb;
         nf = keep + ne;
+        ci = closest_face(E, cb, nf, bd, bi, cur);
     }
     return EPA_NONE;
 }
 
 
-// Queues a candidate whose EPA outgrew the current tier: the warp tier (capacity med_cap),
-// then the large-polytope tier (capacity ovf_cap). The next tier reruns GJK (deterministic,
-// so it sees the same simplex) and EPA from scratch.
 // Returns the tier-3 queue index (the caller may leave its state in handover[q]), or -1.
 __device__ __forceinline__ int escalate(const DevWorld &w, int c, bool to_big)
 {
@@ -505,7 +487,7 @@ __device__ __forceinline__ int escalate(const DevWorld &w, int c, bool to_big)
 __device__ __forceinline__ void handover_put(const DevWorld &w, const EpaFast &E, int q, int4 ovf, int lane)
 {
     EpaHandover &H = w.handover[q];
-    const int nf = ovf.z, nv = ovf.w;
+    const int nf = ovf.z, nv = ovf.w, k = (ovf.y >> 1) & 1;
     for (int i = lane; i < nv; i += 32)
     {
         H.px[i] = E.px[i];
@@ -521,17 +503,17 @@ __device__ __forceinline__ void handover_put(const DevWorld &w, const EpaFast &E
     }
     for (int f = lane; f < nf; f += 32)
     {
-        H.fidx[f] = (unsigned)E.fa[f] | ((unsigned)E.fb[f] << 8) | ((unsigned)E.fc[f] << 16);
-        H.fnx[f] = E.fnx[f];
-        H.fny[f] = E.fny[f];
-        H.fnz[f] = E.fnz[f];
-        H.fd[f] = E.fd[f];
+        H.fidx[f] = (unsigned)E.fa[k][f] | ((unsigned)E.fb[k][f] << 8) | ((unsigned)E.fc[k][f] << 16);
+        H.fnx[f] = E.fnx[k][f];
+        H.fny[f] = E.fny[k][f];
+        H.fnz[f] = E.fnz[k][f];
+        H.fd[f] = E.fd[k][f];
     }
     __syncwarp();
     if (lane == 0)
     {
         H.hdr[0] = ovf.x;
-        H.hdr[1] = ovf.y;
+        H.hdr[1] = ovf.y & 1;
         H.hdr[3] = nv;
         __threadfence();
         H.hdr[2] = nf;
