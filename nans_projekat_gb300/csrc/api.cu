@@ -186,10 +186,8 @@ int alloc_candidates(nans_world *w, int cap)
             return rc;
         d.s_fwd = w->fwd_buf;
     }
-    d.cand_pidx = nullptr;
-    if (w->flags & NANS_WORLD_WARM_START)
-        if ((rc = dalloc(w, L, &d.cand_pidx, cap)))
-            return rc;
+    if ((rc = dalloc(w, L, &d.cand_pidx, cap)))
+        return rc;
     return NANS_OK;
 }
 
@@ -399,6 +397,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &w->d_prm, nall)) || (rc = dalloc(w, L, &w->d_model_in, (size_t)4 * nall)) ||
         (rc = dalloc(w, L, &d.box_lo, nall)) || (rc = dalloc(w, L, &d.box_hi, nall)) ||
         (rc = dalloc(w, L, &d.pair_mask, (size_t)word_acc)) || (rc = dalloc(w, L, &p_wscene, (size_t)word_acc)) ||
+        (rc = dalloc(w, L, &d.epa_hist, (size_t)word_acc * 32)) ||
         (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.cull_total, 1)) ||
         (rc = dalloc(w, L, &d.n_cand, 1)) ||
         (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
@@ -414,6 +413,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &w->d_rec_floor, (size_t)61 * S)) || (rc = dalloc(w, L, &w->d_small, 2)) ||
         (rc = dalloc(w, L, &d.s_last, 1)))
         return rc;
+    // no EPA seen yet: every pair starts in the short-EPA part of the queue
+    CK(cudaMemset(d.epa_hist, 0, std::max(1LL, word_acc * 32)));
     // world vertices are written by the first step; zero until then (the renderer reads them)
     CK(cudaMemset(d.verts, 0, (size_t)std::max(1LL, vert_floats) * sizeof(float)));
     d.sc_cube0 = p_cube0;

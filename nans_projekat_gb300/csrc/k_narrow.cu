@@ -626,7 +626,7 @@ __device__ __forceinline__ bool tiny_edge(TinySmem &S, int t, unsigned long long
 // creation: a running minimum with strict '<' over the kept faces, then the new ones, in list
 // order, is the reference's scan (a NaN first distance keeps face 0, as its scan does).
 __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, const Shape &B, const float *simp,
-                        v3 &out_pa, v3 &out_pb, v3 &out_n)
+                        v3 &out_pa, v3 &out_pb, v3 &out_n, int &iters)
 {
     TinyLocal L;
     unsigned long long canon = 0ull;
@@ -665,6 +665,7 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
     bool stale = false;
     for (int it = 0; it <= 64; ++it)
     {
+        iters = it + 1;
         if (nf == 0 && !stale)
             return EPA_NONE;
         const v3 n = mk3(S.fnx[ci][t], S.fny[ci][t], S.fnz[ci][t]);
@@ -788,19 +789,27 @@ __device__ __forceinline__ void store_simplex(const DevWorld &w, int c, const GV
     o[8] = make_float4(s3.sa.z, s3.sb.x, s3.sb.y, s3.sb.z);
 }
 
-// Appends c to the EPA queue when `hit` (one atomic per warp).
+// Appends c to the EPA queue when `hit` (one atomic per warp and part). Pairs whose EPA took
+// more than kEpaLongIters iterations at its last step fill the queue from the back (count in
+// work counter 9), the others from the front (work counter 10): the per-thread EPA pass takes
+// the long ones first, so that the lanes of a warp run EPAs of similar length.
+constexpr int kEpaLongIters = 4;
 __device__ __forceinline__ void enqueue_epa(const DevWorld &w, int c, bool hit)
 {
     const unsigned act = __activemask();
-    const unsigned bal = __ballot_sync(act, hit);
+    const bool lng = hit && w.epa_hist[w.cand_pidx[c]] > kEpaLongIters;
+    const unsigned bal = __ballot_sync(act, hit && !lng), ball = __ballot_sync(act, lng);
     if (!hit)
         return;
-    const int lane = threadIdx.x & 31, leader = __ffs(bal) - 1;
+    const int lane = threadIdx.x & 31;
+    const unsigned part = lng ? ball : bal;
+    const int leader = __ffs(part) - 1;
     int base = 0;
     if (lane == leader)
-        base = atomicAdd(w.work_counter + 10, __popc(bal));
-    base = __shfl_sync(bal, base, leader);
-    w.s_order[base + __popc(bal & ((1u << lane) - 1u))] = c;
+        base = atomicAdd(w.work_counter + (lng ? 9 : 10), __popc(part));
+    base = __shfl_sync(part, base, leader);
+    const int k = base + __popc(part & ((1u << lane) - 1u));
+    w.s_order[lng ? w.cand_cap - 1 - k : k] = c;
 }
 
 // GJK of candidate c from call `it` with the simplex (s0..s3, n points). With a budget below
@@ -884,7 +893,7 @@ __global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
 {
     __shared__ TinySmem S;
     const int lane = threadIdx.x & 31, t = threadIdx.x;
-    const int n = w.work_counter[10];
+    const int nl = w.work_counter[9], n = nl + w.work_counter[10];
     for (;;)
     {
         int base = 0;
@@ -896,10 +905,13 @@ __global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
         const int i = base + lane;
         if (i >= n)
             continue;
-        const int c = w.s_order[i];
+        const int c = w.s_order[i < nl ? w.cand_cap - 1 - i : i - nl]; // the long part first
         const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
         v3 pa, pb, nn;
-        const int r = epa_tiny(w, S, t, A, B, reinterpret_cast<const float *>(w.s_k + 9 * (size_t)c), pa, pb, nn);
+        int iters = 0;
+        const int r =
+            epa_tiny(w, S, t, A, B, reinterpret_cast<const float *>(w.s_k + 9 * (size_t)c), pa, pb, nn, iters);
+        w.epa_hist[w.cand_pidx[c]] = (unsigned char)(r == EPA_OVERFLOW ? 255 : iters);
         if (r == EPA_OVERFLOW)
             escalate(w, c, false);
         else

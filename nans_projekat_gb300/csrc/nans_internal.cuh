@@ -127,6 +127,7 @@ struct DevWorld
     float4 *warm;
     int *warm_step;                     // step counter, advanced by the sweep
     int *cand_pidx;                     // per candidate: its pair-space index
+    unsigned char *epa_hist;            // per pair-space index: iterations of its last per-thread EPA
     int *s_maxw;                        // per scene: highest wave of the last solve, or null
     unsigned *status;
 };
