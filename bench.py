@@ -342,10 +342,11 @@ def fit_measurement(lib, device, n_scenes=1024, nsteps=120, iters=20):
     """Gradient-based fitting through the differentiable rollout on the mixed workload (1,024
     scenes of 8-128 boxes, spheres and convex hulls, 120 steps, 20 Adam steps): the spheres'
     initial velocities are fitted so that their positions after the rollout match those of a
-    rollout from perturbed velocities (N(0, 0.2) m/s). Gradient norm clipped at 10. (The
-    survey's 4,096 scenes x 240 steps x 50 Adam steps keeps a tape of every candidate pair of
-    every step; scenes whose bodies the reference's solver flings away turn every pair into a
-    candidate, which makes that tape outgrow the GPU.)"""
+    rollout from perturbed velocities (N(0, 0.2) m/s); spheres flung beyond 10 km drop out of
+    the loss. Gradient norm clipped at 10. (A fit of 4,096 scenes x 240 steps x 50 Adam steps
+    keeps a tape of every candidate pair of every step; scenes whose bodies the reference's
+    solver flings away turn every pair into a candidate, which makes that tape outgrow the
+    GPU.)"""
     import torch
     from nans_projekat_gb300 import diff, scenes
     batch = scenes.mixed_batch(n_scenes, seed=4)
