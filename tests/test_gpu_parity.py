@@ -212,6 +212,36 @@ def test_state_arrays_match_records(nl):
     b.close()
 
 
+def test_state_arrays_through_pinned_host_memory(nl):
+    """Page-locked host arrays (the end-to-end benchmark's) carry the same values as pageable
+    arrays, in both directions."""
+    import torch
+    batch = scenes.stack_batch(32, seed=10, lo=4, hi=40)
+    dt = np.float32(1 / 60)
+    w = nl.World()
+    w.upload_batch(batch)
+    w.batch_step(dt, 12, graph_steps=0)
+    n = w.n_bodies
+
+    def pinned():
+        return torch.empty(n * 12, dtype=torch.uint8, pin_memory=True).numpy().view(np.float32).reshape(n, 3)
+
+    ref = w.get_state_arrays()
+    pin = tuple(pinned() for _ in range(4))
+    w.get_state_arrays(out=pin)
+    for r, p in zip(ref, pin):
+        assert canon(r) == canon(p)
+    moved = [p.copy() for p in pin]
+    moved[2][:] += np.float32(0.5)
+    for p, m in zip(pin, moved):
+        p[:] = m
+    w.set_state_arrays(*pin)
+    back = w.get_state_arrays()
+    for m, b in zip(moved, back):
+        assert canon(m) == canon(b)
+    w.close()
+
+
 def test_demo_frames_model_and_vertices(nl):
     """The reference frame's records after 300 frames, Model and Vertices included."""
     scene, meta, digests, saved = load_golden("demo_frames")
