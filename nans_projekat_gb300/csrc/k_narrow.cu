@@ -16,8 +16,10 @@
 //     the warp tier decides every push's fate in parallel from its group of equal edges.
 // A face's "recomputed" normal in the closest-face search and the removal test equals its
 // stored normal bit for bit (same operands, same operations, the flip is an exact negation),
-// so each face's distance |dot(N, A)| is computed once when the face is created.
-// The warp's lanes share the per-face loops; the sequential parts run redundantly.
+// so each face's distance |dot(N, A)| is computed once, when the face is created or kept.
+// An EPA whose support point no face sees ends at once: nothing changes, so every later
+// iteration would repeat it up to the cap. Tier 1 runs one EPA per thread; tier 2 one per
+// warp, whose lanes share the per-face loops while the sequential parts run redundantly.
 #include <algorithm>
 
 #include "nans_gjk.cuh"
@@ -25,12 +27,11 @@
 namespace nans
 {
 
-// Polytope storage of one EPA. The vertex pool holds the GJK tetrahedron plus one support per
-// iteration; faces are an ordered list (vertex indices, normal, cached distance); edges are
-// the current horizon. FMAX / EMAX bound faces and edges.
 // Polytope of one warp-cooperative EPA (shared memory). The vertex pool holds the GJK
-// tetrahedron plus one support per iteration; faces are an ordered list (vertex indices,
-// normal, cached distance); edges are the current horizon.
+// tetrahedron plus one support per iteration, with canonical ids; faces are an ordered list
+// (vertex indices, normal, cached distance) in one of two banks, the removal pass writing the
+// next list into the other; edges are the current horizon, pushes the iteration's horizon
+// candidates. FMAX / EMAX bound faces and horizon edges.
 template <int FMAX, int EMAX> struct EpaBuf
 {
     static constexpr int kFaces = FMAX;
