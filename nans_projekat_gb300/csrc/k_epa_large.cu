@@ -5,7 +5,9 @@
 // whole grid per EPA in tier 4 (a cooperative launch; one arena of 8,388,608 faces). Every
 // step of an iteration is a parallel pass over the face list or the horizon pushes, so a
 // polytope of millions of faces (the reference's EPA can grow geometrically on degenerate
-// input) is processed at memory speed by the whole GPU instead of one SM.
+// input) is processed at memory speed by the whole GPU instead of one SM. Each tier resumes
+// the polytope the previous tier left at the start of the iteration that outgrew it (the warp
+// tier's through a handover buffer, tier 3's in its block arena), so no iteration runs twice.
 //
 // Per iteration:
 //   closest face      argmin of the cached distances, first minimum; a NaN face 0 is chosen
