@@ -45,3 +45,29 @@ def test_two_rank_gloo_aggregation():
     assert [r[1] for r in res] == [11.0, 11.0]        # max over ranks
     assert [r[2] for r in res] == [300.0, 300.0]      # sum over ranks
     assert res[0][3] != res[1][3]                     # independent shards per rank
+
+
+def test_bench_line_is_strict_json(capsys):
+    """The bench line never carries NaN or Infinity tokens (a non-finite secondary figure is
+    written as a string), and numpy scalars serialise as numbers."""
+    import json
+    import sys
+    import numpy as np
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    bench.emit({"value": np.float32(1.5), "n": np.int64(3),
+                "secondary": {"loss": float("inf"), "x": [float("nan"), 2.0]}})
+    line = capsys.readouterr().out.strip()
+    d = json.loads(line, parse_constant=lambda c: (_ for _ in ()).throw(ValueError(c)))
+    assert d["value"] == 1.5 and d["n"] == 3
+    assert d["secondary"]["loss"] == "inf" and d["secondary"]["x"][0] == "nan"
+
+
+def test_traffic_figures_cover_the_reported_kernels():
+    """Every kernel name the bench's roofline can report has a measured DRAM figure."""
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    for k in ("k_narrow_tiny", "k_sweep", "k_cull_mask", "k_solve"):
+        v = bench.measured_traffic(k)
+        assert v is not None and v > 0, k
