@@ -10,68 +10,10 @@
 //   k_cull_scan   exclusive scan of the block counts -> candidate offsets, total, capacity
 //   k_cull_write  the pairs of each word at its prefix position, one lane per pair
 // all_pairs != 0 keeps every pair (the reference's exact all-pairs behaviour).
-#include "nans_kernels.cuh"
+#include "nans_kernels.cuh" // pair-space decode: nans_pairs.cuh
 
 namespace nans
 {
-
-// Largest i with row_start(i) = i*n - i*(i+1)/2 <= k, for pairs i < j < n: a single-precision
-// first guess corrected exactly in integers.
-__device__ __forceinline__ void tri_decode_fast(long long k, long long n, int &i, int &j)
-{
-    const float a = 2.0f * (float)n - 1.0f;
-    const float disc = a * a - 8.0f * (float)k;
-    long long ii = (long long)floorf((a - sqrtf(disc > 0.0f ? disc : 0.0f)) * 0.5f);
-    if (ii < 0)
-        ii = 0;
-    if (ii > n - 2)
-        ii = n - 2;
-    while (ii > 0 && ii * n - ii * (ii + 1) / 2 > k)
-        --ii;
-    while (ii + 1 <= n - 2 && (ii + 1) * n - (ii + 1) * (ii + 2) / 2 <= k)
-        ++ii;
-    const long long rs = ii * n - ii * (ii + 1) / 2;
-    i = (int)ii;
-    j = (int)(ii + 1 + (k - rs));
-}
-
-// Scene-local pair index k -> (type, i, j), as decode_local with the fast triangle decode.
-__device__ __forceinline__ void decode_pair(long long k, int nc, int ns, int &type, int &i, int &j)
-{
-    const long long ncc = (long long)nc * (nc - 1) / 2;
-    if (k < ncc)
-    {
-        type = T_CC;
-        tri_decode_fast(k, nc, i, j);
-        return;
-    }
-    k -= ncc;
-    if (k < nc)
-    {
-        type = T_CF;
-        i = j = (int)k;
-        return;
-    }
-    k -= nc;
-    if (k < ns)
-    {
-        type = T_SF;
-        i = j = (int)k;
-        return;
-    }
-    k -= ns;
-    const long long ncs = (long long)nc * ns;
-    if (k < ncs)
-    {
-        type = T_CS;
-        i = (int)(k / ns);
-        j = (int)(k % ns);
-        return;
-    }
-    k -= ncs;
-    type = T_SS;
-    tri_decode_fast(k, ns, i, j);
-}
 
 __device__ __forceinline__ int block_sum(int v, int *sh)
 {
@@ -120,32 +62,6 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int *total)
     *total = sh[(blockDim.x >> 5) - 1];
     __syncthreads();
     return warp_prefix + x - v;
-}
-
-// (type, i, j) of the pair `off` places after (type0, i0, j0), the pair at scene-local index
-// p0: for cube-cube pairs the same row or the next one directly, otherwise a full decode.
-__device__ __forceinline__ void pair_after(long long p0, int nc, int ns, int type0, int i0, int j0, int off,
-                                           int &type, int &i, int &j)
-{
-    if (type0 == T_CC)
-    {
-        const int r0 = nc - j0; // pairs (i0, j0 .. nc-1)
-        if (off < r0)
-        {
-            type = T_CC;
-            i = i0;
-            j = j0 + off;
-            return;
-        }
-        if (off - r0 < nc - i0 - 2) // pairs (i0+1, i0+2 .. nc-1)
-        {
-            type = T_CC;
-            i = i0 + 1;
-            j = i0 + 2 + (off - r0);
-            return;
-        }
-    }
-    decode_pair(p0 + off, nc, ns, type, i, j);
 }
 
 // Global body ids of pair (type, i, j) of scene s whose cubes start at c0 (nc cubes).

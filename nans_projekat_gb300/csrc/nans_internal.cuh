@@ -22,18 +22,10 @@
 #include <stdint.h>
 #include <cfloat>
 #include "nans_math.cuh"
+#include "nans_pairs.cuh"
 
 namespace nans
 {
-
-enum PairType
-{
-    T_CC = 0,
-    T_CS = 1,
-    T_CF = 2,
-    T_SS = 3,
-    T_SF = 4
-};
 
 // device status bits (or'ed into DevWorld::status)
 enum StatusBits
@@ -209,149 +201,6 @@ __device__ __forceinline__ GV minkowski_support(const float *verts, const Shape 
     r.sb = shape_support(verts, B, -1.0f * d);
     r.p = r.sa - r.sb;
     return r;
-}
-
-// ------------------------------------------------------------------------------------
-// pair-space enumeration of one scene in the reference order (code/nans.cpp:1355-1535)
-// ------------------------------------------------------------------------------------
-__host__ __device__ __forceinline__ long long scene_pair_count(long long nc, long long ns)
-{
-    return nc * (nc - 1) / 2 + nc + ns + nc * ns + ns * (ns - 1) / 2;
-}
-
-// Largest i with row_start(i) = i*n - i*(i+1)/2 <= k, for pairs i < j < n.
-__device__ __forceinline__ void tri_decode(long long k, long long n, int &i, int &j)
-{
-    double a = 2.0 * (double)n - 1.0;
-    double disc = a * a - 8.0 * (double)k;
-    long long ii = (long long)floor((a - sqrt(disc > 0.0 ? disc : 0.0)) * 0.5);
-    if (ii < 0)
-        ii = 0;
-    if (ii > n - 2)
-        ii = n - 2;
-    while (ii > 0 && ii * n - ii * (ii + 1) / 2 > k)
-        --ii;
-    while (ii + 1 <= n - 2 && (ii + 1) * n - (ii + 1) * (ii + 2) / 2 <= k)
-        ++ii;
-    long long rs = ii * n - ii * (ii + 1) / 2;
-    i = (int)ii;
-    j = (int)(ii + 1 + (k - rs));
-}
-
-// Decodes scene-local pair index k into (type, i, j).
-__device__ __forceinline__ void decode_local(long long k, int nc, int ns, int &type, int &i, int &j)
-{
-    long long ncc = (long long)nc * (nc - 1) / 2;
-    if (k < ncc)
-    {
-        type = T_CC;
-        tri_decode(k, nc, i, j);
-        return;
-    }
-    k -= ncc;
-    if (k < nc)
-    {
-        type = T_CF;
-        i = j = (int)k;
-        return;
-    }
-    k -= nc;
-    if (k < ns)
-    {
-        type = T_SF;
-        i = j = (int)k;
-        return;
-    }
-    k -= ns;
-    long long ncs = (long long)nc * ns;
-    if (k < ncs)
-    {
-        type = T_CS;
-        i = (int)(k / ns);
-        j = (int)(k % ns);
-        return;
-    }
-    k -= ncs;
-    type = T_SS;
-    tri_decode(k, ns, i, j);
-}
-
-// Moves to the first pair of the first non-empty region at or after `type`
-// (region order CC, CF, SF, CS, SS); returns false when the scene has no such pair.
-__device__ __forceinline__ bool start_region(int nc, int ns, int from, int &type, int &i, int &j)
-{
-    // region index of each type in enumeration order CC, CF, SF, CS, SS
-    int r0 = (from == T_CC) ? 0 : (from == T_CF) ? 1 : (from == T_SF) ? 2 : (from == T_CS) ? 3 : 4;
-    for (int r = r0; r < 5; ++r)
-    {
-        if (r == 0 && nc > 1) { type = T_CC; i = 0; j = 1; return true; }
-        if (r == 1 && nc > 0) { type = T_CF; i = j = 0; return true; }
-        if (r == 2 && ns > 0) { type = T_SF; i = j = 0; return true; }
-        if (r == 3 && nc > 0 && ns > 0) { type = T_CS; i = 0; j = 0; return true; }
-        if (r == 4 && ns > 1) { type = T_SS; i = 0; j = 1; return true; }
-    }
-    return false;
-}
-
-// Advances (type, i, j) to the next pair of the same scene; returns false past the end.
-__device__ __forceinline__ bool advance_local(int nc, int ns, int &type, int &i, int &j)
-{
-    switch (type)
-    {
-    case T_CC:
-        if (++j < nc)
-            return true;
-        ++i;
-        j = i + 1;
-        if (j < nc)
-            return true;
-        return start_region(nc, ns, T_CF, type, i, j);
-    case T_CF:
-        if (++i < nc)
-        {
-            j = i;
-            return true;
-        }
-        return start_region(nc, ns, T_SF, type, i, j);
-    case T_SF:
-        if (++i < ns)
-        {
-            j = i;
-            return true;
-        }
-        return start_region(nc, ns, T_CS, type, i, j);
-    case T_CS:
-        if (++j < ns)
-            return true;
-        j = 0;
-        if (++i < nc)
-            return true;
-        return start_region(nc, ns, T_SS, type, i, j);
-    default:
-        if (++j < ns)
-            return true;
-        ++i;
-        j = i + 1;
-        return j < ns;
-    }
-}
-
-__host__ __device__ __forceinline__ bool type_b_is_floor(int t) { return t == T_CF || t == T_SF; }
-__host__ __device__ __forceinline__ bool type_a_is_sphere(int t) { return t == T_SS || t == T_SF; }
-__host__ __device__ __forceinline__ bool type_b_is_sphere(int t) { return t == T_CS || t == T_SS; }
-
-// Global body ids of a scene-local pair.
-__device__ __forceinline__ void pair_bodies(const DevWorld &w, int scene, int type, int i, int j, int &a,
-                                            int &b)
-{
-    int c0 = __ldg(w.sc_cube0 + scene);
-    int nc = __ldg(w.sc_nc + scene);
-    int s0 = c0 + nc;
-    a = type_a_is_sphere(type) ? s0 + i : c0 + i;
-    if (type_b_is_floor(type))
-        b = w.n_dyn + scene;
-    else
-        b = type_b_is_sphere(type) ? s0 + j : c0 + j;
 }
 
 } // namespace nans
