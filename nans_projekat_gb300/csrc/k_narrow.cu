@@ -1,9 +1,16 @@
-// Narrowphase: GJK per candidate pair (one lane each), then EPA per hit (one warp each).
+// Narrowphase tiers 1 and 2: GJK per candidate pair (one lane each), then EPA per hit, one
+// per thread on a 12-vertex / 20-face polytope (tier 1) and, for the EPAs that outgrow it,
+// one per warp on a 256-face polytope (tier 2; tiers 3 and 4 are in k_epa_large.cu).
 //
 // GJK follows CheckCollision / EvolveSimplex (code/nans.cpp:571-769, 906-966): the search
 // direction is reset to normalize(PB - PA) on every call, Simplex[0] is the oldest point,
 // at most 65 calls, the degenerate-direction exit at |d| <= 1e-4 and the support test
-// dot(d, P) >= 0. The simplex lives in registers as four named slots.
+// dot(d, P) >= 0. The simplex lives in registers as four named slots. k_gjk gives each pair
+// 8 calls; pairs still evolving are queued with their simplex and call index and resumed by
+// k_gjk_long, so that long runs share warps with each other. A hit's final simplex is stored
+// for the EPA. The tier-1 queue is ordered in two parts: pairs whose EPA ran more than a few
+// iterations at the previous step first, then the rest, so that a warp's lanes run EPAs of
+// similar length.
 //
 // EPA follows ResolveCollision (code/nans.cpp:217-328, 771-904) with the polytope in
 // fixed-capacity shared-memory buffers instead of std::vector:
