@@ -146,6 +146,9 @@ typedef struct nans_step_params
 
 typedef struct nans_world nans_world;
 
+/* A world replaces the sdl_state that SimUpdateAndRender casts out of the platform's
+ * PermanentStorage and initialises on its first call (code/nans.cpp:1721-1729); the world
+ * owns the device memory instead of the platform's mmap block (code/sdl_nans.cpp:541-555). */
 int nans_world_create(const nans_world_desc *desc, nans_world **out);
 int nans_world_destroy(nans_world *world);
 
@@ -167,23 +170,31 @@ int nans_batch_upload(nans_world *world, uint32_t nscenes, const uint32_t *scene
 
 /* The plain drop-in step: nsteps reference steps on every scene of the world, launched
  * stage by stage, synchronised before returning. params (or NULL to keep the current
- * constants) applies to every scene. */
+ * constants) applies to every scene. Replaces the frame's Pairs.clear(), IntegrateForces,
+ * DetectCollisions, SolveConstraints, IntegrateVelocities (code/nans.cpp:1756-1764) and the
+ * render code's Model rebuild (code/nans.cpp:1909-1942). */
 int nans_step(nans_world *world, const nans_step_params *params, float dt, uint32_t nsteps);
 
 /* The batched step: the same stages as persistent kernels with work queues, nsteps steps
- * replayed from a CUDA graph of graph_steps steps (0 = 60). Synchronised before returning. */
+ * replayed from a CUDA graph of graph_steps steps (0 = 60). Synchronised before returning.
+ * The step of code/nans.cpp:1756-1764 for many independent sdl_states at once (the reference
+ * steps one). */
 int nans_batch_step(nans_world *world, float dt, uint32_t nsteps, uint32_t graph_steps);
 
 /* Picks narrowphase / solver launch shapes by timing a few steps on the world's own
- * scenes; the state is restored afterwards. */
+ * scenes; the state is restored afterwards. No reference counterpart. */
 int nans_batch_autotune(nans_world *world, float dt);
 
 /* Bodies back in the reference layouts, all scenes concatenated in upload order; any of
- * the pointers may be NULL. Applies the last step's pending IntegrateVelocities first. */
+ * the pointers may be NULL. Applies the last step's pending IntegrateVelocities first. What
+ * the reference's render code and next frame read from sdl_state's Cubes, Spheres and Floor
+ * (code/nans.h:374-386). */
 int nans_world_download(nans_world *world, nans_cube *cubes, nans_sphere *spheres, nans_cube *floors);
 
 /* Overwrites the dynamic fields (Position, V, Forces, Angles, W, Torque and, with
- * NANS_UPLOAD_KEEP_MODEL, Model) of every body from records laid out as at upload. */
+ * NANS_UPLOAD_KEEP_MODEL, Model) of every body from records laid out as at upload: the
+ * writes the reference's input handling makes to sdl_state between frames (ShootSphere and
+ * the debug moves, code/nans.cpp:112-190). */
 int nans_world_set_state(nans_world *world, const nans_cube *cubes, const nans_sphere *spheres, uint32_t flags);
 
 /* The dynamic state as four float[n_bodies][3] arrays in record order (the cubes of every
@@ -198,13 +209,16 @@ int nans_world_set_state_arrays(nans_world *world, const float *position, const 
 int nans_world_get_state_arrays(nans_world *world, float *position, float *angles, float *velocity, float *omega);
 
 /* Contact list of one scene after its last DetectCollisions, in the reference's order
- * (CC i<j, CF, SF, CS, SS). *count receives the full count even when it exceeds cap. */
+ * (CC i<j, CF, SF, CS, SS): sdl_state's Pairs vector (code/nans.h:385, filled at
+ * code/nans.cpp:1351-1536). *count receives the full count even when it exceeds cap. */
 int nans_get_pairs(nans_world *world, uint32_t scene, nans_contact_pair *out, uint32_t cap, uint32_t *count);
 
-/* Device status bits accumulated since the last call (EPA buffer overflow, ...), cleared. */
+/* Device status bits accumulated since the last call (EPA buffer overflow, ...), cleared.
+ * Stands in for the reference's printf diagnostics (code/nans.cpp:752, 1109, 1118, 1324). */
 int nans_world_status(nans_world *world, uint32_t *status_bits);
 
-/* Counts of the last step: candidate pairs after the cull and contacts. */
+/* Counts of the last step: candidate pairs after the cull and contacts. No reference
+ * counterpart (the reference tests every pair). */
 int nans_world_counts(nans_world *world, uint32_t *candidates, uint32_t *contacts);
 
 /* Large-polytope EPA statistics since upload (or the last reset): out[0] largest face list
@@ -215,10 +229,13 @@ int nans_world_counts(nans_world *world, uint32_t *candidates, uint32_t *contact
  * to the giant tier. out holds 8 entries. */
 int nans_world_epa_stats(nans_world *world, uint32_t *out, int reset);
 
-/* The world's CUDA stream (a cudaStream_t), for event timing by the caller. */
+/* The world's CUDA stream (a cudaStream_t), for event timing by the caller. No reference
+ * counterpart. */
 void *nans_world_stream(nans_world *world);
 
-/* Runs nsteps steps stage by stage with CUDA events on the world's stream between the
+/* Profiling; the reference only shows frame time and FPS in its window title
+ * (code/sdl_nans.cpp:994-1005).
+ * Runs nsteps steps stage by stage with CUDA events on the world's stream between the
  * stages and adds each stage's device time in milliseconds to stage_ms[0..5]:
  * [0] integrate sweep, [1] pair cull (3 kernels), [2] narrowphase (GJK + per-thread EPA),
  * [3] warp-tier EPA, [4] large-polytope EPA, [5] solver. */
@@ -230,10 +247,13 @@ int nans_profile_steps(nans_world *world, float dt, uint32_t nsteps, float *stag
  * the scenes without escalated EPAs, [6] solve of the rest (the step's end). */
 int nans_profile_timeline(nans_world *world, float dt, uint32_t nsteps, float *t_ms);
 
-/* Kernel launches per step on the batched path and on the plain path. */
+/* Kernel launches per step on the batched path and on the plain path. No reference
+ * counterpart. */
 int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain);
 
-/* The project sine/cosine used by the Model rebuild, evaluated on the device (n values). */
+/* The project sine/cosine used by the Model rebuild, evaluated on the device (n values); it
+ * replaces the sin/cos inside glm::rotate of the rebuild (code/nans.cpp:1913-1924), so that
+ * host and device agree bit for bit. */
 int nans_device_sincos(const float *x, float *s, float *c, uint32_t n);
 
 /* ---- differentiable rollout --------------------------------------------------------- */
@@ -318,7 +338,8 @@ int nans_solve_contacts_static(uint32_t nbodies, uint32_t ncubes, const float *d
                                const nans_contact_pair *d_pairs, uint32_t npairs, float cr, float cf,
                                int32_t iterations, float dt, void *stream);
 
-/* Description of the last failure on the calling thread ("" if none). */
+/* Description of the last failure on the calling thread ("" if none). The reference reports
+ * failures only by printf and Assert (code/nans.h:61-69). */
 const char *nans_last_error(void);
 
 #ifdef __cplusplus
