@@ -632,14 +632,16 @@ int check_status(nans_world *w)
     return NANS_OK;
 }
 
-void set_params_all(nans_world *w, const nans_step_params *p)
+int set_params_all(nans_world *w, const nans_step_params *p)
 {
     std::vector<float> cr(w->n_scenes, p->cr), cf(w->n_scenes, p->cf);
     std::vector<int> it(w->n_scenes, p->iterations);
-    cudaMemcpyAsync((void *)w->dw.sc_cr, cr.data(), cr.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream);
-    cudaMemcpyAsync((void *)w->dw.sc_cf, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream);
-    cudaMemcpyAsync((void *)w->dw.sc_iters, it.data(), it.size() * sizeof(int), cudaMemcpyHostToDevice, w->stream);
-    cudaStreamSynchronize(w->stream);
+    CK(cudaMemcpyAsync((void *)w->dw.sc_cr, cr.data(), cr.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    CK(cudaMemcpyAsync((void *)w->dw.sc_cf, cf.data(), cf.size() * sizeof(float), cudaMemcpyHostToDevice, w->stream));
+    CK(cudaMemcpyAsync((void *)w->dw.sc_iters, it.data(), it.size() * sizeof(int), cudaMemcpyHostToDevice,
+                       w->stream));
+    CK(cudaStreamSynchronize(w->stream)); // the host vectors die on return
+    return NANS_OK;
 }
 
 bool steady(const nans_world *w, float dt)
@@ -885,7 +887,11 @@ int nans_step(nans_world *w, const nans_step_params *params, float dt, uint32_t 
         return fail(NANS_ERR_INVALID_ARGUMENT, "step: dt must be finite and positive");
     CK(cudaSetDevice(w->device));
     if (params)
-        set_params_all(w, params);
+    {
+        const int rc = set_params_all(w, params);
+        if (rc)
+            return rc;
+    }
     CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), w->stream));
     for (uint32_t i = 0; i < nsteps; ++i)
     {
@@ -1047,7 +1053,11 @@ int nans_diff_forward(nans_world *w, const nans_step_params *params, float dt, u
         return fail(NANS_ERR_INVALID_ARGUMENT, "diff_forward: not available with NANS_WORLD_WARM_START");
     CK(cudaSetDevice(w->device));
     if (params)
-        set_params_all(w, params);
+    {
+        const int rc = set_params_all(w, params);
+        if (rc)
+            return rc;
+    }
     CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), w->stream));
     w->tape.clear();
     w->tape_chunk = 0;
