@@ -53,3 +53,17 @@ def test_save_ppm(tmp_path):
     lib.save_ppm(str(p), img)
     raw = p.read_bytes()
     assert raw.startswith(b"P6\n3 2\n255\n") and raw[-18:] == img.tobytes()
+
+
+def test_no_silent_fallback_without_a_device():
+    """Without a GPU every compute entry point raises: there is no CPU path to fall back to."""
+    import numpy as np
+    import torch
+    from nans_projekat_gb300 import lib
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(lib.NansError) as e:
+        lib.World()
+    assert e.value.code == 4  # NANS_ERR_CUDA
+    with pytest.raises(lib.NansError):
+        lib.device_sincos(np.zeros(4, np.float32))
