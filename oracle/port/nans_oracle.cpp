@@ -225,6 +225,7 @@ template <class T> struct Scene
 // ---------------------------------------------------------------------------------
 // integration (code/nans.cpp:50-78, 974-1018, 1331-1349)
 // ---------------------------------------------------------------------------------
+// MovementFunction (code/nans.cpp:63-70): (1/m)(F + m g (0,-1,0) - 1.5 v), 1/m in double
 template <class T> static V3<T> movement(V3<T> v, V3<T> f, T m, T invm)
 {
     T s = m * K<T>::gravity();
@@ -232,10 +233,12 @@ template <class T> static V3<T> movement(V3<T> v, V3<T> f, T m, T invm)
     V3<T> t = sub(add(f, g), mul(K<T>::damping(), v));
     return mul(invm, t);
 }
+// RotationFunction (code/nans.cpp:72-78)
 template <class T> static V3<T> rotation(V3<T> w, V3<T> tq, T invi)
 {
     return mul(invi, sub(tq, mul(K<T>::damping(), w)));
 }
+// RK4 (code/nans.cpp:50-61): Y0 + (1/6)(((K1 + 2 K2) + 2 K3) + K4)
 template <class T, class Fn> static V3<T> rk4(Fn f, T dt, V3<T> y0)
 {
     V3<T> k1 = mul(dt, f(y0));
@@ -246,6 +249,7 @@ template <class T, class Fn> static V3<T> rk4(Fn f, T dt, V3<T> y0)
     return add(y0, mul(K<T>::sixth(), s));
 }
 
+// UpdateVertices / FloorUpdateVertices (code/nans.cpp:379-407): Model times each local point
 template <class T> static void update_vertices(Body<T> &b)
 {
     b.verts.resize(b.npts);
@@ -253,6 +257,7 @@ template <class T> static void update_vertices(Body<T> &b)
         b.verts[k] = xform(b.model, b.local[k]);
 }
 
+// the two RK4 calls of IntegrateForces for one body (code/nans.cpp:974-1018)
 template <class T> static void integrate_body(Body<T> &b, T dt)
 {
     T invm = K<T>::inv_mass_rk(b.mass);
@@ -264,6 +269,7 @@ template <class T> static void integrate_body(Body<T> &b, T dt)
     b.W = rk4([&](V3<T> y) { return rotation(y, tq, invi); }, dt, b.W);
 }
 
+// IntegrateForces (code/nans.cpp:974-1018)
 template <class T> static void integrate_forces(Scene<T> &s, T dt)
 {
     for (auto &b : s.cubes)
@@ -282,6 +288,7 @@ template <class T> static void integrate_forces(Scene<T> &s, T dt)
     update_vertices(s.floor);
 }
 
+// IntegrateVelocities (code/nans.cpp:1331-1349)
 template <class T> static void integrate_velocities(Scene<T> &s, T dt)
 {
     for (auto &b : s.cubes)
@@ -296,6 +303,7 @@ template <class T> static void integrate_velocities(Scene<T> &s, T dt)
     }
 }
 
+// the render code's Model rebuild after the step (code/nans.cpp:1870-1881, 1909-1942)
 template <class T> static void rebuild(Scene<T> &s)
 {
     for (auto &b : s.cubes)
@@ -306,6 +314,7 @@ template <class T> static void rebuild(Scene<T> &s)
 // ---------------------------------------------------------------------------------
 // support maps (code/nans.cpp:409-537)
 // ---------------------------------------------------------------------------------
+// GetCubeSupport / GetFloorSupport (code/nans.cpp:409-430, 440-461): first maximum from -FLT_MAX
 template <class T> static V3<T> hull_support(const Body<T> &b, V3<T> d)
 {
     T best = K<T>::neg_flt_max();
@@ -321,6 +330,7 @@ template <class T> static V3<T> hull_support(const Body<T> &b, V3<T> d)
     }
     return r;
 }
+// GetSphereSupport (code/nans.cpp:432-438)
 template <class T> static V3<T> sphere_support(const Body<T> &b, V3<T> d)
 {
     return add(b.P, mul(b.radius, normalize(d)));
@@ -333,6 +343,7 @@ template <class T> struct PairCtx
     bool a_sphere, b_sphere;
 };
 
+// CalculateSupport (code/nans.cpp:463-519): SupA(d) - SupB(-d) by pair type
 template <class T> static Vx<T> support(const PairCtx<T> &p, V3<T> d)
 {
     V3<T> nd = mul(T(-1), d);
@@ -346,6 +357,7 @@ template <class T> static Vx<T> support(const PairCtx<T> &p, V3<T> d)
 // ---------------------------------------------------------------------------------
 enum { NoHit = 0, Found = 1, Evolving = 2 };
 
+// EvolveSimplex (code/nans.cpp:571-769) with ClosestPointOnLine / TripleCross (:539-569)
 template <class T> static int evolve(const PairCtx<T> &p, std::vector<Vx<T>> &S)
 {
     V3<T> dir = normalize(sub(p.B->P, p.A->P));
@@ -482,6 +494,7 @@ template <class T> struct Edge
     Vx<T> a, b;
 };
 
+// PushTriangle (code/nans.cpp:292-328): normal flipped away from the origin
 template <class T> static void push_face(std::vector<Face<T>> &F, const Vx<T> &a, const Vx<T> &b, const Vx<T> &c)
 {
     Face<T> f{a, b, c, normalize(cross(sub(b.P, a.P), sub(c.P, a.P)))};
@@ -490,6 +503,7 @@ template <class T> static void push_face(std::vector<Face<T>> &F, const Vx<T> &a
     F.push_back(f);
 }
 
+// PushEdge (code/nans.cpp:232-266): cancels the first stored reverse edge, else appends
 template <class T> static void push_edge(std::vector<Edge<T>> &E, const Vx<T> &a, const Vx<T> &b)
 {
     for (size_t i = 0; i < E.size(); ++i)
@@ -501,6 +515,7 @@ template <class T> static void push_edge(std::vector<Edge<T>> &E, const Vx<T> &a
     E.push_back(Edge<T>{a, b});
 }
 
+// Barycentric (code/nans.cpp:771-785)
 template <class T> static void barycentric(V3<T> p, V3<T> a, V3<T> b, V3<T> c, T *u, T *v, T *w)
 {
     V3<T> v0 = sub(b, a), v1 = sub(c, a), v2 = sub(p, a);
@@ -512,6 +527,7 @@ template <class T> static void barycentric(V3<T> p, V3<T> a, V3<T> b, V3<T> c, T
     *u = T(1) - *v - *w;
 }
 
+// IsValid (code/nans.cpp:3-17)
 template <class T> static bool finite(T x) { return !(std::isnan(x) || std::isinf(x)); }
 
 // EPA size statistics (max faces, max horizon edges, max iterations), for sizing the
@@ -538,6 +554,7 @@ static void atomic_max(std::atomic<int> &a, int v)
     }
 }
 
+// ResolveCollision (code/nans.cpp:787-904)
 template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>> &S, Contact<T> &out)
 {
     if (g_stats)
@@ -734,6 +751,7 @@ template <class T> static bool epa(const PairCtx<T> &p, const std::vector<Vx<T>>
     return false;
 }
 
+// CheckCollision (code/nans.cpp:906-966)
 template <class T> static bool check_collision(const PairCtx<T> &p, Contact<T> &c)
 {
     std::vector<Vx<T>> S;
@@ -757,6 +775,7 @@ template <class T> static bool check_collision(const PairCtx<T> &p, Contact<T> &
 // ---------------------------------------------------------------------------------
 // narrowphase driver: pair order CC, CF, SF, CS, SS (code/nans.cpp:1351-1536)
 // ---------------------------------------------------------------------------------
+// DetectCollisions (code/nans.cpp:1351-1536)
 template <class T> static void detect(Scene<T> &s)
 {
     s.pairs.clear();
@@ -786,6 +805,7 @@ template <class T> static void detect(Scene<T> &s)
 // ---------------------------------------------------------------------------------
 // sequential impulses (code/nans.cpp:1020-1329, 1538-1548)
 // ---------------------------------------------------------------------------------
+// Constraint (code/nans.cpp:1020-1329)
 template <class T> static void constraint(Scene<T> &s, Contact<T> &c, T dt)
 {
     Body<T> *A, *B;
@@ -882,6 +902,7 @@ template <class T> static void constraint(Scene<T> &s, Contact<T> &c, T dt)
 // With warm starting (the reference's TODO at its pair dedupe, code/nans.cpp:1386-1389) a
 // contact whose pair (type, IndexA, IndexB) was in contact at the previous solve starts its
 // accumulators from that solve's final values instead of zero.
+// SolveConstraints (code/nans.cpp:1538-1548)
 template <class T> static void solve(Scene<T> &s, T dt)
 {
     for (auto &c : s.pairs)
