@@ -72,6 +72,11 @@ def parse():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--no-secondary", action="store_true",
                    help="skip the plain-path and single-large-scene measurements")
+    p.add_argument("--fit-full", action="store_true",
+                   help="only the gradient fit at full size (4,096 mixed scenes x 240 steps x 50 Adam "
+                        "steps) with checkpointed rollouts; prints its own JSON line")
+    p.add_argument("--checkpoint-every", type=int, default=20,
+                   help="steps per rollout segment for --fit-full")
     return p.parse_args()
 
 
@@ -338,7 +343,7 @@ def secondary_measurements(lib, batch, device):
     return out
 
 
-def fit_measurement(lib, device, n_scenes=1024, nsteps=120, iters=20):
+def fit_measurement(lib, device, n_scenes=1024, nsteps=120, iters=20, checkpoint_every=None):
     """Gradient-based fitting through the differentiable rollout on the mixed workload (1,024
     scenes of 8-128 boxes, spheres and convex hulls, 120 steps, 20 Adam steps): the spheres'
     initial velocities are fitted so that their positions after the rollout match those of a
@@ -346,7 +351,7 @@ def fit_measurement(lib, device, n_scenes=1024, nsteps=120, iters=20):
     the loss. Gradient norm clipped at 10. (A fit of 4,096 scenes x 240 steps x 50 Adam steps
     keeps a tape of every candidate pair of every step; scenes whose bodies the reference's
     solver flings away turn every pair into a candidate, which makes that tape outgrow the
-    GPU.)"""
+    GPU; `checkpoint_every` keeps one segment's tape at a time, see --fit-full.)"""
     import torch
     from nans_projekat_gb300 import diff, scenes
     batch = scenes.mixed_batch(n_scenes, seed=4)
@@ -357,7 +362,8 @@ def fit_measurement(lib, device, n_scenes=1024, nsteps=120, iters=20):
     noise = np.zeros(V0.shape, np.float32)
     noise[n_cubes:] = rng.normal(0.0, 0.2, (V0.shape[0] - n_cubes, 3))
     with torch.no_grad():
-        target = diff.rollout(w, batch, DT, nsteps, P0, A0, V0 + torch.from_numpy(noise), W0, m, cr, cf)[0]
+        target = diff.rollout(w, batch, DT, nsteps, P0, A0, V0 + torch.from_numpy(noise), W0, m, cr, cf,
+                              checkpoint_every=checkpoint_every)[0]
     # spheres that the reference's solver flings to huge or non-finite coordinates drop out
     keep = torch.isfinite(target).all(dim=1) & (target.abs() < 1e4).all(dim=1)
     keep[:n_cubes] = False
@@ -368,7 +374,7 @@ def fit_measurement(lib, device, n_scenes=1024, nsteps=120, iters=20):
     t0 = time.perf_counter()
     for _ in range(iters):
         opt.zero_grad()
-        P = diff.rollout(w, batch, DT, nsteps, P0, A0, V, W0, m, cr, cf)[0]
+        P = diff.rollout(w, batch, DT, nsteps, P0, A0, V, W0, m, cr, cf, checkpoint_every=checkpoint_every)[0]
         ok = keep & torch.isfinite(P).all(dim=1) & (P.abs() < 1e4).all(dim=1)
         loss = ((P[ok] - target[ok]) ** 2).sum() / max(1, int(ok.sum()))
         loss.backward()
@@ -379,11 +385,14 @@ def fit_measurement(lib, device, n_scenes=1024, nsteps=120, iters=20):
     t = time.perf_counter() - t0
     bodies = int(V0.shape[0])
     w.close()
-    return {"workload": "mixed%d: %d scenes of 8-128 boxes, spheres and convex hulls" % (n_scenes, n_scenes),
-            "bodies": bodies,
-            "steps": nsteps, "adam_steps": iters, "s_per_adam_step": t / iters,
-            "forward_backward_value": bodies * nsteps * iters / t, "unit": UNIT,
-            "mean_sq_error_first": losses[0], "mean_sq_error_last": losses[-1], "fitted_spheres": int(keep.sum())}
+    out = {"workload": "mixed%d: %d scenes of 8-128 boxes, spheres and convex hulls" % (n_scenes, n_scenes),
+           "bodies": bodies,
+           "steps": nsteps, "adam_steps": iters, "s_per_adam_step": t / iters,
+           "forward_backward_value": bodies * nsteps * iters / t, "unit": UNIT,
+           "mean_sq_error_first": losses[0], "mean_sq_error_last": losses[-1], "fitted_spheres": int(keep.sum())}
+    if checkpoint_every:
+        out["checkpoint_every"] = int(checkpoint_every)
+    return out
 
 
 def differentiable_measurement(lib, device):
@@ -564,10 +573,29 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_fit_full(args):
+    """The differentiable configuration at full size: 4,096 mixed scenes, 240 steps, 50 Adam
+    steps, rollouts checkpointed every --checkpoint-every steps (one segment's tape on the GPU at
+    a time). Time-consuming; not part of the default run."""
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device")
+    torch.cuda.set_device(0)
+    from nans_projekat_gb300 import lib
+    r = fit_measurement(lib, 0, n_scenes=4096, nsteps=240, iters=50, checkpoint_every=args.checkpoint_every)
+    emit({"metric": "body-steps/s (taped forward + adjoint, Adam fit)", "value": r["forward_backward_value"],
+          "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+          "config": {"workload": r["workload"], "bodies": r["bodies"], "steps": 240, "adam_steps": 50,
+                     "checkpoint_every": args.checkpoint_every},
+          "fit": r})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference_arm(args)
+    elif args.fit_full:
+        run_fit_full(args)
     else:
         run_ours(args)
 
