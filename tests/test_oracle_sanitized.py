@@ -7,7 +7,10 @@ grow to hundreds of faces, bodies flung to huge or non-finite coordinates, FP64 
 runs. `make -C oracle port-san` builds the sanitized library; a child process loads it with the
 ASan runtime preloaded, steps the golden cases (checking each step's digest against the
 reference's) and the known-answer scenes, and any sanitizer report ends it with a non-zero
-status."""
+status.
+
+The same runner also checks the restatement built with -funsigned-char: the GPU machine is an Arm
+machine, where plain char is unsigned, and the oracle is the checker there."""
 import os
 import subprocess
 import sys
@@ -36,7 +39,23 @@ def test_oracle_is_clean_under_sanitizers():
                UBSAN_OPTIONS="print_stacktrace=1:halt_on_error=1:exitcode=24")
     r = subprocess.run([sys.executable, os.path.abspath(__file__)], cwd=ROOT, env=env, capture_output=True,
                        text=True, timeout=900)
-    assert r.returncode == 0 and "sanitized run ok" in r.stdout, (r.stdout[-2000:] + r.stderr[-4000:])
+    assert r.returncode == 0 and "oracle run ok" in r.stdout, (r.stdout[-2000:] + r.stderr[-4000:])
+
+
+def test_oracle_is_bit_exact_with_unsigned_char(tmp_path):
+    import shutil
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no g++")
+    lib = str(tmp_path / "libnans_oracle_uchar.so")
+    subprocess.run([cxx, "-O2", "-funsigned-char", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", "-fPIC",
+                    "-shared", "-pthread", "-I", os.path.join(ROOT, "oracle", "port"),
+                    "-I", os.path.join(ROOT, "oracle", "shim", "glm"),
+                    os.path.join(ROOT, "oracle", "port", "nans_oracle.cpp"), "-o", lib], check=True)
+    env = dict(os.environ, NANS_ORACLE_LIB=lib)
+    r = subprocess.run([sys.executable, os.path.abspath(__file__)], cwd=ROOT, env=env, capture_output=True,
+                       text=True, timeout=900)
+    assert r.returncode == 0 and "oracle run ok" in r.stdout, (r.stdout[-2000:] + r.stderr[-4000:])
 
 
 def _child():
@@ -44,7 +63,7 @@ def _child():
     sys.path.insert(0, os.path.join(ROOT, "tests"))
     import numpy as np
     from oracle import portbind
-    portbind.LIB_PATH = SAN_LIB
+    portbind.LIB_PATH = os.environ.get("NANS_ORACLE_LIB", SAN_LIB)
     from helpers import GOLDEN_CASES, load_golden, step_digest
     import test_known_answers
     from nans_projekat_gb300 import scenes
@@ -63,7 +82,7 @@ def _child():
     w = portbind.OracleWorld(scenes.mixed_batch(16, seed=4))
     w.set_warm(True)
     w.step(dt, 20, threads=4)
-    print("sanitized run ok")
+    print("oracle run ok")
 
 
 if __name__ == "__main__":
