@@ -12,7 +12,7 @@ built from source.
 
 CPU: the oracle gives the physical answers; the reference build (when present) gives the
 oracle's contacts bit for bit. GPU: the plain path gives the oracle's contacts bit for bit, and
-the box-sphere stress case goes through the warp EPA tier."""
+the box-sphere stress case leaves the per-thread EPA tier."""
 import numpy as np
 import pytest
 
@@ -180,5 +180,6 @@ def test_known_answers_on_the_gpu(nl, oracle_lib):
             if k == 0:
                 assert [int(t) for t in got["Type"]] == types, name
         if name == "box_sphere_epa_stress":
-            assert w.epa_stats()["warp_tier"] >= 1
+            st = w.epa_stats()  # the EPA left the per-thread polytope (20 faces)
+            assert st["warp_tier"] + st["slow_epas"] >= 1
         w.close()
