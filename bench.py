@@ -585,8 +585,8 @@ def run_fit_full(args):
     r = fit_measurement(lib, 0, n_scenes=4096, nsteps=240, iters=50, checkpoint_every=args.checkpoint_every)
     emit({"metric": "body-steps/s (taped forward + adjoint, Adam fit)", "value": r["forward_backward_value"],
           "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
-          "config": {"workload": r["workload"], "bodies": r["bodies"], "steps": 240, "adam_steps": 50,
-                     "checkpoint_every": args.checkpoint_every},
+          "config": {"workload": r["workload"], "bodies": r["bodies"], "steps": r["steps"],
+                     "adam_steps": r["adam_steps"], "checkpoint_every": args.checkpoint_every},
           "fit": r})
 
 
