@@ -1,6 +1,7 @@
-"""Hand-built known-answer cases of the detect stage: a sphere and boxes resting on the
-ground, overlapping and separated box pairs, a box-sphere pair whose EPA outgrows the
-per-thread polytope, and the symmetric poses in which the reference's GJK reports nothing.
+"""Hand-built known-answer cases of the detect stage: a sphere, boxes and a convex hull resting
+on the ground, overlapping and separated box pairs, a hull against a box, a box-sphere pair
+whose EPA outgrows the per-thread polytope, and the symmetric poses in which the reference's
+GJK reports nothing.
 
 Each case holds its physical answer (contact type, normal, depth = |PointA - PointB|, contact
 points) where the reference gives one. The reference's GJK resets its search direction to
@@ -37,6 +38,24 @@ def _balls(pos, r=0.5, m=2.0):
     return _spheres(np.array(pos, np.float64).reshape(-1, 3), r, m, sphere_moi(m, r))
 
 
+def _hull_scene(pos, k, seed, more_boxes=None):
+    """A convex hull of k points on a sphere of radius 0.5 (a shape the reference does not have;
+    its checker is the oracle), unrotated and unscaled, so its world points are pos + points."""
+    from nans_projekat_gb300 import scenes
+    pts = scenes.hull_points(scenes.SplitMix64(seed), k).astype(np.float32)
+    hull = _boxes([pos])
+    hull["MOI"] = np.float32(0.4 * 0.25)
+    cubes = hull if more_boxes is None else np.concatenate([hull, more_boxes])
+    npts = np.zeros(len(cubes), np.int32)
+    npts[0] = k
+    return Scene(cubes, _balls(NONE), ground(20.0), cube_scale=np.ones((len(cubes), 3), np.float32),
+                 hull_npts=npts, hull_pts=pts)
+
+
+def _hull_world_points(sc):
+    return sc.cubes["Position"][0].astype(np.float64) + sc.hull_pts.astype(np.float64)
+
+
 def cases():
     """name -> (scene, expected contact types in list order)."""
     g = ground(20.0)  # top face at y = 0
@@ -51,6 +70,10 @@ def cases():
         "box_sphere": (Scene(_boxes([0.0, 5.0, 0.0], [[5.0, 15.0, 25.0]]), _balls([0.8, 5.3, 0.1]), g), [CS]),
         "box_sphere_epa_stress": (Scene(_boxes([0.0, 5.0, 0.0], [[79.64529, 11.156005, 28.8532]]),
                                         _balls([-0.77295178, 5.4026804, 0.16208237], r=0.4682042), g), [CS]),
+        # convex hulls (no reference counterpart)
+        "hull_on_ground": (_hull_scene([0.1, 0.40, 0.2], 24, 5), [CF]),
+        "hull_above_ground": (_hull_scene([0.1, 0.45, 0.2], 24, 5), []),
+        "hull_box": (_hull_scene([0.0, 5.0, 0.0], 24, 6, _boxes([[0.8, 5.2, 0.1]])), [CC]),
         # the reference's answers for symmetric poses: no contact
         "sphere_above_origin": (Scene(_boxes(NONE), _balls([0.0, 0.49, 0.0]), g), []),
         "boxes_in_line": (Scene(_boxes([[0.0, 5.0, 0.0], [0.9, 5.0, 0.0]]), _balls(NONE), g), []),
@@ -102,6 +125,10 @@ def test_known_answer_on_the_oracle(oracle_lib, name):
                 s = spheres[p["IndexA"]]
                 lowest = s["Position"].astype(np.float64) - (0.0, float(s["Radius"]), 0.0)
                 assert np.allclose(p["PointA"], lowest, atol=1e-4)
+            elif sc.hull_npts is not None:
+                pts = _hull_world_points(sc)
+                lowest = pts[np.argmin(pts[:, 1])]
+                assert np.allclose(p["PointA"], lowest, atol=1e-4)
             else:
                 # a point of the box at the height of its lowest vertex (a face when level)
                 v = cubes[p["IndexA"]]["Vertices"]
@@ -113,6 +140,11 @@ def test_known_answer_on_the_oracle(oracle_lib, name):
             s = spheres[p["IndexB"]]
             d = _box_point_distance(cubes[p["IndexA"]]["Vertices"], s["Position"].astype(np.float64))
             assert abs(depth - (float(s["Radius"]) - d)) < 1e-3  # EPA tolerance
+        elif name == "hull_box":
+            # the hull's furthest point along +x against the box's face x = 0.3
+            reach = _hull_world_points(sc)[:, 0].max()
+            assert np.allclose(n, (-1.0, 0.0, 0.0), atol=1e-6)
+            assert abs(p["PointB"][0] - 0.3) < 1e-5 and abs(depth - (reach - 0.3)) < 1e-4
         elif name == "boxes_overlapping":
             # faces x = 0.5 of box 0 and x = 0.4 of box 1: 0.1 deep along x, normal towards box 0
             assert np.allclose(n, (-1.0, 0.0, 0.0), atol=1e-6)
@@ -141,6 +173,8 @@ def test_known_answer_matches_the_reference(oracle_lib, name):
         pytest.skip("reference build absent (make -C oracle ref needs the reference checkout)")
     from oracle.portbind import OracleWorld
     sc, _ = cases()[name]
+    if sc.hull_npts is not None:
+        pytest.skip("the reference has no convex hulls")
     o = OracleWorld([sc])
     r = refbind.RefWorld(sc)
     for _ in range(3):
