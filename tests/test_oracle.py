@@ -181,3 +181,15 @@ def test_reference_contacts_have_overlapping_cull_boxes(oracle_lib, seed):
             w.stage(3, dt)
             w.stage(4, dt)
     assert checked > 1000
+
+
+def test_fp32_step_against_fp64_at_short_horizons(oracle_lib):
+    """FP32 (what the GPU computes bit for bit) against an FP64 run of the same method
+    (oracle/fp64_error.py): relative position error well inside 1e-4 over the first steps,
+    before contacts that switch on in one precision and not the other make the runs diverge."""
+    from oracle.fp64_error import errors
+    from nans_projekat_gb300 import scenes as sc
+    e = errors([sc.stack_scene(0)], [1, 10, 60], threads=1)
+    assert e[1][1] < 1e-7 and e[10][1] < 1e-6 and e[60][0] < 1e-5 and e[60][1] < 1e-4
+    g = errors(sc.grid_stack_batch(8, seed=3), [1], threads=4)
+    assert g[1][1] < 1e-7
