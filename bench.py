@@ -3,8 +3,9 @@
 Workload (default): 16,384 independent scenes whose body counts are log-uniform in [4, 256]
 (seeded stacks of boxes with half-extents U[0.25, 0.75] on a ground box plus one sphere
 projectile at U[5, 25] m/s), FP32, dt = 1/60, 10 impulse iterations, restitution 0.2,
-friction 0.5; the batched path replays a CUDA graph of 60 steps. A step is one full physics
-step over every scene. value = dynamic body-steps / device time of the timed steps.
+friction 0.5; the batched path replays CUDA graphs of min(60, K) steps (the warm-up captures
+the graph, so the timed region is graph replays only). A step is one full physics step over
+every scene. value = dynamic body-steps / device time of the timed steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -31,6 +32,9 @@ UNIT = "body-steps/s"
 DT = np.float32(1.0 / 60.0)
 ALG_BYTES_SWEEP_BODY = 68 + 72     # read P,A,V,W,m,I,extents; write P,A,V,W,AABB
 ALG_BYTES_SWEEP_BOX_VERTS = 96     # world vertices written for the narrowphase
+# per body-step with the world vertices kept in registers: read P,A,V,W,F,T (72 B), m, I (8 B),
+# half-extents (12 B); write P,A,V,W (48 B), AABB (24 B)
+ALG_BYTES_SWEEP_164 = 92 + 72
 ALG_BYTES_NARROW_CAND = 12 + 4 + 2 * (16 + 16) + 2 * 96  # pair, flag, 2 shapes, 2 vertex sets
 ALG_BYTES_NARROW_HIT = 36          # contact points and normal
 
@@ -66,7 +70,7 @@ def parse():
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--scenes", type=int, default=16384)
     p.add_argument("--graph-steps", type=int, default=60)
-    p.add_argument("--e2e-steps", type=int, default=30)
+    p.add_argument("--e2e-steps", type=int, default=60)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
@@ -294,11 +298,69 @@ def run_reference_arm(args):
     emit(line)
 
 
+def single_scene_line(lib, device, scene, name, gpu_steps, cpu_steps):
+    """One scene on the plain drop-in path: GPU microseconds per step (one nans_step call per
+    step, as the reference's frame calls its step; with and without reading the bodies back
+    after each step), next to the reference step on one host core: the oracle's restatement
+    (-O2), and where the reference compiled from source is present (oracle/_ref), the
+    reference itself at -O0 as its build script compiles it and at -O2."""
+    import torch
+    dt = np.float32(scene.constants.dt)
+    w = lib.World(device=device)
+    w.upload(scene)
+    w.step(dt, 2)
+    w.download()
+    w.step(dt, 1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(gpu_steps):
+        w.step(dt, 1)
+    t_call = (time.perf_counter() - t0) / gpu_steps
+    t0 = time.perf_counter()
+    for _ in range(gpu_steps):
+        w.step(dt, 1)
+        w.download()
+    t_frame = (time.perf_counter() - t0) / gpu_steps
+    t0 = time.perf_counter()
+    w.step(dt, gpu_steps)
+    t_batch = (time.perf_counter() - t0) / gpu_steps
+    graph_steps, eager_steps = w.path_counts()
+    w.close()
+    out = {"workload": name, "bodies": int(scene.n_bodies),
+           "gpu_us_per_step": 1e6 * t_call, "gpu_us_per_step_with_download": 1e6 * t_frame,
+           "gpu_us_per_step_one_call": 1e6 * t_batch,
+           "gpu_path": "nans_step; %d of %d steps replayed from one-step CUDA graphs" % (
+               graph_steps, graph_steps + eager_steps)}
+    from oracle.portbind import OracleWorld
+    o = OracleWorld([scene])
+    t0 = time.perf_counter()
+    o.step(dt, cpu_steps, 1)
+    out["cpu_port_O2_us_per_step"] = 1e6 * (time.perf_counter() - t0) / cpu_steps
+    out["cpu_steps"] = cpu_steps
+    out["cpu_cores"] = 1
+    from oracle import refbind
+    for variant, key in (("refbig", "cpu_reference_O0_us_per_step"), ("refbig_O2", "cpu_reference_O2_us_per_step")):
+        if refbind.ref_available(variant):
+            r = refbind.RefWorld(scene, variant, rebuild=scene.rebuild_models)
+            n = max(1, cpu_steps // (4 if variant == "refbig" else 1))
+            t0 = time.perf_counter()
+            r.step(dt, n)
+            out[key] = 1e6 * (time.perf_counter() - t0) / n
+    if "cpu_reference_O0_us_per_step" not in out:
+        out["cpu_reference"] = "reference build absent on this host (no reference checkout): the port stands in"
+    out["speedup_vs_cpu_port"] = out["cpu_port_O2_us_per_step"] / out["gpu_us_per_step"]
+    return out
+
+
 def secondary_measurements(lib, batch, device):
     """Plain path vs batched path on the same scenes, and the single large scene."""
     import torch
     from nans_projekat_gb300 import scenes
     out = {}
+    out["c0_plain"] = single_scene_line(lib, device, scenes.stack_scene(0), "stack8: 8 unit cubes + 1 sphere",
+                                        600, 600)
+    out["c1_plain"] = single_scene_line(lib, device, scenes.random_scene(1),
+                                        "random4608: 4,096 boxes + 512 spheres in a 64^3 m box", 60, 3)
     # plain drop-in: one world per scene, stepped with nans_step (stage-by-stage launches and
     # one synchronisation per call), on every 256th scene of the batched workload
     sample = batch[::256]
@@ -432,6 +494,53 @@ def differentiable_measurement(lib, device):
             "forward_value": bodies * n / (t_fwd / 1e3), "unit": UNIT}
 
 
+def e2e_overlapped(lib, batch, device, steps, dist):
+    """End to end through the C ABI with the scenes split over two worlds (two streams), each
+    driven by its own host thread: every step, each world's state arrays go in from pinned host
+    memory (H2D), the world steps once (nans_batch_step with a one-step CUDA graph) and its state
+    arrays come back (D2H), so that one world's copies overlap the other world's step."""
+    import torch
+
+    def pinned(shape, dtype):
+        n = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        return torch.empty(max(1, n), dtype=torch.uint8, pin_memory=True).numpy()[:n].view(dtype).reshape(shape)
+
+    half = len(batch) // 2
+    worlds, states = [], []
+    for part in (batch[:half], batch[half:]):
+        wd = lib.World(device=device)
+        wd.upload_batch(part)
+        wd.batch_step(DT, 2, 1)
+        st = tuple(pinned((wd.n_bodies, 3), np.float32) for _ in range(4))
+        wd.get_state_arrays(out=st)
+        worlds.append(wd)
+        states.append(st)
+
+    def loop(wd, st, n):
+        for _ in range(n):
+            wd.lib.nans_world_set_state_arrays(wd.h, *[a.ctypes.data for a in st])
+            wd.batch_step(DT, 1, 1)
+            wd.lib.nans_world_get_state_arrays(wd.h, *[a.ctypes.data for a in st])
+
+    for wd, st in zip(worlds, states):  # capture the one-step graphs
+        loop(wd, st, 2)
+    torch.cuda.synchronize()
+    barrier(dist, device)
+    threads = [threading.Thread(target=loop, args=(wd, st, steps)) for wd, st in zip(worlds, states)]
+    t0 = time.perf_counter()
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    t = max_over_ranks(dist, time.perf_counter() - t0, device)
+    bodies = sum(wd.n_bodies for wd in worlds)
+    nbytes = sum(a.nbytes for st in states for a in st)
+    paths = [wd.path_counts() for wd in worlds]
+    for wd in worlds:
+        wd.close()
+    return t, bodies, nbytes, paths
+
+
 def run_ours(args):
     import torch
     dist, rank, ws = dist_init()
@@ -449,8 +558,17 @@ def run_ours(args):
     bodies = w.n_bodies
     if not args.no_autotune:
         w.autotune(DT)
-    # warm-up (also runs the first, non-graph step and captures the graph)
-    w.batch_step(DT, args.warmup, args.graph_steps)
+    # one CUDA graph covers gsteps steps; with fewer timed steps than that the graph is cut to the
+    # timed step count, so that the timed region always replays graphs
+    gsteps = max(1, min(args.graph_steps, args.steps))
+    # warm-up: W steps, then (if those did not already replay one) one more graph of gsteps steps,
+    # which captures the graph outside the timed region
+    w.batch_step(DT, args.warmup, gsteps)
+    warm_steps = args.warmup
+    if w.path_counts()[0] == 0:
+        w.batch_step(DT, gsteps, gsteps)
+        warm_steps += gsteps
+    g0, e0_ = w.path_counts()
     stream = torch.cuda.ExternalStream(w.stream, device=device)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -460,11 +578,13 @@ def run_ours(args):
     barrier(dist, device)
     torch.cuda.synchronize()
     e0.record(stream)
-    w.batch_step(DT, args.steps, args.graph_steps)
+    w.batch_step(DT, args.steps, gsteps)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier(dist, device)
     clocks = sampler.stop()
+    g1, e1_ = w.path_counts()
+    timed_graph, timed_eager = g1 - g0, e1_ - e0_
     ms = e0.elapsed_time(e1)
     ms_max = max_over_ranks(dist, ms, device)
     total_bodies = sum_over_ranks(dist, float(bodies), device)
@@ -480,11 +600,13 @@ def run_ours(args):
     peak, peak_kind = measured_peaks()
     n_boxes = int(sum(len(s.cubes) for s in batch))
     sweep_bytes = ALG_BYTES_SWEEP_BODY * bodies + ALG_BYTES_SWEEP_BOX_VERTS * n_boxes
+    sweep_bytes_164 = ALG_BYTES_SWEEP_164 * bodies
     narrow_bytes = ALG_BYTES_NARROW_CAND * n_cand + ALG_BYTES_NARROW_HIT * n_contacts
-    alg = {0: sweep_bytes, 2: narrow_bytes, 3: narrow_bytes, 4: narrow_bytes}
+    alg = {0: sweep_bytes_164, 2: narrow_bytes, 3: narrow_bytes, 4: narrow_bytes}
     dom_bytes = alg.get(dom, narrow_bytes)
     achieved = dom_bytes / (stage_ms[dom] / 1000.0) / 1e9
     sweep_gbs = sweep_bytes / (stage_ms[0] / 1000.0) / 1e9
+    sweep_gbs_164 = sweep_bytes_164 / (stage_ms[0] / 1000.0) / 1e9
 
     # end to end through the C ABI with pinned host buffers, every step: the whole dynamic
     # state in (Position, Angles, V, W as float[n][3], H2D), one step, the whole state out (D2H)
@@ -494,16 +616,22 @@ def run_ours(args):
 
     state = tuple(pinned((bodies, 3), np.float32) for _ in range(4))
     w.get_state_arrays(out=state)
+    for _ in range(2):  # capture the one-step graph
+        w.lib.nans_world_set_state_arrays(w.h, *[a.ctypes.data for a in state])
+        w.batch_step(DT, 1, 1)
+        w.lib.nans_world_get_state_arrays(w.h, *[a.ctypes.data for a in state])
     barrier(dist, device)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         w.lib.nans_world_set_state_arrays(w.h, *[a.ctypes.data for a in state])
-        w.batch_step(DT, 1, args.graph_steps)
+        w.batch_step(DT, 1, 1)
         w.lib.nans_world_get_state_arrays(w.h, *[a.ctypes.data for a in state])
-    te2e = time.perf_counter() - t0
-    te2e = max_over_ranks(dist, te2e, device)
-    e2e_value = total_bodies * args.e2e_steps / te2e
+    te2e_serial = max_over_ranks(dist, time.perf_counter() - t0, device)
     state_bytes = sum(a.nbytes for a in state)
+    e2e_serial = {"value": total_bodies * args.e2e_steps / te2e_serial, "unit": UNIT,
+                  "h2d_bytes_per_step": int(state_bytes), "d2h_bytes_per_step": int(state_bytes),
+                  "path": "one world: nans_world_set_state_arrays + nans_batch_step(1, one-step graph) + "
+                          "nans_world_get_state_arrays, pinned host, serial"}
 
     # the same through the reference's record layouts (cube 244 B, sphere 148 B)
     cubes, spheres, floors = w.download()
@@ -516,15 +644,19 @@ def run_ours(args):
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
         w.set_state(pin_c, pin_s, keep_model=True)
-        w.batch_step(DT, 1, args.graph_steps)
+        w.batch_step(DT, 1, 1)
         w.lib.nans_world_download(w.h, pin_c.ctypes.data, pin_s.ctypes.data, pin_f.ctypes.data)
     trec = max_over_ranks(dist, time.perf_counter() - t0, device)
     e2e_records = {"value": total_bodies * args.e2e_steps / trec, "unit": UNIT,
                    "h2d_bytes_per_step": int(cubes.nbytes + spheres.nbytes),
                    "d2h_bytes_per_step": int(cubes.nbytes + spheres.nbytes + pin_f.nbytes),
-                   "path": "nans_world_set_state + nans_batch_step(1) + nans_world_download (records), pinned host"}
+                   "path": "nans_world_set_state + nans_batch_step(1, one-step graph) + nans_world_download "
+                           "(records), pinned host"}
     launches_batched, _ = w.launches_per_step()
-    w.close()  # the secondary measurements build worlds of their own
+    w.close()  # the overlapped e2e and the secondary measurements build worlds of their own
+
+    te2e, e2e_bodies, e2e_bytes, e2e_paths = e2e_overlapped(lib, batch, local, args.e2e_steps, dist)
+    e2e_value = sum_over_ranks(dist, float(e2e_bodies), device) * args.e2e_steps / te2e
 
     secondary = None
     if rank == 0 and not args.no_secondary:
@@ -532,9 +664,10 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_sample_rate(batch, args.cpu_seconds, os.cpu_count() or 1, "port")
+        cpu = cpu_sample_rate(batch, args.cpu_seconds, os.cpu_count() or 1, cpu_reference_impl())
 
     if rank == 0:
+        path = "batched: %d steps from CUDA graphs of %d steps, %d eager" % (timed_graph, gsteps, timed_eager)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -542,8 +675,9 @@ def run_ours(args):
             "config": {
                 "workload": "stack_batch%d" % args.scenes, "scenes_per_gpu": args.scenes,
                 "bodies_per_gpu": bodies, "body_counts": "log-uniform [4, 256]", "dt": float(DT),
-                "iterations": 10, "restitution": 0.2, "friction": 0.5, "graph_steps": args.graph_steps,
-                "path": "batched (persistent kernels, CUDA graph)",
+                "iterations": 10, "restitution": 0.2, "friction": 0.5, "graph_steps": gsteps,
+                "path": path, "timed_graph_steps": timed_graph, "timed_eager_steps": timed_eager,
+                "warmup_steps_run": warm_steps,
                 "l2": "working set larger than L2 (%.0f MB of state, vertices and candidates)"
                       % ((bodies * 64 + n_boxes * 96 + n_cand * 60) / 1e6),
                 "candidates_per_step": n_cand, "contacts_per_step": n_contacts,
@@ -556,19 +690,25 @@ def run_ours(args):
                          "peak_source": peak_kind + " hbm_gbs",
                          "bytes_per_launch": dom_bytes,
                          "stage_ms": {n: float(x) for n, x in zip(names, stage_ms)},
-                         "sweep": {"achieved": sweep_gbs, "frac": sweep_gbs / peak,
-                                   "bytes_per_launch": sweep_bytes, "traffic": measured_traffic("k_sweep")}},
-            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(state_bytes),
-                    "d2h_bytes_per_step": int(state_bytes),
-                    "path": "nans_world_set_state_arrays + nans_batch_step(1) + nans_world_get_state_arrays, "
-                            "pinned host", "records": e2e_records},
+                         "sweep": {"basis_164B_per_body": {"achieved": sweep_gbs_164, "frac": sweep_gbs_164 / peak,
+                                                           "bytes_per_launch": sweep_bytes_164},
+                                   "basis_with_vertices": {"achieved": sweep_gbs, "frac": sweep_gbs / peak,
+                                                           "bytes_per_launch": sweep_bytes},
+                                   "traffic": measured_traffic("k_sweep")}},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(e2e_bytes),
+                    "d2h_bytes_per_step": int(e2e_bytes),
+                    "path": "two worlds of half the scenes, one host thread each: "
+                            "nans_world_set_state_arrays + nans_batch_step(1, one-step graph) + "
+                            "nans_world_get_state_arrays per step, pinned host, copies of one world "
+                            "overlapping the other's step",
+                    "graph_and_eager_steps_per_world": e2e_paths,
+                    "serial": e2e_serial, "records": e2e_records},
             "gpu_launches": int(launches_batched * args.steps),
             "secondary": secondary,
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
         emit(line)
-    w.close()
     if dist is not None:
         dist.destroy_process_group()
 

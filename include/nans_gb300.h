@@ -251,6 +251,11 @@ int nans_profile_timeline(nans_world *world, float dt, uint32_t nsteps, float *t
  * counterpart. */
 int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain);
 
+/* Steps run since the last upload by nans_step and nans_batch_step, split into those replayed
+ * from a CUDA graph and those launched kernel by kernel (the first step after an upload or a
+ * set_state, and steps left over from whole graphs). No reference counterpart. */
+int nans_world_path_counts(nans_world *world, uint64_t *graph_steps, uint64_t *eager_steps);
+
 /* The project sine/cosine used by the Model rebuild, evaluated on the device (n values); it
  * replaces the sin/cos inside glm::rotate of the rebuild (code/nans.cpp:1913-1924), so that
  * host and device agree bit for bit. */
@@ -318,9 +323,9 @@ int nans_render_scene(nans_world *world, uint32_t scene, const float eye[3], con
  * to the application's pool, or a real-time loop that forbids allocation once running. The
  * nans_world_* calls allocate with cudaMalloc; this one allocates nothing.
  *
- * It runs the sequential-impulse solve of one scene's contact list (the world's solver:
- * SolveConstraints, code/nans.cpp:1538-1548, with contacts touching disjoint bodies run in
- * parallel waves; results are bit-identical) on device buffers the caller owns:
+ * It runs the sequential-impulse solve of one scene's contact list -- the same solve as the
+ * world's step, contacts touching disjoint bodies in parallel waves, results bit-identical to
+ * solving the list in order -- on device buffers the caller owns:
  *   bodies [0, ncubes) are cubes, [ncubes, nbodies) spheres; d_position, d_velocity and
  *   d_angular_velocity hold nbodies x 3 floats, d_mass and d_moi nbodies floats; velocities
  *   are updated in place. floor (host) holds Position[3], V[3], W[3], Mass, MOI of the static
@@ -328,11 +333,12 @@ int nans_render_scene(nans_world *world, uint32_t scene, const float eye[3], con
  * Scratch lives in one fixed device array inside the library (about 2.7 MB on every GPU that
  * loads it, kept until the process exits): at most 16,384 bodies and 16,384 contacts per call,
  * larger requests fail with NANS_ERR_INVALID_ARGUMENT. Every call shares that array, so calls
- * whose kernels overlap on the GPU race; serialise them. The first call on a device looks up
- * the array's device address (once per device, with that device current); make that first
- * call before any stream capture. The call is synchronous on `stream` (a cudaStream_t, NULL for
- * the default stream). A contact naming a body outside the scene is skipped and reported as
- * NANS_ERR_INVALID_ARGUMENT. */
+ * whose kernels overlap on the GPU race; serialise them. The first call on a device (and the
+ * first after a cudaDeviceReset of it) looks up the array's device address, with that device
+ * current. The call is synchronous on `stream` (a cudaStream_t, NULL for the default stream):
+ * it waits for the solve and reads a status word back, so it cannot be recorded into a stream
+ * capture. A contact naming a body outside the scene, or the same body on both sides, is
+ * skipped and reported as NANS_ERR_INVALID_ARGUMENT. */
 int nans_solve_contacts_static(uint32_t nbodies, uint32_t ncubes, const float *d_position, const float *d_mass,
                                const float *d_moi, float *d_velocity, float *d_angular_velocity, const float *floor,
                                const nans_contact_pair *d_pairs, uint32_t npairs, float cr, float cf,

@@ -93,10 +93,14 @@ struct nans_world
     int narrow_bpsm = 0; // 0 = occupancy limit
     int solve_bpsm = 0;
 
-    cudaGraphExec_t gexec = nullptr;
+    cudaGraphExec_t gexec = nullptr;    // batched path: graph of g_steps steps
     int g_steps = 0;
     float g_dt = 0.0f;
     int g_cfg = -1;
+    cudaGraphExec_t gexec1 = nullptr;   // plain path: graph of one step
+    float g1_dt = 0.0f, g1_pdt = 0.0f;
+    int g1_flags = -1, g1_cfg = -1;
+    unsigned long long graph_steps_run = 0, eager_steps_run = 0; // nans_step / nans_batch_step
 
     // differentiable rollout: the tape lives in a chunked device arena reused across forwards
     bool tape_on = false;           // the solve records its adjoint data (s_fwd, s_maxw)
@@ -145,6 +149,12 @@ void drop_graph(nans_world *w)
     }
     w->g_steps = 0;
     w->g_cfg = -1;
+    if (w->gexec1)
+    {
+        cudaGraphExecDestroy(w->gexec1);
+        w->gexec1 = nullptr;
+    }
+    w->g1_cfg = -1;
 }
 
 int cfg_id(const nans_world *w) { return w->narrow_warps * 10000 + w->narrow_bpsm * 100 + w->solve_bpsm; }
@@ -399,6 +409,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.pair_mask, (size_t)word_acc)) || (rc = dalloc(w, L, &p_wscene, (size_t)word_acc)) ||
         (rc = dalloc(w, L, &d.epa_hist, (size_t)word_acc * 32)) ||
         (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.cull_total, 1)) ||
+        (rc = dalloc(w, L, &d.cull_max, 1)) ||
         (rc = dalloc(w, L, &d.n_cand, 1)) ||
         (rc = dalloc(w, L, &d.cand_begin, S)) || (rc = dalloc(w, L, &d.cand_end, S)) ||
         (rc = dalloc(w, L, &d.scene_late, S)) || (rc = dalloc(w, L, &d.late_list, S)) ||
@@ -435,6 +446,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.ovf_cap = kEpaOverflowCap;
     d.med_cap = kEpaMediumCap;
     d.medium_blocks = 2 * w->sm_count;
+    d.tiny_blocks = epa_tiny_grid(w->sm_count);
     d.giant_blocks = giant_grid(w->sm_count);
     d.blk_blocks = kBlockPerSm * w->sm_count;
     d.blk_face_limit = (w->flags & NANS_WORLD_TEST_GIANT_TIER) ? 0 : kBlockFaces;
@@ -472,6 +484,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     CK(cudaMemsetAsync(d.giant_scratch, 0, epa_giant_scratch_bytes(), st));
     CK(cudaMemsetAsync(d.epa_stats, 0, 8 * sizeof(unsigned), st));
     CK(cudaMemsetAsync(d.n_cand, 0, sizeof(int), st));
+    CK(cudaMemsetAsync(d.cull_max, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, S * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, S * sizeof(int), st));
     CK(cudaMemsetAsync(d.scene_late, 0, S * sizeof(int), st));
@@ -492,10 +505,14 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     int cap = (int)(w->max_cand_req ? w->max_cand_req : std::min<long long>(16LL * ndyn + 4096, INT32_MAX / 16));
     if ((rc = alloc_candidates(w, std::max(1, cap))))
         return rc;
+    // the attribute is per device and per kernel, shared by every world on the device: set it to
+    // the largest wave table any world may use, so that one world never lowers another's limit
     if ((size_t)max_bodies * sizeof(int) > 48 * 1024)
-        CK(cudaFuncSetAttribute(solve_kernel(d), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)solve_smem(w)));
+        CK(cudaFuncSetAttribute(solve_kernel(d), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmemMax));
     CK(cudaStreamSynchronize(st));
     w->uploaded = true;
+    w->graph_steps_run = 0;
+    w->eager_steps_run = 0;
     w->pending = false;
     w->pending_dt = 0.0f;
     w->model_input = (flags & NANS_UPLOAD_KEEP_MODEL) != 0;
@@ -618,18 +635,14 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
     return NANS_OK;
 }
 
+int status_code(nans_world *w, unsigned status);
+
 int check_status(nans_world *w)
 {
     unsigned status = 0;
     CK(cudaMemcpyAsync(&status, w->dw.status, sizeof(unsigned), cudaMemcpyDeviceToHost, w->stream));
     CK(cudaStreamSynchronize(w->stream));
-    if (status & ST_CANDIDATES)
-        return fail(NANS_ERR_CAPACITY, "step: more candidate pairs than the world's capacity");
-    if (status & ST_EPA_TIMEOUT)
-        return fail(NANS_ERR_EPA_CAPACITY, "step: the large-polytope EPA's grid barrier timed out");
-    if ((status & (ST_EPA_FACES | ST_EPA_EDGES)) && (w->flags & NANS_WORLD_STRICT_EPA))
-        return fail(NANS_ERR_EPA_CAPACITY, "step: an EPA polytope outgrew the large-polytope buffers");
-    return NANS_OK;
+    return status_code(w, status);
 }
 
 int set_params_all(nans_world *w, const nans_step_params *p)
@@ -649,11 +662,18 @@ bool steady(const nans_world *w, float dt)
     return w->pending && w->pending_dt == dt && !w->model_input && !w->forces_pending;
 }
 
-int ensure_graph(nans_world *w, float dt, int gsteps)
+// Captures gsteps steps into *exec (destroying what it held): the first with the previous
+// step's dt pdt0 and sweep flags flags0, the others steady.
+int capture_steps(nans_world *w, float dt, int gsteps, cudaGraphExec_t *exec, float pdt0 = 0.0f,
+                  int flags0 = SW_INTEGRATE | SW_APPLY_VEL)
 {
-    if (w->gexec && w->g_steps == gsteps && w->g_dt == dt && w->g_cfg == cfg_id(w))
-        return NANS_OK;
-    drop_graph(w);
+    if (flags0 & SW_APPLY_VEL)
+        pdt0 = dt;
+    if (*exec)
+    {
+        cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+    }
     cudaStream_t st = w->stream;
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -664,24 +684,68 @@ int ensure_graph(nans_world *w, float dt, int gsteps)
         cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st);
         cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st);
         cudaMemsetAsync(d.scene_late, 0, w->n_scenes * sizeof(int), st);
-        k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, dt, dt,
-                                                                                           SW_INTEGRATE | SW_APPLY_VEL);
+        k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(
+            d, i == 0 ? pdt0 : dt, dt, i == 0 ? flags0 : (SW_INTEGRATE | SW_APPLY_VEL));
         enqueue_cull(w);
         enqueue_narrow_solve(w, dt, nullptr);
     }
     cudaError_t e = cudaStreamEndCapture(st, &graph);
     if (e != cudaSuccess)
         return fail(NANS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-    e = cudaGraphInstantiate(&w->gexec, graph, cudaGraphInstantiateFlagUseNodePriority);
+    e = cudaGraphInstantiate(exec, graph, cudaGraphInstantiateFlagUseNodePriority);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess)
     {
-        w->gexec = nullptr;
+        *exec = nullptr;
         return fail(NANS_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     }
+    return NANS_OK;
+}
+
+int ensure_graph(nans_world *w, float dt, int gsteps)
+{
+    if (w->gexec && w->g_steps == gsteps && w->g_dt == dt && w->g_cfg == cfg_id(w))
+        return NANS_OK;
+    w->g_steps = 0;
+    w->g_cfg = -1;
+    int rc = capture_steps(w, dt, gsteps, &w->gexec);
+    if (rc)
+        return rc;
     w->g_steps = gsteps;
     w->g_dt = dt;
     w->g_cfg = cfg_id(w);
+    return NANS_OK;
+}
+
+// A one-step graph for the world's current step flags (steady or not): the plain path and
+// one-step batched calls replay it; it is captured again when the flags, dt or the previous
+// step's dt change.
+int ensure_graph1(nans_world *w, float dt)
+{
+    const int flags = sweep_flags(w);
+    const float pdt = (flags & SW_APPLY_VEL) ? w->pending_dt : 0.0f;
+    if (w->gexec1 && w->g1_dt == dt && w->g1_pdt == pdt && w->g1_flags == flags && w->g1_cfg == cfg_id(w))
+        return NANS_OK;
+    w->g1_cfg = -1;
+    int rc = capture_steps(w, dt, 1, &w->gexec1, pdt, flags);
+    if (rc)
+        return rc;
+    w->g1_dt = dt;
+    w->g1_pdt = pdt;
+    w->g1_flags = flags;
+    w->g1_cfg = cfg_id(w);
+    return NANS_OK;
+}
+
+// One step from a one-step graph.
+int step_graph1(nans_world *w, float dt)
+{
+    int rc = ensure_graph1(w, dt);
+    if (rc)
+        return rc;
+    CK(cudaGraphLaunch(w->gexec1, w->stream));
+    after_step(w, dt);
+    ++w->graph_steps_run;
     return NANS_OK;
 }
 
@@ -690,11 +754,19 @@ int batch_steps(nans_world *w, float dt, uint32_t nsteps, uint32_t gsteps)
     w->tape_valid = false;
     uint32_t done = 0;
     int rc;
+    if (gsteps == 1)
+    {
+        for (uint32_t i = 0; i < nsteps; ++i)
+            if ((rc = step_graph1(w, dt)))
+                return rc;
+        return NANS_OK;
+    }
     while (done < nsteps && !steady(w, dt))
     {
         if ((rc = step_eager(w, dt, false)))
             return rc;
         ++done;
+        ++w->eager_steps_run;
     }
     uint32_t rem = nsteps - done;
     if (gsteps > 0 && rem >= gsteps)
@@ -704,12 +776,98 @@ int batch_steps(nans_world *w, float dt, uint32_t nsteps, uint32_t gsteps)
         for (uint32_t g = 0; g < rem / gsteps; ++g)
             CK(cudaGraphLaunch(w->gexec, w->stream));
         w->steps_run += (rem / gsteps) * gsteps;
+        w->graph_steps_run += (rem / gsteps) * gsteps;
         rem %= gsteps;
     }
     for (uint32_t i = 0; i < rem; ++i)
+    {
         if ((rc = step_eager(w, dt, false)))
             return rc;
+        ++w->eager_steps_run;
+    }
     return NANS_OK;
+}
+
+// Status bits of the last steps as a return code.
+int status_code(nans_world *w, unsigned status)
+{
+    if (status & ST_CANDIDATES)
+        return fail(NANS_ERR_CAPACITY, "step: more candidate pairs than the world's capacity");
+    if (status & ST_EPA_TIMEOUT)
+        return fail(NANS_ERR_EPA_CAPACITY, "step: the large-polytope EPA's grid barrier timed out");
+    if ((status & (ST_EPA_FACES | ST_EPA_EDGES)) && (w->flags & NANS_WORLD_STRICT_EPA))
+        return fail(NANS_ERR_EPA_CAPACITY, "step: an EPA polytope outgrew the large-polytope buffers");
+    return NANS_OK;
+}
+
+// The plain path with one host synchronisation per call. The world's mutable state is copied
+// aside on the device, the steps are enqueued without reading the candidate count back (each
+// step replays a one-step CUDA graph, except the first after an upload or a set_state), and
+// the status word and the largest candidate
+// count are read once at the end. If a step found more candidate pairs than the buffers hold
+// (the cull then caps its writes and flags the step), the copy is restored, the buffers grow
+// to the largest count seen and the steps run again, synchronising after each cull as before.
+// Worlds with warm starting keep that synchronising loop: their contact cache is stamped per
+// step and cannot be rolled back.
+int plain_steps(nans_world *w, float dt, uint32_t nsteps)
+{
+    cudaStream_t st = w->stream;
+    DevWorld &d = w->dw;
+    const size_t n = (size_t)w->n_all;
+    if (!w->d_snap)
+        CK(cudaMalloc(&w->d_snap, 6 * n * sizeof(float4)));
+    float4 *bufs[6] = {d.pos, d.ang, d.vel, d.omg, d.frc, d.trq};
+    for (int i = 0; i < 6; ++i)
+        CK(cudaMemcpyAsync(w->d_snap + i * n, bufs[i], n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    const bool s_pending = w->pending, s_model = w->model_input, s_forces = w->forces_pending;
+    const float s_pdt = w->pending_dt;
+    const long long s_steps = w->steps_run;
+    const unsigned long long s_graph = w->graph_steps_run, s_eager = w->eager_steps_run;
+    CK(cudaMemsetAsync(d.cull_max, 0, sizeof(int), st));
+    int rc;
+    for (uint32_t i = 0; i < nsteps; ++i)
+    {
+        // graphs for the repeating flags (steady steps, and steps after a download or a state
+        // write); the first step after an upload or set_state (forces, input Model) is eager
+        if (!(sweep_flags(w) & (SW_FORCES | SW_MODEL_INPUT)))
+        {
+            if ((rc = step_graph1(w, dt)))
+                return rc;
+        }
+        else
+        {
+            if ((rc = step_eager(w, dt, false)))
+                return rc;
+            ++w->eager_steps_run;
+        }
+    }
+    unsigned hdr[2] = {0u, 0u};
+    CK(cudaMemcpyAsync(&hdr[0], d.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(&hdr[1], d.cull_max, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    if (!(hdr[0] & ST_CANDIDATES))
+        return status_code(w, hdr[0]);
+    // roll back, grow, run again
+    for (int i = 0; i < 6; ++i)
+        CK(cudaMemcpyAsync(bufs[i], w->d_snap + i * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    w->pending = s_pending;
+    w->model_input = s_model;
+    w->forces_pending = s_forces;
+    w->pending_dt = s_pdt;
+    w->steps_run = s_steps;
+    w->graph_steps_run = s_graph;
+    w->eager_steps_run = s_eager;
+    const long long need = (long long)(int)hdr[1];
+    if ((rc = alloc_candidates(w, (int)std::min<long long>(need + need / 4 + 1024, INT32_MAX / 16))))
+        return rc;
+    CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
+    for (uint32_t i = 0; i < nsteps; ++i)
+    {
+        if ((rc = step_eager(w, dt, true)))
+            return rc;
+        ++w->eager_steps_run;
+    }
+    return check_status(w);
 }
 
 int valid_dt(float dt) { return std::isfinite(dt) && dt > 0.0f; }
@@ -814,6 +972,10 @@ int nans_world_create(const nans_world_desc *desc, nans_world **out)
         e = cudaEventCreateWithFlags(&w->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess)
         e = cudaDeviceGetAttribute(&w->sm_count, cudaDevAttrMultiProcessorCount, w->device);
+    if (e == cudaSuccess)
+        e = (cudaError_t)narrow_kernel_attrs();
+    if (e == cudaSuccess)
+        e = (cudaError_t)large_kernel_attrs();
     if (e != cudaSuccess)
     {
         if (w->stream)
@@ -893,11 +1055,14 @@ int nans_step(nans_world *w, const nans_step_params *params, float dt, uint32_t 
             return rc;
     }
     CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), w->stream));
+    if (!flags_world_warm(w))
+        return plain_steps(w, dt, nsteps);
     for (uint32_t i = 0; i < nsteps; ++i)
     {
         int rc = step_eager(w, dt, true);
         if (rc)
             return rc;
+        ++w->eager_steps_run;
     }
     return check_status(w);
 }
@@ -1496,6 +1661,17 @@ int nans_profile_timeline(nans_world *w, float dt, uint32_t nsteps, float *t_ms)
     for (int i = 0; i < 8; ++i)
         cudaEventDestroy(ev[i]);
     return check_status(w);
+}
+
+int nans_world_path_counts(nans_world *w, uint64_t *graph_steps, uint64_t *eager_steps)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "path_counts: null world");
+    if (graph_steps)
+        *graph_steps = w->graph_steps_run;
+    if (eager_steps)
+        *eager_steps = w->eager_steps_run;
+    return NANS_OK;
 }
 
 int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)

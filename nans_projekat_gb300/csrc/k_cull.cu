@@ -162,6 +162,7 @@ __global__ void __launch_bounds__(1024) k_cull_scan(DevWorld w, int nblocks)
     {
         long long n = carry;
         *w.cull_total = (int)min(n, (long long)INT32_MAX);
+        *w.cull_max = max(*w.cull_max, *w.cull_total);
         if (n > w.cand_cap)
         {
             atomicOr(w.status, (unsigned)ST_CANDIDATES);

@@ -820,14 +820,16 @@ int giant_grid(int sm_count)
     return std::min(per * sm_count, kGiantMaxWarps / (kLargeThreads / 32));
 }
 
+// The block tier's group table in dynamic shared memory beyond 48 KB. The attribute belongs to
+// the current device's context, so every world sets it for its own device when it is created.
+int large_kernel_attrs()
+{
+    return (int)cudaFuncSetAttribute(k_epa_block, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(GroupTable));
+}
+
 int launch_narrow_big(cudaStream_t st, const DevWorld &w)
 {
-    static bool attrs = false;
-    if (!attrs)
-    {
-        cudaFuncSetAttribute(k_epa_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(GroupTable));
-        attrs = true;
-    }
     cudaLaunchAttribute prio;
     prio.id = cudaLaunchAttributePriority;
     prio.val.priority = tier_priority();

@@ -978,13 +978,12 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(
 
 static size_t medium_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }
 
-static void narrow_attrs()
+// The warp tier's dynamic shared memory beyond 48 KB. The attribute belongs to the current
+// device's context, so every world sets it for its own device when it is created.
+int narrow_kernel_attrs()
 {
-    static bool done = false;
-    if (done)
-        return;
-    cudaFuncSetAttribute(k_epa_medium<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)medium_smem(4));
-    done = true;
+    return (int)cudaFuncSetAttribute(k_epa_medium<4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)medium_smem(4));
 }
 
 int narrow_blocks_per_sm(int warps)
@@ -995,25 +994,18 @@ int narrow_blocks_per_sm(int warps)
     return per;
 }
 
-static int epa_tiny_grid()
+int epa_tiny_grid(int sm_count)
 {
-    static int grid = 0;
-    if (grid == 0)
-    {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_epa_tiny, kTinyThreads, 0);
-        grid = std::max(1, per) * std::max(1, sms);
-    }
-    return grid;
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_epa_tiny, kTinyThreads, 0);
+    return std::max(1, per) * std::max(1, sm_count);
 }
 
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w)
 {
     k_gjk<<<grid, kGjkThreads, 0, st>>>(w);
     k_gjk_long<<<grid, kGjkThreads, 0, st>>>(w);
-    k_epa_tiny<<<epa_tiny_grid(), kTinyThreads, 0, st>>>(w);
+    k_epa_tiny<<<w.tiny_blocks, kTinyThreads, 0, st>>>(w);
 }
 
 int tier_priority()
@@ -1033,7 +1025,6 @@ int tier_priority()
 // solve pass that becomes ready at the same time.
 void launch_epa_medium(cudaStream_t st, const DevWorld &w)
 {
-    narrow_attrs();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(w.medium_blocks);
     cfg.blockDim = dim3(128);

@@ -73,6 +73,7 @@ struct DevWorld
     int n_words;
     int *block_hits;                    // per cull block: culled pairs, then candidate offset
     int *cull_total;                    // candidates before the capacity clamp
+    int *cull_max;                      // largest cull_total since the host last cleared it
     int *cand_begin, *cand_end;         // per scene candidate range
     int *scene_late;                    // per scene: 1 if a candidate went beyond the per-thread
                                         // EPA tier (solved after those tiers)
@@ -91,6 +92,7 @@ struct DevWorld
     int *med_cand;                      // candidates queued for the warp tier
     int2 *long_cand;                    // candidates whose GJK needs the long pass: (c, n | it << 8)
     int medium_blocks;                  // warp-tier grid
+    int tiny_blocks;                    // per-thread EPA grid (resident blocks on every SM)
     int ovf_cap;                        // block-EPA queue capacity
     int *ovf_cand;                      // candidates queued for the block tier
     unsigned char *blk_arena;           // block-tier polytope buffers, one per block

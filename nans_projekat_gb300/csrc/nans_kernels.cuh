@@ -83,6 +83,9 @@ int giant_grid(int sm_count);
 void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w);
 int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaError_t
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
+int epa_tiny_grid(int sm_count);   // resident blocks of the per-thread EPA on sm_count SMs
+int narrow_kernel_attrs();         // per-device kernel attributes (cudaError_t), set at world creation
+int large_kernel_attrs();
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
 int tier_priority(); // the device's greatest stream priority
 int solve_threads(int max_scene_bodies);

@@ -55,9 +55,49 @@ static_assert(kOffK % 4 == 0, "constants must be 16-byte aligned");
 // About 2.7 MB, resident on each device that loads the library.
 static __device__ __align__(256) unsigned g_solve_scratch[kScratchWords];
 
-// Device address of g_solve_scratch per device, taken once with that device current.
+// Device address of g_solve_scratch per device, looked up once with that device current. A
+// cudaDeviceReset destroys the device's context, and the library's module, with the array in
+// it, is loaded again in the next context, possibly at another address. So each entry also keeps
+// the id of the context it was taken in, and the address is looked up again when the device's
+// current context has another id.
+struct ScratchAddr
+{
+    void *ptr;
+    unsigned long long ctx;
+};
 std::mutex g_setup_mutex;
-void *g_scratch_addr[64] = {};
+ScratchAddr g_scratch_addr[64] = {};
+
+typedef int (*CtxGetCurrentFn)(void **);
+typedef int (*CtxGetIdFn)(void *, unsigned long long *);
+
+// Id of the calling thread's current context through the driver's cuCtxGetCurrent and
+// cuCtxGetId (CUDA 12.0 and later); 0 when the driver does not provide them. Call with
+// g_setup_mutex held.
+unsigned long long current_context_id()
+{
+    static bool looked_up = false;
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    if (!looked_up)
+    {
+        looked_up = true;
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (CtxGetCurrentFn)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (CtxGetIdFn)f;
+    }
+    void *ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current && get_id && get_current(&ctx) == 0 && ctx && get_id(ctx, &id) == 0)
+        return id;
+    return 0;
+}
 
 struct Floor
 {
@@ -81,7 +121,8 @@ __device__ __forceinline__ void st3(float *a, int i, v3 v)
 }
 
 // Body index of each side of a contact record (code/nans.h:338-372); -1 = the floor,
-// -2 = an index outside the scene.
+// -2 = a contact that is skipped and reported: an index outside the scene, or both sides the
+// same body.
 __device__ __forceinline__ void sides(const Bodies &B, const nans_contact_pair &c, int &a, int &b)
 {
     int t = c.Type;
@@ -93,7 +134,9 @@ __device__ __forceinline__ void sides(const Bodies &B, const nans_contact_pair &
     int nsph = B.nbodies - B.ncubes;
     bool a_ok = c.IndexA >= 0 && (a_sphere ? c.IndexA < nsph : c.IndexA < B.ncubes);
     bool b_ok = b_floor || (c.IndexB >= 0 && (b_sphere ? c.IndexB < nsph : c.IndexB < B.ncubes));
-    if (t < 0 || t > 4 || !a_ok || !b_ok)
+    // a contact whose two sides are one body: the sequential solve would interleave the two
+    // sides' updates on that body, which the per-side loads and stores below cannot reproduce
+    if (t < 0 || t > 4 || !a_ok || !b_ok || (b >= 0 && a == b))
         a = b = -2;
 }
 
@@ -306,17 +349,24 @@ extern "C" int nans_solve_contacts_static(uint32_t nbodies, uint32_t ncubes, con
         return static_fail(NANS_ERR_CUDA, "nans_solve_contacts_static: no current CUDA device");
     void *scratch = nullptr;
     {
-        // once per device, with that device current: the device address of the scratch array
+        // set-up, once per device (again after a reset of that device), with that device
+        // current: the device address of the scratch array. cudaSetDevice makes the device's
+        // primary context current on this thread, so that its id can be read.
         std::lock_guard<std::mutex> lock(g_setup_mutex);
-        if (!g_scratch_addr[dev])
+        e = cudaSetDevice(dev);
+        if (e != cudaSuccess)
+            return static_fail(NANS_ERR_CUDA, "nans_solve_contacts_static: cudaSetDevice failed");
+        const unsigned long long ctx = current_context_id();
+        if (!g_scratch_addr[dev].ptr || ctx == 0 || ctx != g_scratch_addr[dev].ctx)
         {
             void *p = nullptr;
             e = cudaGetSymbolAddress(&p, g_solve_scratch);
             if (e != cudaSuccess || !p)
                 return static_fail(NANS_ERR_CUDA, "nans_solve_contacts_static: cudaGetSymbolAddress failed");
-            g_scratch_addr[dev] = p;
+            g_scratch_addr[dev].ptr = p;
+            g_scratch_addr[dev].ctx = ctx;
         }
-        scratch = g_scratch_addr[dev];
+        scratch = g_scratch_addr[dev].ptr;
     }
     Bodies B{d_position, d_mass, d_moi, d_velocity, d_angular_velocity, (int)nbodies, (int)ncubes};
     // floor: Position[3], V[3], W[3], Mass, MOI
@@ -327,15 +377,16 @@ extern "C" int nans_solve_contacts_static(uint32_t nbodies, uint32_t ncubes, con
     e = cudaGetLastError();
     if (e != cudaSuccess)
         return static_fail(NANS_ERR_CUDA, "nans_solve_contacts_static: kernel launch failed");
-    e = cudaStreamSynchronize(st);
+    // the status word (scratch word 0), read on the caller's stream
+    unsigned err = 0;
+    e = cudaMemcpyAsync(&err, scratch, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess)
+        e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
         return static_fail(NANS_ERR_CUDA, "nans_solve_contacts_static: kernel failed");
-    unsigned err = 0;
-    e = cudaMemcpyFromSymbol(&err, g_solve_scratch, sizeof(unsigned), 0, cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess)
-        return static_fail(NANS_ERR_CUDA, "nans_solve_contacts_static: reading the status word failed");
     if (err & 1u)
         return static_fail(NANS_ERR_INVALID_ARGUMENT,
-                           "nans_solve_contacts_static: a contact names a body outside the scene (skipped)");
+                           "nans_solve_contacts_static: a contact names a body outside the scene, or the same "
+                           "body on both sides (skipped)");
     return NANS_OK;
 }

@@ -41,6 +41,7 @@ EXPORTS = (
     "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps", "nans_profile_timeline",
     "nans_world_epa_stats", "nans_solve_contacts_static", "nans_diff_forward", "nans_diff_backward",
     "nans_diff_tape_info", "nans_world_set_state_arrays", "nans_world_get_state_arrays", "nans_render_scene",
+    "nans_world_path_counts",
 )
 
 
@@ -95,6 +96,7 @@ def load(path=LIB_PATH):
     L.nans_world_stream.argtypes = [_P]
     L.nans_world_stream.restype = _P
     L.nans_launches_per_step.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(_U)]
+    L.nans_world_path_counts.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
     L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
     L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
     L.nans_profile_timeline.argtypes = [_P, _F, _U, _P]
@@ -280,6 +282,12 @@ class World:
         a, b = _U(), _U()
         _check(self.lib.nans_launches_per_step(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def path_counts(self):
+        """(steps replayed from CUDA graphs, steps launched eagerly) since the last upload."""
+        g, e = ctypes.c_uint64(), ctypes.c_uint64()
+        _check(self.lib.nans_world_path_counts(self.h, ctypes.byref(g), ctypes.byref(e)))
+        return g.value, e.value
 
     def profile(self, dt, n):
         """Device milliseconds per stage summed over n steps: sweep, cull, narrowphase

@@ -14,7 +14,7 @@ from nans_projekat_gb300.types import CUBE_DTYPE, SPHERE_DTYPE, PAIR_DTYPE
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
-VARIANTS = ("ref16", "refbig", "ref_pristine", "ref16_O2")
+VARIANTS = ("ref16", "refbig", "ref_pristine", "ref16_O2", "refbig_O2")
 
 
 def ref_path(variant="refbig"):

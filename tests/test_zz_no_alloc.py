@@ -4,7 +4,8 @@ layer does, or an engine with a fixed memory pool).
 
 It is called through the C ABI on device buffers the test owns and must give the same
 velocities, bit for bit, as the solve inside the existing nans_step entry point, on two
-calls in a row (the second call reuses the library's static scratch array).
+calls in a row (the second call reuses the library's static scratch array), and the second call
+must leave the device's free memory unchanged.
 This file is named so that pytest collects it last.
 """
 import numpy as np
@@ -69,15 +70,51 @@ def test_static_solve_matches_world_step(oracle_lib):
         floor = np.concatenate([f["Position"], f["V"], f["W"], [f["Mass"], f["MOI"]]]).astype(np.float32)
         c = sc.constants
         torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info(dev)[0]
         lib.solve_contacts_static(len(pos), len(sc.cubes), t_pos.data_ptr(), t_mass.data_ptr(), t_moi.data_ptr(),
                                   t_vel.data_ptr(), t_omg.data_ptr(), floor, t_pairs.data_ptr(), len(pairs),
                                   c.cr, c.cf, c.iterations, DT, None)
+        torch.cuda.synchronize()
+        free_after = torch.cuda.mem_get_info(dev)[0]
         calls += 1
+        if calls == 2:
+            # the first call may load the kernel's module (lazy loading takes device memory once);
+            # the second must not change the device's free memory at all
+            assert free_after == free_before, (free_before, free_after)
         got_v = t_vel.cpu().numpy()
         got_w = t_omg.cpu().numpy()
         assert canon(got_v) == canon(v_ref.astype(np.float32)), sc.name
         assert canon(got_w) == canon(w_ref.astype(np.float32)), sc.name
     assert calls == 2
+
+
+def test_static_solve_rejects_same_body_contacts():
+    """A cube-cube contact naming one body on both sides is skipped and reported: the sequential
+    solve interleaves both sides' updates on that body, which a per-side solve cannot reproduce."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required")
+    from nans_projekat_gb300 import lib
+    from nans_projekat_gb300.types import PAIR_DTYPE
+    dev = torch.device("cuda", 0)
+    pos = torch.zeros(6, device=dev)
+    vel = torch.ones(6, device=dev)
+    omg = torch.zeros(6, device=dev)
+    mass = torch.ones(2, device=dev)
+    moi = torch.ones(2, device=dev)
+    pair = np.zeros(1, PAIR_DTYPE)
+    pair["Type"] = 0  # cube-cube
+    pair["IndexA"] = 1
+    pair["IndexB"] = 1
+    pair["N"] = (0.0, 1.0, 0.0)
+    t_pair = torch.from_numpy(np.frombuffer(pair.tobytes(), np.uint8).copy()).to(dev)
+    floor = np.zeros(11, np.float32)
+    floor[9] = floor[10] = 1.0
+    with pytest.raises(lib.NansError) as e:
+        lib.solve_contacts_static(2, 2, pos.data_ptr(), mass.data_ptr(), moi.data_ptr(), vel.data_ptr(),
+                                  omg.data_ptr(), floor, t_pair.data_ptr(), 1, 0.2, 0.5, 10, DT, None)
+    assert e.value.code == 1 and "same body" in str(e.value)
+    assert torch.equal(vel, torch.ones(6, device=dev))
 
 
 def test_static_solve_rejects_oversized_requests():
