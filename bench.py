@@ -3,8 +3,8 @@
 Workload (default): 16,384 independent scenes whose body counts are log-uniform in [4, 256]
 (seeded stacks of boxes with half-extents U[0.25, 0.75] on a ground box plus one sphere
 projectile at U[5, 25] m/s), FP32, dt = 1/60, 10 impulse iterations, restitution 0.2,
-friction 0.5; the batched path replays CUDA graphs of min(60, K) steps (the warm-up captures
-the graph, so the timed region is graph replays only). A step is one full physics step over
+friction 0.5; the batched path replays CUDA graphs of min(60, K) steps (captured after the
+warm-up steps, so the timed region is graph replays only). A step is one full physics step over
 every scene. value = dynamic body-steps / device time of the timed steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -561,13 +561,10 @@ def run_ours(args):
     # one CUDA graph covers gsteps steps; with fewer timed steps than that the graph is cut to the
     # timed step count, so that the timed region always replays graphs
     gsteps = max(1, min(args.graph_steps, args.steps))
-    # warm-up: W steps, then (if those did not already replay one) one more graph of gsteps steps,
-    # which captures the graph outside the timed region
+    # warm-up: W steps, then the capture of the graph the timed steps replay (no step runs)
     w.batch_step(DT, args.warmup, gsteps)
+    w.prepare(DT, gsteps)
     warm_steps = args.warmup
-    if w.path_counts()[0] == 0:
-        w.batch_step(DT, gsteps, gsteps)
-        warm_steps += gsteps
     g0, e0_ = w.path_counts()
     stream = torch.cuda.ExternalStream(w.stream, device=device)
     e0 = torch.cuda.Event(enable_timing=True)

@@ -181,6 +181,12 @@ int nans_step(nans_world *world, const nans_step_params *params, float dt, uint3
  * steps one). */
 int nans_batch_step(nans_world *world, float dt, uint32_t nsteps, uint32_t graph_steps);
 
+/* Captures, without running a step, the CUDA graph that the next nans_batch_step(world, dt, n,
+ * graph_steps) call would replay first (graph capture and instantiation cost milliseconds for
+ * large worlds; a caller that times its steps, or runs them under a deadline, prepares the
+ * graph beforehand). No reference counterpart. */
+int nans_batch_prepare(nans_world *world, float dt, uint32_t graph_steps);
+
 /* Picks narrowphase / solver launch shapes by timing a few steps on the world's own
  * scenes; the state is restored afterwards. No reference counterpart. */
 int nans_batch_autotune(nans_world *world, float dt);
@@ -250,6 +256,18 @@ int nans_profile_timeline(nans_world *world, float dt, uint32_t nsteps, float *t
 /* Kernel launches per step on the batched path and on the plain path. No reference
  * counterpart. */
 int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain);
+
+/* The launch parameters nans_batch_autotune chose (or the defaults): out[0] the per-thread EPA's
+ * iteration budget before an EPA is set aside for the resume pass (65 = no budget), out[1] GJK
+ * blocks per SM (0 = as many as fit), out[2] solver threads per scene in the first solve pass,
+ * out[3] solver threads per late scene, out[4] candidates the autotuner timed, out[5] the
+ * chosen candidate's microseconds per step. No reference counterpart. */
+int nans_world_tuning(nans_world *world, int32_t *out);
+
+/* Sets the launch parameters out[0..3] of nans_world_tuning (for instance a choice of the
+ * autotuner kept from an earlier run); results do not depend on them. No reference
+ * counterpart. */
+int nans_world_set_tuning(nans_world *world, const int32_t *in);
 
 /* Steps run since the last upload by nans_step and nans_batch_step, split into those replayed
  * from a CUDA graph and those launched kernel by kernel (the first step after an upload or a

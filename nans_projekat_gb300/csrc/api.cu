@@ -51,6 +51,7 @@ void nans::set_last_error(const char *msg) { g_err = msg; }
 namespace
 {
 constexpr int kSweepThreads = 256;
+constexpr int kTuneSteps = 20;       // timed steps per autotuner candidate
 constexpr size_t kSolveSmemMax = 200 * 1024;
 } // namespace
 
@@ -89,14 +90,22 @@ struct nans_world
     bool forces_pending = false;
     long long steps_run = 0;
 
-    int narrow_warps = 4;
-    int narrow_bpsm = 0; // 0 = occupancy limit
-    int solve_bpsm = 0;
+    int narrow_bpsm = 0;     // GJK blocks per SM (0 = occupancy limit)
+    int gjk_cap_blocks = 1;  // GJK blocks the world's pairs can keep busy
+    int solve_threads0 = 0;  // solver threads per scene, first pass (0 = by the largest scene)
+    int solve_threads1 = kSolveLateThreads; // solver threads per late scene
+    int tune_trials = 0;
+    float tune_ms = 0.0f;
+    unsigned char *d_snap_hist = nullptr;
+    size_t snap_n = 0, snap_hist_n = 0;  // bodies / bytes the snapshot buffers hold
 
-    cudaGraphExec_t gexec = nullptr;    // batched path: graph of g_steps steps
+    cudaGraphExec_t gexec = nullptr;    // batched path: graph of g_steps steady steps
     int g_steps = 0;
     float g_dt = 0.0f;
     int g_cfg = -1;
+    cudaGraphExec_t gexec_b = nullptr;  // batched path: the same whose first step has flags gb_flags
+    int gb_steps = 0, gb_flags = -1, gb_cfg = -1;
+    float gb_dt = 0.0f;
     cudaGraphExec_t gexec1 = nullptr;   // plain path: graph of one step
     float g1_dt = 0.0f, g1_pdt = 0.0f;
     int g1_flags = -1, g1_cfg = -1;
@@ -149,6 +158,12 @@ void drop_graph(nans_world *w)
     }
     w->g_steps = 0;
     w->g_cfg = -1;
+    if (w->gexec_b)
+    {
+        cudaGraphExecDestroy(w->gexec_b);
+        w->gexec_b = nullptr;
+    }
+    w->gb_cfg = -1;
     if (w->gexec1)
     {
         cudaGraphExecDestroy(w->gexec1);
@@ -157,16 +172,19 @@ void drop_graph(nans_world *w)
     w->g1_cfg = -1;
 }
 
-int cfg_id(const nans_world *w) { return w->narrow_warps * 10000 + w->narrow_bpsm * 100 + w->solve_bpsm; }
+int cfg_id(const nans_world *w)
+{
+    return ((w->dw.tiny_budget * 64 + w->narrow_bpsm) * 1024 + w->solve_threads0) * 1024 + w->solve_threads1;
+}
 
 int narrow_grid(nans_world *w)
 {
-    int per = narrow_blocks_per_sm(w->narrow_warps);
+    int per = narrow_blocks_per_sm(4);
     if (per < 1)
         per = 1;
     if (w->narrow_bpsm > 0)
         per = std::min(per, w->narrow_bpsm);
-    return per * w->sm_count;
+    return std::min(per * w->sm_count, w->gjk_cap_blocks);
 }
 
 size_t solve_smem(const nans_world *w) { return (size_t)std::max(1, w->max_scene_bodies) * sizeof(int); }
@@ -197,6 +215,11 @@ int alloc_candidates(nans_world *w, int cap)
         d.s_fwd = w->fwd_buf;
     }
     if ((rc = dalloc(w, L, &d.cand_pidx, cap)))
+        return rc;
+    // resume slots for half the candidates: a 4-iteration budget sets aside about a fifth of the
+    // EPAs on the stack workload; beyond the slots, EPAs run to their end in the first pass
+    d.res_cap = std::max(1, std::min(cap / 2, kResumeSlotsMax));
+    if ((rc = dalloc(w, L, &d.epa_res, epa_resume_words() * (size_t)d.res_cap)))
         return rc;
     return NANS_OK;
 }
@@ -445,10 +468,19 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.model_in = w->d_model_in;
     d.ovf_cap = kEpaOverflowCap;
     d.med_cap = kEpaMediumCap;
-    d.medium_blocks = 2 * w->sm_count;
-    d.tiny_blocks = epa_tiny_grid(w->sm_count);
-    d.giant_blocks = giant_grid(w->sm_count);
-    d.blk_blocks = kBlockPerSm * w->sm_count;
+    // persistent grids: resident blocks on every SM, but no more blocks than the world's pairs
+    // (an upper bound of its candidates) can keep busy, so that a small scene's step does not
+    // launch hundreds of blocks that exit at once
+    const long long maxc = std::max(1LL, pair_acc);
+    auto upto = [&](long long per_block, int resident) {
+        return (int)std::max(1LL, std::min<long long>(resident, (maxc + per_block - 1) / per_block));
+    };
+    w->gjk_cap_blocks = upto(128, INT32_MAX);
+    d.medium_blocks = upto(4, 2 * w->sm_count);
+    d.tiny_blocks = upto(64, epa_tiny_grid(w->sm_count));
+    d.tiny_budget = kTinyBudgetDefault;
+    d.giant_blocks = std::min(giant_grid(w->sm_count), upto(1, INT32_MAX) < 4096 ? 16 : INT32_MAX);
+    d.blk_blocks = upto(1, kBlockPerSm * w->sm_count);
     d.blk_face_limit = (w->flags & NANS_WORLD_TEST_GIANT_TIER) ? 0 : kBlockFaces;
     d.giant_cap = kGiantQueueCap;
     cudaStream_t st = w->stream;
@@ -556,7 +588,8 @@ cudaError_t enqueue_narrow_solve(nans_world *w, float dt, cudaEvent_t *tl)
     e = (cudaError_t)launch_narrow_big(st2, w->dw);
     if (tl)
         cudaEventRecord(tl[2], st2);
-    launch_solve(w->dw, w->n_scenes, solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
+    launch_solve(w->dw, w->n_scenes, w->solve_threads0 ? w->solve_threads0 : solve_threads(w->max_scene_bodies),
+                 solve_smem(w), st, dt, 0);
     if (tl)
         cudaEventRecord(tl[3], st);
     cudaError_t e2 = cudaEventRecord(w->ev_join, st2);
@@ -564,7 +597,7 @@ cudaError_t enqueue_narrow_solve(nans_world *w, float dt, cudaEvent_t *tl)
         e2 = cudaStreamWaitEvent(st, w->ev_join, 0);
     // the late scenes (few, and mostly the larger ones) solve with wider blocks: their waves
     // are on the step's critical path
-    launch_solve(w->dw, std::min(w->n_scenes, 2 * w->sm_count), kSolveLateThreads, solve_smem(w), st, dt, 1);
+    launch_solve(w->dw, std::min(w->n_scenes, 2 * w->sm_count), w->solve_threads1, solve_smem(w), st, dt, 1);
     if (tl)
         cudaEventRecord(tl[4], st);
     return e != cudaSuccess ? e : e2;
@@ -702,18 +735,39 @@ int capture_steps(nans_world *w, float dt, int gsteps, cudaGraphExec_t *exec, fl
     return NANS_OK;
 }
 
-int ensure_graph(nans_world *w, float dt, int gsteps)
+// The gsteps-step graph for the world's current state: the steady graph, or (after a download
+// or a state-array write, whose first step does not apply a pending velocity) the graph whose
+// first step runs with the world's current sweep flags. Returns it in *exec.
+int ensure_graph(nans_world *w, float dt, int gsteps, cudaGraphExec_t *exec)
 {
-    if (w->gexec && w->g_steps == gsteps && w->g_dt == dt && w->g_cfg == cfg_id(w))
+    int rc;
+    if (steady(w, dt))
+    {
+        if (!(w->gexec && w->g_steps == gsteps && w->g_dt == dt && w->g_cfg == cfg_id(w)))
+        {
+            w->g_steps = 0;
+            w->g_cfg = -1;
+            if ((rc = capture_steps(w, dt, gsteps, &w->gexec)))
+                return rc;
+            w->g_steps = gsteps;
+            w->g_dt = dt;
+            w->g_cfg = cfg_id(w);
+        }
+        *exec = w->gexec;
         return NANS_OK;
-    w->g_steps = 0;
-    w->g_cfg = -1;
-    int rc = capture_steps(w, dt, gsteps, &w->gexec);
-    if (rc)
-        return rc;
-    w->g_steps = gsteps;
-    w->g_dt = dt;
-    w->g_cfg = cfg_id(w);
+    }
+    const int flags = sweep_flags(w);
+    if (!(w->gexec_b && w->gb_steps == gsteps && w->gb_dt == dt && w->gb_flags == flags && w->gb_cfg == cfg_id(w)))
+    {
+        w->gb_cfg = -1;
+        if ((rc = capture_steps(w, dt, gsteps, &w->gexec_b, 0.0f, flags)))
+            return rc;
+        w->gb_steps = gsteps;
+        w->gb_dt = dt;
+        w->gb_flags = flags;
+        w->gb_cfg = cfg_id(w);
+    }
+    *exec = w->gexec_b;
     return NANS_OK;
 }
 
@@ -761,7 +815,9 @@ int batch_steps(nans_world *w, float dt, uint32_t nsteps, uint32_t gsteps)
                 return rc;
         return NANS_OK;
     }
-    while (done < nsteps && !steady(w, dt))
+    // the first step after an upload or set_state (external forces, input Model) runs eagerly;
+    // whole blocks of gsteps steps replay graphs, the rest replays the one-step graph
+    while (done < nsteps && (sweep_flags(w) & (SW_FORCES | SW_MODEL_INPUT)))
     {
         if ((rc = step_eager(w, dt, false)))
             return rc;
@@ -769,21 +825,48 @@ int batch_steps(nans_world *w, float dt, uint32_t nsteps, uint32_t gsteps)
         ++w->eager_steps_run;
     }
     uint32_t rem = nsteps - done;
-    if (gsteps > 0 && rem >= gsteps)
-    {
-        if ((rc = ensure_graph(w, dt, (int)gsteps)))
-            return rc;
-        for (uint32_t g = 0; g < rem / gsteps; ++g)
-            CK(cudaGraphLaunch(w->gexec, w->stream));
-        w->steps_run += (rem / gsteps) * gsteps;
-        w->graph_steps_run += (rem / gsteps) * gsteps;
-        rem %= gsteps;
-    }
+    if (gsteps > 1)
+        for (; rem >= gsteps; rem -= gsteps)
+        {
+            cudaGraphExec_t exec = nullptr;
+            if ((rc = ensure_graph(w, dt, (int)gsteps, &exec)))
+                return rc;
+            CK(cudaGraphLaunch(exec, w->stream));
+            after_step(w, dt);
+            w->steps_run += gsteps - 1;
+            w->graph_steps_run += gsteps;
+        }
     for (uint32_t i = 0; i < rem; ++i)
-    {
-        if ((rc = step_eager(w, dt, false)))
+        if ((rc = step_graph1(w, dt)))
             return rc;
-        ++w->eager_steps_run;
+    return NANS_OK;
+}
+
+// The state snapshot buffer (6 float4 per body: the mutable state) and, with_hist, the copy of
+// the per-pair EPA lengths, sized for the current upload.
+int ensure_snapshot(nans_world *w, bool with_hist)
+{
+    const size_t n = (size_t)w->n_all;
+    if (w->d_snap && w->snap_n < n)
+    {
+        cudaFree(w->d_snap);
+        w->d_snap = nullptr;
+    }
+    if (!w->d_snap)
+    {
+        CK(cudaMalloc(&w->d_snap, 6 * std::max<size_t>(1, n) * sizeof(float4)));
+        w->snap_n = n;
+    }
+    const size_t nhist = (size_t)w->dw.n_words * 32;
+    if (with_hist && w->d_snap_hist && w->snap_hist_n < nhist)
+    {
+        cudaFree(w->d_snap_hist);
+        w->d_snap_hist = nullptr;
+    }
+    if (with_hist && !w->d_snap_hist)
+    {
+        CK(cudaMalloc(&w->d_snap_hist, std::max<size_t>(1, nhist)));
+        w->snap_hist_n = nhist;
     }
     return NANS_OK;
 }
@@ -802,20 +885,21 @@ int status_code(nans_world *w, unsigned status)
 
 // The plain path with one host synchronisation per call. The world's mutable state is copied
 // aside on the device, the steps are enqueued without reading the candidate count back (each
-// step replays a one-step CUDA graph, except the first after an upload or a set_state), and
-// the status word and the largest candidate
-// count are read once at the end. If a step found more candidate pairs than the buffers hold
-// (the cull then caps its writes and flags the step), the copy is restored, the buffers grow
-// to the largest count seen and the steps run again, synchronising after each cull as before.
-// Worlds with warm starting keep that synchronising loop: their contact cache is stamped per
-// step and cannot be rolled back.
+// step replays a one-step CUDA graph, except the first after an upload or a set_state), and the
+// status word and the largest candidate count are read once at the end. If a step found more
+// candidate pairs than the buffers hold (the cull then caps its writes and flags the step), the
+// copy is restored, the buffers grow (to 1.5 times the largest count seen, at least double) and
+// the steps run again the same way; after three such rounds they run synchronising after every
+// cull. Worlds with warm starting keep that synchronising loop: their contact cache is stamped
+// per step and cannot be rolled back.
 int plain_steps(nans_world *w, float dt, uint32_t nsteps)
 {
     cudaStream_t st = w->stream;
     DevWorld &d = w->dw;
     const size_t n = (size_t)w->n_all;
-    if (!w->d_snap)
-        CK(cudaMalloc(&w->d_snap, 6 * n * sizeof(float4)));
+    int rc = ensure_snapshot(w, false);
+    if (rc)
+        return rc;
     float4 *bufs[6] = {d.pos, d.ang, d.vel, d.omg, d.frc, d.trq};
     for (int i = 0; i < 6; ++i)
         CK(cudaMemcpyAsync(w->d_snap + i * n, bufs[i], n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
@@ -823,44 +907,47 @@ int plain_steps(nans_world *w, float dt, uint32_t nsteps)
     const float s_pdt = w->pending_dt;
     const long long s_steps = w->steps_run;
     const unsigned long long s_graph = w->graph_steps_run, s_eager = w->eager_steps_run;
-    CK(cudaMemsetAsync(d.cull_max, 0, sizeof(int), st));
-    int rc;
-    for (uint32_t i = 0; i < nsteps; ++i)
+    for (int round = 0; round < 3; ++round)
     {
-        // graphs for the repeating flags (steady steps, and steps after a download or a state
-        // write); the first step after an upload or set_state (forces, input Model) is eager
-        if (!(sweep_flags(w) & (SW_FORCES | SW_MODEL_INPUT)))
+        CK(cudaMemsetAsync(d.cull_max, 0, sizeof(int), st));
+        for (uint32_t i = 0; i < nsteps; ++i)
         {
-            if ((rc = step_graph1(w, dt)))
-                return rc;
+            // graphs for the repeating flags (steady steps, and steps after a download or a state
+            // write); the first step after an upload or set_state (forces, input Model) is eager
+            if (!(sweep_flags(w) & (SW_FORCES | SW_MODEL_INPUT)))
+            {
+                if ((rc = step_graph1(w, dt)))
+                    return rc;
+            }
+            else
+            {
+                if ((rc = step_eager(w, dt, false)))
+                    return rc;
+                ++w->eager_steps_run;
+            }
         }
-        else
-        {
-            if ((rc = step_eager(w, dt, false)))
-                return rc;
-            ++w->eager_steps_run;
-        }
+        unsigned hdr[2] = {0u, 0u};
+        CK(cudaMemcpyAsync(&hdr[0], d.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(&hdr[1], d.cull_max, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CK(cudaStreamSynchronize(st));
+        if (!(hdr[0] & ST_CANDIDATES))
+            return status_code(w, hdr[0]);
+        // roll back and grow
+        for (int i = 0; i < 6; ++i)
+            CK(cudaMemcpyAsync(bufs[i], w->d_snap + i * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+        w->pending = s_pending;
+        w->model_input = s_model;
+        w->forces_pending = s_forces;
+        w->pending_dt = s_pdt;
+        w->steps_run = s_steps;
+        w->graph_steps_run = s_graph;
+        w->eager_steps_run = s_eager;
+        const long long need = (long long)(int)hdr[1];
+        const long long grow = std::max(need + need / 2, 2LL * w->cand_cap) + 1024;
+        if ((rc = alloc_candidates(w, (int)std::min<long long>(grow, INT32_MAX / 16))))
+            return rc;
+        CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
     }
-    unsigned hdr[2] = {0u, 0u};
-    CK(cudaMemcpyAsync(&hdr[0], d.status, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-    CK(cudaMemcpyAsync(&hdr[1], d.cull_max, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CK(cudaStreamSynchronize(st));
-    if (!(hdr[0] & ST_CANDIDATES))
-        return status_code(w, hdr[0]);
-    // roll back, grow, run again
-    for (int i = 0; i < 6; ++i)
-        CK(cudaMemcpyAsync(bufs[i], w->d_snap + i * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
-    w->pending = s_pending;
-    w->model_input = s_model;
-    w->forces_pending = s_forces;
-    w->pending_dt = s_pdt;
-    w->steps_run = s_steps;
-    w->graph_steps_run = s_graph;
-    w->eager_steps_run = s_eager;
-    const long long need = (long long)(int)hdr[1];
-    if ((rc = alloc_candidates(w, (int)std::min<long long>(need + need / 4 + 1024, INT32_MAX / 16))))
-        return rc;
-    CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
     for (uint32_t i = 0; i < nsteps; ++i)
     {
         if ((rc = step_eager(w, dt, true)))
@@ -1007,6 +1094,8 @@ int nans_world_destroy(nans_world *w)
         cudaFree(w->d_pairs_out);
     if (w->d_snap)
         cudaFree(w->d_snap);
+    if (w->d_snap_hist)
+        cudaFree(w->d_snap_hist);
     for (void *p : w->tape_chunks)
         cudaFree(p);
     if (w->d_tape)
@@ -1083,6 +1172,30 @@ int nans_batch_step(nans_world *w, float dt, uint32_t nsteps, uint32_t graph_ste
     return check_status(w);
 }
 
+int nans_batch_prepare(nans_world *w, float dt, uint32_t graph_steps)
+{
+    if (!w)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "batch_prepare: null world");
+    if (!w->uploaded)
+        return fail(NANS_ERR_NOT_UPLOADED, "batch_prepare: no scene uploaded");
+    if (!valid_dt(dt))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "batch_prepare: dt must be finite and positive");
+    CK(cudaSetDevice(w->device));
+    const uint32_t g = graph_steps ? graph_steps : 60;
+    int rc = NANS_OK;
+    if (g == 1)
+        rc = ensure_graph1(w, dt);
+    else if (!(sweep_flags(w) & (SW_FORCES | SW_MODEL_INPUT)))
+    {
+        cudaGraphExec_t exec = nullptr;
+        rc = ensure_graph(w, dt, (int)g, &exec);
+    }
+    if (rc)
+        return rc;
+    CK(cudaStreamSynchronize(w->stream));
+    return NANS_OK;
+}
+
 int nans_batch_autotune(nans_world *w, float dt)
 {
     if (!w || !w->uploaded)
@@ -1092,62 +1205,121 @@ int nans_batch_autotune(nans_world *w, float dt)
     CK(cudaSetDevice(w->device));
     cudaStream_t st = w->stream;
     const size_t n = (size_t)w->n_all;
-    if (!w->d_snap)
-        CK(cudaMalloc(&w->d_snap, 6 * n * sizeof(float4)));
-    // snapshot the mutable state and the host-side step flags
+    const size_t nhist = (size_t)w->dw.n_words * 32;
+    {
+        const int r0 = ensure_snapshot(w, true);
+        if (r0)
+            return r0;
+    }
+    // snapshot the mutable state (and the per-pair EPA lengths that order the EPA queue) and the
+    // host-side step flags: every candidate runs the same window of the simulation
     float4 *bufs[6] = {w->dw.pos, w->dw.ang, w->dw.vel, w->dw.omg, w->dw.frc, w->dw.trq};
     for (int i = 0; i < 6; ++i)
         CK(cudaMemcpyAsync(w->d_snap + i * n, bufs[i], n * sizeof(float4), cudaMemcpyDeviceToDevice, st));
+    if (nhist)
+        CK(cudaMemcpyAsync(w->d_snap_hist, w->dw.epa_hist, nhist, cudaMemcpyDeviceToDevice, st));
     const bool s_pending = w->pending, s_model = w->model_input, s_forces = w->forces_pending;
     const float s_pdt = w->pending_dt;
     const long long s_steps = w->steps_run;
-    struct Cfg
-    {
-        int warps, nbpsm, sbpsm;
-    };
-    const Cfg cands[] = {{4, 0, 0}, {8, 0, 0}, {4, 8, 0}, {8, 4, 0}, {4, 0, 4}, {8, 0, 2}};
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    float best = 1e30f;
-    Cfg bestc = cands[0];
     int rc = NANS_OK;
-    for (const Cfg &c : cands)
-    {
-        w->narrow_warps = c.warps;
-        w->narrow_bpsm = c.nbpsm;
-        w->solve_bpsm = c.sbpsm;
-        if ((rc = step_eager(w, dt, false)))
-            break;
+    // one candidate: a warm step, then kTuneSteps timed steps from the snapshot, restored after
+    auto trial = [&](float &ms) -> int {
+        int r = step_eager(w, dt, false);
         cudaEventRecord(e0, st);
-        for (int k = 0; k < 2 && rc == NANS_OK; ++k)
-            rc = step_eager(w, dt, false);
+        for (int k = 0; k < kTuneSteps && r == NANS_OK; ++k)
+            r = step_eager(w, dt, false);
         cudaEventRecord(e1, st);
         cudaEventSynchronize(e1);
-        float ms = 0.0f;
+        ms = 0.0f;
         cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best)
-        {
-            best = ms;
-            bestc = c;
-        }
         for (int i = 0; i < 6; ++i)
             cudaMemcpyAsync(bufs[i], w->d_snap + i * n, n * sizeof(float4), cudaMemcpyDeviceToDevice, st);
+        if (nhist)
+            cudaMemcpyAsync(w->dw.epa_hist, w->d_snap_hist, nhist, cudaMemcpyDeviceToDevice, st);
         w->pending = s_pending;
         w->model_input = s_model;
         w->forces_pending = s_forces;
         w->pending_dt = s_pdt;
         w->steps_run = s_steps;
+        return r;
+    };
+    // coordinate descent over the launch parameters, one at a time from the defaults: the
+    // per-thread EPA's iteration budget, the GJK pass's blocks per SM, and the solver's threads
+    // per scene in its first pass (1 or 2 warps) and for the late scenes (4 or 8 warps)
+    struct Axis
+    {
+        int *field;
+        int cands[4];
+        int ncand;
+    };
+    const int solve0_auto = solve_threads(w->max_scene_bodies);
+    Axis axes[] = {
+        {&w->dw.tiny_budget, {kTinyBudgetDefault, 3, 6, 65}, 4},
+        {&w->narrow_bpsm, {0, 4, 0, 0}, 2},
+        {&w->solve_threads0, {solve0_auto, 64, 0, 0}, solve0_auto == 32 ? 2 : 1},
+        {&w->solve_threads1, {kSolveLateThreads, 256, 0, 0}, 2},
+    };
+    w->tune_trials = 0;
+    for (Axis &ax : axes)
+    {
+        float best = 1e30f;
+        int bestv = *ax.field;
+        for (int c = 0; c < ax.ncand && rc == NANS_OK; ++c)
+        {
+            *ax.field = ax.cands[c];
+            float ms = 0.0f;
+            rc = trial(ms);
+            ++w->tune_trials;
+            if (ms < best)
+            {
+                best = ms;
+                bestv = ax.cands[c];
+            }
+        }
+        *ax.field = bestv;
+        w->tune_ms = best / kTuneSteps;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    w->narrow_warps = bestc.warps;
-    w->narrow_bpsm = bestc.nbpsm;
-    w->solve_bpsm = bestc.sbpsm;
     drop_graph(w);
     CK(cudaStreamSynchronize(st));
     CK(cudaMemsetAsync(w->dw.status, 0, sizeof(unsigned), st));
     return rc;
+}
+
+int nans_world_set_tuning(nans_world *w, const int32_t *in)
+{
+    if (!w || !in)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: null world or input");
+    const bool threads_ok =
+        in[2] >= 32 && in[2] <= 256 && in[2] % 32 == 0 && in[3] >= 32 && in[3] <= 256 && in[3] % 32 == 0;
+    if (in[0] < 1 || in[0] > 65 || in[1] < 0 || in[1] > 32 || !threads_ok)
+        return fail(NANS_ERR_INVALID_ARGUMENT,
+                    "set_tuning: budget in [1, 65], GJK blocks per SM in [0, 32], solver threads multiples of 32 "
+                    "in [32, 256]");
+    if (in[2] < 256 && w->max_scene_bodies > 512)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: scenes above 512 bodies need 256 solver threads");
+    w->dw.tiny_budget = in[0];
+    w->narrow_bpsm = in[1];
+    w->solve_threads0 = in[2];
+    w->solve_threads1 = in[3];
+    return NANS_OK;
+}
+
+int nans_world_tuning(nans_world *w, int32_t *out)
+{
+    if (!w || !out)
+        return fail(NANS_ERR_INVALID_ARGUMENT, "tuning: null world or output");
+    out[0] = w->dw.tiny_budget;
+    out[1] = w->narrow_bpsm;
+    out[2] = w->solve_threads0 ? w->solve_threads0 : solve_threads(w->max_scene_bodies);
+    out[3] = w->solve_threads1;
+    out[4] = w->tune_trials;
+    out[5] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
+    return NANS_OK;
 }
 
 int nans_world_download(nans_world *w, nans_cube *cubes, nans_sphere *spheres, nans_cube *floors)
@@ -1601,8 +1773,9 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[4], st));
         CK((cudaError_t)launch_narrow_big(st, w->dw));
         CK(cudaEventRecord(ev[5], st));
-        launch_solve(w->dw, w->n_scenes, solve_threads(w->max_scene_bodies), solve_smem(w), st, dt, 0);
-        launch_solve(w->dw, std::min(w->n_scenes, 2 * w->sm_count), kSolveLateThreads, solve_smem(w), st, dt, 1);
+        launch_solve(w->dw, w->n_scenes, w->solve_threads0 ? w->solve_threads0 : solve_threads(w->max_scene_bodies),
+                 solve_smem(w), st, dt, 0);
+        launch_solve(w->dw, std::min(w->n_scenes, 2 * w->sm_count), w->solve_threads1, solve_smem(w), st, dt, 1);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());
         after_step(w, dt);
@@ -1678,9 +1851,9 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
 {
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
-    // sweep, [cull mask, cull write], cull scan, gjk, gjk_long, epa_tiny, epa_medium, block
-    // EPA, giant EPA, solve (two passes)
-    uint32_t k = 10 + (w->cull_blocks > 0 ? 2u : 0u);
+    // sweep, [cull mask, cull write], cull scan, gjk, gjk_long, epa_tiny, [epa_tiny_resume],
+    // epa_medium, block EPA, giant EPA, solve (two passes)
+    uint32_t k = 10 + (w->cull_blocks > 0 ? 2u : 0u) + (w->dw.tiny_budget < 65 ? 1u : 0u);
     if (batched)
         *batched = k;
     if (plain)

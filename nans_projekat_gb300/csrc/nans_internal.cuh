@@ -87,12 +87,17 @@ struct DevWorld
                                         // [8] giant-EPA queue length, [9] giant-EPA head,
                                         // [10] per-thread EPA queue length (queue: s_order),
                                         // [11] per-thread EPA head, [12] late-solve head,
-                                        // [13] late-scene count
+                                        // [13] late-scene count, [14] resume slots taken,
+                                        // [15] resume head
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
     int2 *long_cand;                    // candidates whose GJK needs the long pass: (c, n | it << 8)
     int medium_blocks;                  // warp-tier grid
     int tiny_blocks;                    // per-thread EPA grid (resident blocks on every SM)
+    int tiny_budget;                    // per-thread EPA iterations before an EPA is set aside
+                                        // for the resume pass (65: no budget)
+    unsigned *epa_res;                  // resume slots of budgeted per-thread EPAs
+    int res_cap;                        // resume slots
     int ovf_cap;                        // block-EPA queue capacity
     int *ovf_cand;                      // candidates queued for the block tier
     unsigned char *blk_arena;           // block-tier polytope buffers, one per block

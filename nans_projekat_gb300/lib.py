@@ -41,7 +41,7 @@ EXPORTS = (
     "nans_launches_per_step", "nans_device_sincos", "nans_last_error", "nans_profile_steps", "nans_profile_timeline",
     "nans_world_epa_stats", "nans_solve_contacts_static", "nans_diff_forward", "nans_diff_backward",
     "nans_diff_tape_info", "nans_world_set_state_arrays", "nans_world_get_state_arrays", "nans_render_scene",
-    "nans_world_path_counts",
+    "nans_world_path_counts", "nans_world_tuning", "nans_world_set_tuning", "nans_batch_prepare",
 )
 
 
@@ -88,6 +88,7 @@ def load(path=LIB_PATH):
     L.nans_step.argtypes = [_P, ctypes.POINTER(StepParams), _F, _U]
     L.nans_batch_step.argtypes = [_P, _F, _U, _U]
     L.nans_batch_autotune.argtypes = [_P, _F]
+    L.nans_batch_prepare.argtypes = [_P, _F, _U]
     L.nans_world_download.argtypes = [_P, _P, _P, _P]
     L.nans_world_set_state.argtypes = [_P, _P, _P, _U]
     L.nans_get_pairs.argtypes = [_P, _U, _P, _U, ctypes.POINTER(_U)]
@@ -97,6 +98,8 @@ def load(path=LIB_PATH):
     L.nans_world_stream.restype = _P
     L.nans_launches_per_step.argtypes = [_P, ctypes.POINTER(_U), ctypes.POINTER(_U)]
     L.nans_world_path_counts.argtypes = [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+    L.nans_world_tuning.argtypes = [_P, _P]
+    L.nans_world_set_tuning.argtypes = [_P, _P]
     L.nans_device_sincos.argtypes = [_P, _P, _P, _U]
     L.nans_profile_steps.argtypes = [_P, _F, _U, _P]
     L.nans_profile_timeline.argtypes = [_P, _F, _U, _P]
@@ -210,6 +213,10 @@ class World:
     def batch_step(self, dt, n=1, graph_steps=60):
         _check(self.lib.nans_batch_step(self.h, dt, n, graph_steps))
 
+    def prepare(self, dt, graph_steps=60):
+        """Captures the graph the next batch_step(dt, n, graph_steps) replays first."""
+        _check(self.lib.nans_batch_prepare(self.h, dt, graph_steps))
+
     def autotune(self, dt):
         _check(self.lib.nans_batch_autotune(self.h, dt))
 
@@ -282,6 +289,18 @@ class World:
         a, b = _U(), _U()
         _check(self.lib.nans_launches_per_step(self.h, ctypes.byref(a), ctypes.byref(b)))
         return a.value, b.value
+
+    def tuning(self):
+        """The launch parameters in use (nans_batch_autotune's choice, or the defaults)."""
+        out = np.zeros(6, np.int32)
+        _check(self.lib.nans_world_tuning(self.h, _ptr(out)))
+        return {"epa_budget": int(out[0]), "gjk_blocks_per_sm": int(out[1]), "solve_threads": int(out[2]),
+                "solve_threads_late": int(out[3]), "candidates_timed": int(out[4]),
+                "us_per_step": int(out[5])}
+
+    def set_tuning(self, epa_budget, gjk_blocks_per_sm, solve_threads, solve_threads_late):
+        a = np.array([epa_budget, gjk_blocks_per_sm, solve_threads, solve_threads_late], np.int32)
+        _check(self.lib.nans_world_set_tuning(self.h, _ptr(a)))
 
     def path_counts(self):
         """(steps replayed from CUDA graphs, steps launched eagerly) since the last upload."""

@@ -204,6 +204,8 @@ template <class T> struct Contact
     int type, a, b;
     V3<T> pa, pb, n;
     T sn, st1, st2; // accumulated impulses: initial values (warm start), then final values
+    bool held = false;   // replayed contact: the solve takes the bodies' positions from pos_a / pos_b
+    V3<T> pos_a, pos_b;  // (replayed contacts only) the two bodies' positions at the recorded solve
 };
 
 struct Consts
@@ -220,6 +222,13 @@ template <class T> struct Scene
     Consts k;
     bool warm = false;                // warm starting: accumulators carried across steps
     std::vector<Contact<T>> prev;     // the last solve's contacts with their accumulators
+    // Held contacts (test infrastructure for gradient checks): when replay is non-empty, the
+    // detect stage of the k-th step does not run GJK/EPA but takes replay[k], the contact list
+    // and contact geometry recorded from another run, and the solve computes its
+    // velocity-independent constants (lever arms, depth) from the recorded body positions. The
+    // step is then the rollout with its contact set and geometry held fixed.
+    std::vector<std::vector<Contact<T>>> replay;
+    size_t replay_step = 0;
 };
 
 // ---------------------------------------------------------------------------------
@@ -778,6 +787,14 @@ template <class T> static bool check_collision(const PairCtx<T> &p, Contact<T> &
 // DetectCollisions (code/nans.cpp:1351-1536)
 template <class T> static void detect(Scene<T> &s)
 {
+    if (!s.replay.empty())
+    {
+        if (s.replay_step < s.replay.size())
+            s.pairs = s.replay[s.replay_step++];
+        else
+            s.pairs.clear();
+        return;
+    }
     s.pairs.clear();
     const int nc = (int)s.cubes.size(), ns = (int)s.spheres.size();
     auto run = [&](int type, int ia, int ib, const Body<T> *A, const Body<T> *B, bool as, bool bs) {
@@ -819,7 +836,7 @@ template <class T> static void constraint(Scene<T> &s, Contact<T> &c, T dt)
     }
     const bool writes_b = (c.type != TCF && c.type != TSF);
     V3<T> n = normalize(c.n);
-    V3<T> pa = A->P, pb = B->P;
+    V3<T> pa = c.held ? c.pos_a : A->P, pb = c.held ? c.pos_b : B->P;
     T invi1 = T(1) / A->moi, invi2 = T(1) / B->moi;
     T invm1 = T(1) / A->mass, invm2 = T(1) / B->mass;
     V3<T> v1 = A->V, v2 = B->V, w1 = A->W, w2 = B->W;
@@ -1268,6 +1285,44 @@ uint32_t nanso_pairs(void *h, int scene, void *outp, uint32_t cap)
 }
 
 // Sets the per-scene solver constants (restitution, friction, iterations).
+// Holds the contacts of one scene for its next nsteps steps (see Scene::replay): counts[k]
+// contact records (the reference's contact_pair layout) for step k, concatenated in `pairs`,
+// with the two bodies' positions at that step's solve in pos_a / pos_b (3 floats per contact).
+// nsteps = 0 turns the replay off (GJK/EPA again).
+void nanso_set_replay(void *h, int scene, int nsteps, const int32_t *counts, const void *pairs, const float *pos_a,
+                      const float *pos_b)
+{
+    World *w = (World *)h;
+    const RPair *rp = (const RPair *)pairs;
+    auto fill = [&](auto &sc) {
+        using T = decltype(sc.floor.mass);
+        sc.replay.assign((size_t)std::max(0, nsteps), {});
+        sc.replay_step = 0;
+        size_t q = 0;
+        for (int k = 0; k < nsteps; ++k)
+            for (int i = 0; i < counts[k]; ++i, ++q)
+            {
+                const RPair &r = rp[q];
+                Contact<T> c{};
+                c.type = r.Type;
+                c.a = r.IndexA;
+                c.b = r.IndexB;
+                c.pa = v3<T>(r.PointA);
+                c.pb = v3<T>(r.PointB);
+                c.n = v3<T>(r.N);
+                c.sn = c.st1 = c.st2 = T(0);
+                c.held = true;
+                c.pos_a = v3<T>(pos_a + 3 * q);
+                c.pos_b = v3<T>(pos_b + 3 * q);
+                sc.replay[k].push_back(c);
+            }
+    };
+    if (w->fp64)
+        fill(w->sd[scene]);
+    else
+        fill(w->sf[scene]);
+}
+
 void nanso_set_constants(void *h, int scene, float cr, float cf, int iters)
 {
     World *w = (World *)h;

@@ -49,6 +49,7 @@ def lib():
         L.nanso_pairs.argtypes = [_P, _I, _P, _U]
         L.nanso_pairs.restype = _U
         L.nanso_set_constants.argtypes = [_P, _I, _F, _F, _I]
+        L.nanso_set_replay.argtypes = [_P, _I, _I, _P, _P, _P, _P]
         L.nanso_sincosf.argtypes = [_P, _P, _P, _I]
         L.nanso_epa_stats.argtypes = [_P, _I]
         L.nanso_stats_enable.argtypes = [_I]
@@ -113,6 +114,31 @@ class OracleWorld:
         out = np.zeros((n, 12), np.float64)
         self.lib.nanso_state_f64(self.h, i, _ptr(out))
         return out
+
+    def hold_contacts(self, i, steps):
+        """Holds scene i's contacts for its next len(steps) steps: steps[k] = (positions of the
+        scene's dynamic bodies at step k's solve, the floor's position, the contact records of
+        step k), as recorded from another run. The detect stage then replays them and the solve
+        takes lever arms and depth from the recorded positions: the rollout with its contact set
+        and contact geometry held fixed. An empty list turns it off."""
+        nc = len(self.scenes[i].cubes)
+        counts = np.array([len(p) for _, _, p in steps], np.int32)
+        pairs = np.concatenate([p for _, _, p in steps]) if len(steps) else np.zeros(0, PAIR_DTYPE)
+        pos_a = np.zeros((len(pairs), 3), np.float32)
+        pos_b = np.zeros((len(pairs), 3), np.float32)
+        q = 0
+        for pos, floor_pos, prs in steps:
+            for r in prs:
+                t = int(r["Type"])
+                a = int(r["IndexA"]) + (nc if t in (3, 4) else 0)           # SS, SF: A is a sphere
+                pos_a[q] = pos[a]
+                if t in (2, 4):                                              # CF, SF: B is the floor
+                    pos_b[q] = floor_pos
+                else:
+                    pos_b[q] = pos[int(r["IndexB"]) + (nc if t in (1, 3) else 0)]  # CS, SS: B a sphere
+                q += 1
+        pairs = np.ascontiguousarray(pairs)
+        self.lib.nanso_set_replay(self.h, i, len(steps), _ptr(counts), _ptr(pairs), _ptr(pos_a), _ptr(pos_b))
 
     def pairs(self, i=0):
         n = self.lib.nanso_pairs(self.h, i, None, 0)

@@ -415,3 +415,69 @@ def test_full_size_batch_samples_match_oracle(nl, oracle_lib):
         assert same_fields(oc, cubes, STATE_FIELDS)[0], (i, first_difference(oc, cubes, STATE_FIELDS))
         assert same_fields(os_, spheres, STATE_FIELDS)[0], i
         assert same_fields(o.pairs(j), w.pairs(i), PAIR_FIELDS)[0], i
+
+
+@pytest.mark.parametrize("tuning", [(65, 0, 32, 128), (1, 0, 32, 128), (2, 4, 64, 256), (4, 0, 32, 128)])
+def test_results_do_not_depend_on_launch_parameters(nl, oracle_lib, tuning):
+    """The per-thread EPA's iteration budget (1: nearly every EPA goes through the resume pass; 65:
+    none), the GJK blocks per SM and the solver's threads per scene change the schedule, never the
+    result: 256 workload scenes for 40 steps against the oracle, bit for bit."""
+    batch = scenes.stack_batch(16384, seed=2)[:256]
+    dt = np.float32(1 / 60)
+    w = nl.World()
+    w.upload_batch(batch)
+    w.set_tuning(*tuning)
+    w.batch_step(dt, 40, graph_steps=20)
+    assert w.status() == 0
+    t = w.tuning()
+    assert (t["epa_budget"], t["gjk_blocks_per_sm"], t["solve_threads"], t["solve_threads_late"]) == tuning
+    state = w.download()
+    o = _oracle_states(batch, 40, dt)
+    for i in range(len(batch)):
+        cubes, spheres, _ = w.scene_state(i, state)
+        oc, os_, _ = o.state(i)
+        assert same_fields(oc, cubes, STATE_FIELDS)[0], (i, first_difference(oc, cubes, STATE_FIELDS))
+        assert same_fields(os_, spheres, STATE_FIELDS)[0], i
+        assert same_fields(o.pairs(i), w.pairs(i), PAIR_FIELDS)[0], i
+    w.close()
+
+
+def test_epa_resume_slots_exhausted(nl, oracle_lib):
+    """With fewer resume slots than budgeted EPAs (a world keeps resume slots for half its
+    candidate capacity; with a one-iteration budget nearly every EPA asks for one), the EPAs
+    without a slot finish in the first pass: the same result, bit for bit."""
+    batch = scenes.stack_batch(16384, seed=2)[:8]
+    dt = np.float32(1 / 60)
+    probe = nl.World()
+    probe.upload_batch(batch)
+    cap = 0
+    for _ in range(20):
+        probe.batch_step(dt, 1, 1)
+        cap = max(cap, probe.counts()[0])
+    probe.close()
+    w = nl.World(max_candidates=cap)
+    w.upload_batch(batch)
+    w.set_tuning(1, 0, 32, 128)
+    w.batch_step(dt, 20, graph_steps=10)
+    assert w.status() == 0
+    n_cand, n_contacts = w.counts()
+    assert n_contacts > cap // 2  # more EPAs than resume slots
+    state = w.download()
+    o = _oracle_states(batch, 20, dt)
+    for i in range(len(batch)):
+        cubes, spheres, _ = w.scene_state(i, state)
+        assert same_fields(o.state(i)[0], cubes, STATE_FIELDS)[0], i
+        assert same_fields(o.pairs(i), w.pairs(i), PAIR_FIELDS)[0], i
+    w.close()
+
+
+def test_autotuner_times_every_candidate(nl):
+    batch = scenes.stack_batch(16384, seed=2)[:512]
+    w = nl.World()
+    w.upload_batch(batch)
+    w.step(np.float32(1 / 60), 2)
+    w.autotune(np.float32(1 / 60))
+    t = w.tuning()
+    assert t["candidates_timed"] == 10 and t["us_per_step"] > 0
+    assert t["epa_budget"] in (3, 4, 6, 65) and t["solve_threads"] in (32, 64)
+    w.close()
