@@ -113,12 +113,19 @@ typedef struct nans_contact_pair
 #define NANS_WORLD_ALL_PAIRS 1u    /* run GJK on every pair (the reference's all-pairs
                                       loop); default: conservative AABB cull first */
 #define NANS_WORLD_STRICT_EPA 2u   /* an EPA polytope beyond the large-polytope buffers
-                                      (2,097,152 faces) fails the step with
+                                      (8,388,608 faces) fails the step with
                                       NANS_ERR_EPA_CAPACITY; default: that pair gets no
                                       contact (the reference's result for every EPA that does
                                       not converge) and the event is counted */
 #define NANS_WORLD_TEST_GIANT_TIER 4u /* testing: every EPA beyond the warp tier's 256 faces
                                       runs on the grid-wide tier (results are the same) */
+#define NANS_WORLD_TEST_BARRIER_TIMEOUT 16u /* testing: the grid-wide tier's barrier waits for
+                                      one block more than its grid has (an arrival that never
+                                      comes) and gives up after 4,096 polls, so that the bounded
+                                      wait's error path runs: the step returns
+                                      NANS_ERR_EPA_CAPACITY with the timeout status bit. Use with
+                                      NANS_WORLD_TEST_GIANT_TIER. The reference caps its loops
+                                      instead (code/nans.cpp:804, 915). */
 #define NANS_WORLD_WARM_START 8u   /* warm starting, the reference's TODO at its pair dedupe
                                       (code/nans.cpp:1386-1389): a pair (type, IndexA,
                                       IndexB) that was in contact at the previous step starts
@@ -257,14 +264,13 @@ int nans_profile_timeline(nans_world *world, float dt, uint32_t nsteps, float *t
  * counterpart. */
 int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain);
 
-/* The launch parameters nans_batch_autotune chose (or the defaults): out[0] the per-thread EPA's
- * iteration budget before an EPA is set aside for the resume pass (65 = no budget), out[1] GJK
- * blocks per SM (0 = as many as fit), out[2] solver threads per scene in the first solve pass,
- * out[3] solver threads per late scene, out[4] candidates the autotuner timed, out[5] the
- * chosen candidate's microseconds per step. No reference counterpart. */
+/* The launch parameters nans_batch_autotune chose (or the defaults): out[0] GJK blocks per SM
+ * (0 = as many as fit), out[1] solver threads per scene in the first solve pass, out[2] solver
+ * threads per late scene, out[3] candidates the autotuner timed, out[4] the chosen candidate's
+ * microseconds per step. No reference counterpart. */
 int nans_world_tuning(nans_world *world, int32_t *out);
 
-/* Sets the launch parameters out[0..3] of nans_world_tuning (for instance a choice of the
+/* Sets the launch parameters out[0..2] of nans_world_tuning (for instance a choice of the
  * autotuner kept from an earlier run); results do not depend on them. No reference
  * counterpart. */
 int nans_world_set_tuning(nans_world *world, const int32_t *in);

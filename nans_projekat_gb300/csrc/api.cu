@@ -174,7 +174,7 @@ void drop_graph(nans_world *w)
 
 int cfg_id(const nans_world *w)
 {
-    return ((w->dw.tiny_budget * 64 + w->narrow_bpsm) * 1024 + w->solve_threads0) * 1024 + w->solve_threads1;
+    return (w->narrow_bpsm * 1024 + w->solve_threads0) * 1024 + w->solve_threads1;
 }
 
 int narrow_grid(nans_world *w)
@@ -215,11 +215,6 @@ int alloc_candidates(nans_world *w, int cap)
         d.s_fwd = w->fwd_buf;
     }
     if ((rc = dalloc(w, L, &d.cand_pidx, cap)))
-        return rc;
-    // resume slots for half the candidates: a 4-iteration budget sets aside about a fifth of the
-    // EPAs on the stack workload; beyond the slots, EPAs run to their end in the first pass
-    d.res_cap = std::max(1, std::min(cap / 2, kResumeSlotsMax));
-    if ((rc = dalloc(w, L, &d.epa_res, epa_resume_words() * (size_t)d.res_cap)))
         return rc;
     return NANS_OK;
 }
@@ -442,7 +437,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &d.giant_scratch, epa_giant_scratch_bytes())) ||
         (rc = dalloc(w, L, &d.blk_arena, epa_block_bytes() * (size_t)(kBlockPerSm * w->sm_count))) ||
         (rc = dalloc(w, L, &d.giant_cand, kGiantQueueCap)) || (rc = dalloc(w, L, &d.handover, kHandoverSlots)) ||
-        (rc = dalloc(w, L, &d.epa_stats, 8)) ||
+        (rc = dalloc(w, L, &d.epa_stats, 8)) || (rc = dalloc(w, L, &d.check, 4)) ||
         (rc = dalloc(w, L, &w->d_rec_cube, (size_t)61 * tc)) || (rc = dalloc(w, L, &w->d_rec_sphere, (size_t)37 * ts)) ||
         (rc = dalloc(w, L, &w->d_rec_floor, (size_t)61 * S)) || (rc = dalloc(w, L, &w->d_small, 2)) ||
         (rc = dalloc(w, L, &d.s_last, 1)))
@@ -478,10 +473,12 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     w->gjk_cap_blocks = upto(128, INT32_MAX);
     d.medium_blocks = upto(4, 2 * w->sm_count);
     d.tiny_blocks = upto(64, epa_tiny_grid(w->sm_count));
-    d.tiny_budget = kTinyBudgetDefault;
     d.giant_blocks = std::min(giant_grid(w->sm_count), upto(1, INT32_MAX) < 4096 ? 16 : INT32_MAX);
     d.blk_blocks = upto(1, kBlockPerSm * w->sm_count);
     d.blk_face_limit = (w->flags & NANS_WORLD_TEST_GIANT_TIER) ? 0 : kBlockFaces;
+    const bool barrier_test = (w->flags & NANS_WORLD_TEST_BARRIER_TIMEOUT) != 0;
+    d.barrier_spins = barrier_test ? kBarrierSpinsTest : kBarrierSpins;
+    d.barrier_extra = barrier_test ? 1u : 0u;
     d.giant_cap = kGiantQueueCap;
     cudaStream_t st = w->stream;
     CK(cudaMemcpyAsync(p_cube0, sc_cube0.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
@@ -515,6 +512,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
     CK(cudaMemsetAsync(d.giant_scratch, 0, epa_giant_scratch_bytes(), st));
     CK(cudaMemsetAsync(d.epa_stats, 0, 8 * sizeof(unsigned), st));
+    CK(cudaMemsetAsync(d.check, 0, 4 * sizeof(int), st));
     CK(cudaMemsetAsync(d.n_cand, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.cull_max, 0, sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, S * sizeof(int), st));
@@ -874,6 +872,14 @@ int ensure_snapshot(nans_world *w, bool with_hist)
 // Status bits of the last steps as a return code.
 int status_code(nans_world *w, unsigned status)
 {
+    if (status & ST_CHECK)
+    {
+        int chk[4] = {0, 0, 0, 0};
+        cudaMemcpy(chk, w->dw.check, sizeof(chk), cudaMemcpyDeviceToHost);
+        return fail(NANS_ERR_CUDA, "step: a device bounds check failed (site " + std::to_string(chk[0]) + ", index " +
+                                       std::to_string(chk[1]) + ", bound " + std::to_string(chk[2]) +
+                                       "); the access was skipped");
+    }
     if (status & ST_CANDIDATES)
         return fail(NANS_ERR_CAPACITY, "step: more candidate pairs than the world's capacity");
     if (status & ST_EPA_TIMEOUT)
@@ -1246,9 +1252,9 @@ int nans_batch_autotune(nans_world *w, float dt)
         w->steps_run = s_steps;
         return r;
     };
-    // coordinate descent over the launch parameters, one at a time from the defaults: the
-    // per-thread EPA's iteration budget, the GJK pass's blocks per SM, and the solver's threads
-    // per scene in its first pass (1 or 2 warps) and for the late scenes (4 or 8 warps)
+    // coordinate descent over the launch parameters, one at a time from the defaults: the GJK
+    // pass's blocks per SM, and the solver's threads per scene in its first pass (1 or 2 warps)
+    // and for the late scenes (4 or 8 warps)
     struct Axis
     {
         int *field;
@@ -1257,7 +1263,6 @@ int nans_batch_autotune(nans_world *w, float dt)
     };
     const int solve0_auto = solve_threads(w->max_scene_bodies);
     Axis axes[] = {
-        {&w->dw.tiny_budget, {kTinyBudgetDefault, 3, 6, 65}, 4},
         {&w->narrow_bpsm, {0, 4, 0, 0}, 2},
         {&w->solve_threads0, {solve0_auto, 64, 0, 0}, solve0_auto == 32 ? 2 : 1},
         {&w->solve_threads1, {kSolveLateThreads, 256, 0, 0}, 2},
@@ -1295,17 +1300,15 @@ int nans_world_set_tuning(nans_world *w, const int32_t *in)
     if (!w || !in)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: null world or input");
     const bool threads_ok =
-        in[2] >= 32 && in[2] <= 256 && in[2] % 32 == 0 && in[3] >= 32 && in[3] <= 256 && in[3] % 32 == 0;
-    if (in[0] < 1 || in[0] > 65 || in[1] < 0 || in[1] > 32 || !threads_ok)
+        in[1] >= 32 && in[1] <= 256 && in[1] % 32 == 0 && in[2] >= 32 && in[2] <= 256 && in[2] % 32 == 0;
+    if (in[0] < 0 || in[0] > 32 || !threads_ok)
         return fail(NANS_ERR_INVALID_ARGUMENT,
-                    "set_tuning: budget in [1, 65], GJK blocks per SM in [0, 32], solver threads multiples of 32 "
-                    "in [32, 256]");
-    if (in[2] < 256 && w->max_scene_bodies > 512)
+                    "set_tuning: GJK blocks per SM in [0, 32], solver threads multiples of 32 in [32, 256]");
+    if (in[1] < 256 && w->max_scene_bodies > 512)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: scenes above 512 bodies need 256 solver threads");
-    w->dw.tiny_budget = in[0];
-    w->narrow_bpsm = in[1];
-    w->solve_threads0 = in[2];
-    w->solve_threads1 = in[3];
+    w->narrow_bpsm = in[0];
+    w->solve_threads0 = in[1];
+    w->solve_threads1 = in[2];
     return NANS_OK;
 }
 
@@ -1313,12 +1316,11 @@ int nans_world_tuning(nans_world *w, int32_t *out)
 {
     if (!w || !out)
         return fail(NANS_ERR_INVALID_ARGUMENT, "tuning: null world or output");
-    out[0] = w->dw.tiny_budget;
-    out[1] = w->narrow_bpsm;
-    out[2] = w->solve_threads0 ? w->solve_threads0 : solve_threads(w->max_scene_bodies);
-    out[3] = w->solve_threads1;
-    out[4] = w->tune_trials;
-    out[5] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
+    out[0] = w->narrow_bpsm;
+    out[1] = w->solve_threads0 ? w->solve_threads0 : solve_threads(w->max_scene_bodies);
+    out[2] = w->solve_threads1;
+    out[3] = w->tune_trials;
+    out[4] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
     return NANS_OK;
 }
 
@@ -1851,9 +1853,9 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
 {
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
-    // sweep, [cull mask, cull write], cull scan, gjk, gjk_long, epa_tiny, [epa_tiny_resume],
-    // epa_medium, block EPA, giant EPA, solve (two passes)
-    uint32_t k = 10 + (w->cull_blocks > 0 ? 2u : 0u) + (w->dw.tiny_budget < 65 ? 1u : 0u);
+    // sweep, [cull mask, cull write], cull scan, gjk, gjk_long, epa_tiny, epa_medium, block
+    // EPA, giant EPA, solve (two passes)
+    uint32_t k = 10 + (w->cull_blocks > 0 ? 2u : 0u);
     if (batched)
         *batched = k;
     if (plain)

@@ -42,7 +42,6 @@ constexpr int kGroupSlots = kEpaMaxVerts * (kEpaMaxVerts + 1) / 2;
 constexpr int kGroupSlotsPad = (kGroupSlots + 31) & ~31;
 constexpr int kLargeThreads = 256;
 constexpr int kGiantMaxWarps = 4096;
-constexpr long long kBarrierSpins = 1ll << 24;
 
 enum
 {
@@ -113,6 +112,8 @@ struct GridTeam
     float *af;
     int *ai, *c1, *c2, *flag;
     GridBarrier *bar;
+    long long spins;   // polls before a wait gives up
+    unsigned extra;    // arrivals beyond the grid's blocks a barrier waits for (0)
     __device__ int rank() const { return blockIdx.x * blockDim.x + threadIdx.x; }
     __device__ int size() const { return gridDim.x * blockDim.x; }
     __device__ int warp() const { return rank() >> 5; }
@@ -132,7 +133,7 @@ struct GridTeam
             {
                 const unsigned g = atomicAdd(&bar->gen, 0u);
                 __threadfence();
-                if (atomicAdd(&bar->arrive, 1u) == gridDim.x - 1)
+                if (atomicAdd(&bar->arrive, 1u) == gridDim.x - 1 + extra)
                 {
                     atomicExch(&bar->arrive, 0u);
                     __threadfence();
@@ -143,7 +144,7 @@ struct GridTeam
                     long long spins = 0;
                     while (*vgen == g)
                     {
-                        if (*verr || ++spins > kBarrierSpins)
+                        if (*verr || ++spins > this->spins)
                         {
                             atomicExch(&bar->err, 1u);
                             ok = 0;
@@ -747,7 +748,7 @@ __global__ void __launch_bounds__(kLargeThreads) k_epa_block(DevWorld w)
 __global__ void __launch_bounds__(kLargeThreads) k_epa_giant(DevWorld w)
 {
     GiantScratch &S = *reinterpret_cast<GiantScratch *>(w.giant_scratch);
-    const GridTeam team{S.af, S.ai, S.c1, S.c2, &S.flag, &S.bar};
+    const GridTeam team{S.af, S.ai, S.c1, S.c2, &S.flag, &S.bar, w.barrier_spins, w.barrier_extra};
     GiantArena &E = *reinterpret_cast<GiantArena *>(w.epa_arena);
     const int n = min(w.work_counter[8], w.giant_cap);
     for (int q = 0; q < n; ++q)

@@ -628,24 +628,16 @@ __device__ __forceinline__ bool tiny_edge(TinySmem &S, int t, unsigned long long
     return true;
 }
 
-// The per-thread EPA's state between iterations: canonical vertex ids (4 bits each), the
-// closest face and its distance, face and vertex counts, the emptied-list flag and the next
-// iteration. With the polytope in TinySmem / TinyLocal it is all a resumed EPA needs.
-struct TinyRun
+// ResolveCollision (code/nans.cpp:787-904) by one thread; same results as epa_run.
+// `simp` is the GJK simplex as the GJK pass stored it (4 x (P, SupA, SupB), 36 floats).
+// The closest-face search of the next iteration is folded into the removal pass and the face
+// creation: a running minimum with strict '<' over the kept faces, then the new ones, in list
+// order, is the reference's scan (a NaN first distance keeps face 0, as its scan does).
+__device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, const Shape &B, const float *simp,
+                        v3 &out_pa, v3 &out_pb, v3 &out_n, int &iters)
 {
-    unsigned long long canon;
-    float cur;
-    int ci, nf, nv, it;
-    bool stale;
-};
-
-constexpr int EPA_BUDGET = 2; // the iteration budget ran out with the EPA still running
-
-// The GJK simplex as the GJK pass stored it (4 x (P, SupA, SupB), 36 floats) as the initial
-// tetrahedron: faces ABC, ACD, ADB, BDC (code/nans.cpp:799-802) and the closest of them.
-__device__ __forceinline__ void tiny_start(TinySmem &S, TinyLocal &L, int t, const float *simp, TinyRun &r)
-{
-    r.canon = 0ull;
+    TinyLocal L;
+    unsigned long long canon = 0ull;
     for (int i = 0; i < 4; ++i)
     {
         const float *q = simp + 9 * i;
@@ -653,64 +645,34 @@ __device__ __forceinline__ void tiny_start(TinySmem &S, TinyLocal &L, int t, con
         g.p = mk3(q[0], q[1], q[2]);
         g.sa = mk3(q[3], q[4], q[5]);
         g.sb = mk3(q[6], q[7], q[8]);
-        r.canon |= (unsigned long long)tiny_put(S, L, t, i, g, r.canon) << (4 * i);
+        canon |= (unsigned long long)tiny_put(S, L, t, i, g, canon) << (4 * i);
     }
     float cur = tiny_face(S, t, 0, 0, 1, 2);
     int ci = 0;
-    const float d1 = tiny_face(S, t, 1, 0, 2, 3);
-    if (d1 < cur)
     {
-        cur = d1;
-        ci = 1;
-    }
-    const float d2 = tiny_face(S, t, 2, 0, 3, 1);
-    if (d2 < cur)
-    {
-        cur = d2;
-        ci = 2;
-    }
-    const float d3 = tiny_face(S, t, 3, 1, 3, 2);
-    if (d3 < cur)
-    {
-        cur = d3;
-        ci = 3;
-    }
-    r.cur = cur;
-    r.ci = ci;
-    r.nf = 4;
-    r.nv = 4;
-    r.it = 0;
-    r.stale = false;
-}
-
-// ResolveCollision (code/nans.cpp:787-904) by one thread; same results as epa_run. Runs the
-// iterations r.it .. it_end - 1 (the reference's cap is iteration 64) and returns EPA_CONTACT
-// with the contact written, EPA_NONE, EPA_OVERFLOW when the polytope outgrows the per-thread
-// buffers, or EPA_BUDGET when iteration it_end is reached with the EPA still running (then r and
-// the polytope are the state at the start of iteration it_end). iters = the iterations run.
-// The closest-face search of the next iteration is folded into the removal pass and the face
-// creation: a running minimum with strict '<' over the kept faces, then the new ones, in list
-// order, is the reference's scan (a NaN first distance keeps face 0, as its scan does).
-__device__ int epa_tiny(const DevWorld &w, TinySmem &S, TinyLocal &L, int t, const Shape &A, const Shape &B,
-                        TinyRun &r, int it_end, v3 &out_pa, v3 &out_pb, v3 &out_n, int &iters)
-{
-    unsigned long long canon = r.canon;
-    float cur = r.cur;
-    int ci = r.ci, nf = r.nf, nv = r.nv;
-    bool stale = r.stale;
-    for (int it = r.it; it <= 64; ++it)
-    {
-        if (it >= it_end)
+        const float d1 = tiny_face(S, t, 1, 0, 2, 3);
+        if (d1 < cur)
         {
-            r.canon = canon;
-            r.cur = cur;
-            r.ci = ci;
-            r.nf = nf;
-            r.nv = nv;
-            r.it = it;
-            r.stale = stale;
-            return EPA_BUDGET;
+            cur = d1;
+            ci = 1;
         }
+        const float d2 = tiny_face(S, t, 2, 0, 3, 1);
+        if (d2 < cur)
+        {
+            cur = d2;
+            ci = 2;
+        }
+        const float d3 = tiny_face(S, t, 3, 1, 3, 2);
+        if (d3 < cur)
+        {
+            cur = d3;
+            ci = 3;
+        }
+    }
+    int nf = 4, nv = 4;
+    bool stale = false;
+    for (int it = 0; it <= 64; ++it)
+    {
         iters = it + 1;
         if (nf == 0 && !stale)
             return EPA_NONE;
@@ -813,86 +775,6 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, TinyLocal &L, int t, con
         ci = nci;
     }
     return EPA_NONE;
-}
-
-// Resume slots of budgeted per-thread EPAs: 32-bit words in field-major order ([word][slot],
-// so that the lanes of a warp, which take consecutive slots, move consecutive words).
-// Words: candidate, (ci | nf << 8 | nv << 16 | stale << 24), next iteration, cur, canon low /
-// high, then per vertex P, SupA, SupB (9 words), then per face the packed indices and the
-// normal (4 words).
-constexpr int kResHdr = 6;
-constexpr int kResWords = kResHdr + 9 * kTinyV + 4 * kTinyF;
-
-__device__ __forceinline__ void tiny_save(const DevWorld &w, const TinySmem &S, const TinyLocal &L, int t,
-                                          const TinyRun &r, int q, int c)
-{
-    const size_t R = (size_t)w.res_cap;
-    unsigned *u = reinterpret_cast<unsigned *>(w.epa_res) + q;
-    u[0 * R] = (unsigned)c;
-    u[1 * R] = (unsigned)r.ci | ((unsigned)r.nf << 8) | ((unsigned)r.nv << 16) | ((r.stale ? 1u : 0u) << 24);
-    u[2 * R] = (unsigned)r.it;
-    u[3 * R] = __float_as_uint(r.cur);
-    u[4 * R] = (unsigned)(r.canon & 0xffffffffull);
-    u[5 * R] = (unsigned)(r.canon >> 32);
-    for (int i = 0; i < r.nv; ++i)
-    {
-        unsigned *v = u + (size_t)(kResHdr + 9 * i) * R;
-        v[0 * R] = __float_as_uint(S.px[i][t]);
-        v[1 * R] = __float_as_uint(S.py[i][t]);
-        v[2 * R] = __float_as_uint(S.pz[i][t]);
-        v[3 * R] = __float_as_uint(L.sa[i][0]);
-        v[4 * R] = __float_as_uint(L.sa[i][1]);
-        v[5 * R] = __float_as_uint(L.sa[i][2]);
-        v[6 * R] = __float_as_uint(L.sb[i][0]);
-        v[7 * R] = __float_as_uint(L.sb[i][1]);
-        v[8 * R] = __float_as_uint(L.sb[i][2]);
-    }
-    for (int f = 0; f < r.nf; ++f)
-    {
-        unsigned *g = u + (size_t)(kResHdr + 9 * kTinyV + 4 * f) * R;
-        g[0 * R] = S.fidx[f][t];
-        g[1 * R] = __float_as_uint(S.fnx[f][t]);
-        g[2 * R] = __float_as_uint(S.fny[f][t]);
-        g[3 * R] = __float_as_uint(S.fnz[f][t]);
-    }
-}
-
-// Loads resume slot q into this thread's polytope; returns the candidate.
-__device__ __forceinline__ int tiny_load(const DevWorld &w, TinySmem &S, TinyLocal &L, int t, TinyRun &r, int q)
-{
-    const size_t R = (size_t)w.res_cap;
-    const unsigned *u = reinterpret_cast<const unsigned *>(w.epa_res) + q;
-    const int c = (int)u[0 * R];
-    const unsigned h = u[1 * R];
-    r.ci = (int)(h & 0xffu);
-    r.nf = (int)((h >> 8) & 0xffu);
-    r.nv = (int)((h >> 16) & 0xffu);
-    r.stale = ((h >> 24) & 1u) != 0;
-    r.it = (int)u[2 * R];
-    r.cur = __uint_as_float(u[3 * R]);
-    r.canon = (unsigned long long)u[4 * R] | ((unsigned long long)u[5 * R] << 32);
-    for (int i = 0; i < r.nv; ++i)
-    {
-        const unsigned *v = u + (size_t)(kResHdr + 9 * i) * R;
-        S.px[i][t] = __uint_as_float(v[0 * R]);
-        S.py[i][t] = __uint_as_float(v[1 * R]);
-        S.pz[i][t] = __uint_as_float(v[2 * R]);
-        L.sa[i][0] = __uint_as_float(v[3 * R]);
-        L.sa[i][1] = __uint_as_float(v[4 * R]);
-        L.sa[i][2] = __uint_as_float(v[5 * R]);
-        L.sb[i][0] = __uint_as_float(v[6 * R]);
-        L.sb[i][1] = __uint_as_float(v[7 * R]);
-        L.sb[i][2] = __uint_as_float(v[8 * R]);
-    }
-    for (int f = 0; f < r.nf; ++f)
-    {
-        const unsigned *g = u + (size_t)(kResHdr + 9 * kTinyV + 4 * f) * R;
-        S.fidx[f][t] = g[0 * R];
-        S.fnx[f][t] = __uint_as_float(g[1 * R]);
-        S.fny[f][t] = __uint_as_float(g[2 * R]);
-        S.fnz[f][t] = __uint_as_float(g[3 * R]);
-    }
-    return c;
 }
 
 // GJK and the per-thread EPA run as separate kernels. The GJK pass keeps its registers low
@@ -1013,30 +895,13 @@ __global__ void __launch_bounds__(kGjkThreads, 6) k_gjk_long(DevWorld w)
     }
 }
 
-// The end of one per-thread EPA: its length for the next step's queue order, then the contact
-// or the escalation to the warp tier.
-__device__ __forceinline__ void tiny_finish(const DevWorld &w, int c, int r, int iters, const v3 &pa, const v3 &pb,
-                                            const v3 &nn)
-{
-    w.epa_hist[w.cand_pidx[c]] = (unsigned char)(r == EPA_OVERFLOW ? 255 : iters);
-    if (r == EPA_OVERFLOW)
-        escalate(w, c, false);
-    else
-        write_result(w, c, r, pa, pb, nn);
-}
-
-// Tier 1 EPA, first pass: one thread per hit from the queue, at most w.tiny_budget iterations.
-// EPAs still running then are saved to a resume slot (consecutive slots for the lanes of a
-// warp, one atomic per warp) and finished by k_epa_tiny_resume, whose warps hold only such
-// long EPAs, instead of keeping 31 finished lanes of their warp idle. Without a free slot an
-// EPA runs to its end here. EPAs that outgrow the per-thread polytope are queued for the warp
-// tier.
+// Tier 1 EPA: one thread per hit from the queue; EPAs that outgrow the per-thread polytope
+// are queued for the warp tier.
 __global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
 {
     __shared__ TinySmem S;
     const int lane = threadIdx.x & 31, t = threadIdx.x;
     const int nl = w.work_counter[9], n = nl + w.work_counter[10];
-    const int budget = w.tiny_budget;
     for (;;)
     {
         int base = 0;
@@ -1046,71 +911,26 @@ __global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
         if (base >= n)
             break;
         const int i = base + lane;
-        const bool active = i < n;
-        int c = 0, r = EPA_NONE, iters = 0;
-        Shape A, B;
-        TinyRun run;
-        TinyLocal L;
-        v3 pa, pb, nn;
-        if (active)
-        {
-            c = w.s_order[i < nl ? w.cand_cap - 1 - i : i - nl]; // the long part first
-            A = load_shape(w, w.cand_a[c]);
-            B = load_shape(w, w.cand_b[c]);
-            tiny_start(S, L, t, reinterpret_cast<const float *>(w.s_k + 9 * (size_t)c), run);
-            r = epa_tiny(w, S, L, t, A, B, run, budget, pa, pb, nn, iters);
-        }
-        const bool more = active && r == EPA_BUDGET;
-        const unsigned bal = __ballot_sync(0xffffffffu, more);
-        int q = -1;
-        if (bal)
-        {
-            int q0 = 0;
-            const int leader = __ffs(bal) - 1;
-            if (lane == leader)
-                q0 = atomicAdd(w.work_counter + 14, __popc(bal));
-            q0 = __shfl_sync(0xffffffffu, q0, leader);
-            q = q0 + __popc(bal & ((1u << lane) - 1u));
-        }
-        if (more)
-        {
-            if (q < w.res_cap)
-            {
-                tiny_save(w, S, L, t, run, q, c);
-                continue;
-            }
-            r = epa_tiny(w, S, L, t, A, B, run, 65, pa, pb, nn, iters); // no slot: finish here
-        }
-        if (active)
-            tiny_finish(w, c, r, iters, pa, pb, nn);
-    }
-}
-
-// Tier 1 EPA, second pass: the EPAs the first pass saved, resumed where the budget stopped them.
-__global__ void __launch_bounds__(kTinyThreads) k_epa_tiny_resume(DevWorld w)
-{
-    __shared__ TinySmem S;
-    const int lane = threadIdx.x & 31, t = threadIdx.x;
-    const int n = min(w.work_counter[14], w.res_cap);
-    for (;;)
-    {
-        int base = 0;
-        if (lane == 0)
-            base = atomicAdd(w.work_counter + 15, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n)
-            break;
-        const int q = base + lane;
-        if (q >= n)
+        if (i >= n)
             continue;
-        TinyRun run;
-        TinyLocal L;
-        const int c = tiny_load(w, S, L, t, run, q);
+        const int slot = i < nl ? w.cand_cap - 1 - i : i - nl; // the long part first
+        if (!dev_check(w, slot >= 0 && slot < w.cand_cap, 12, slot, w.cand_cap))
+            continue;
+        const int c = w.s_order[slot];
+        if (!dev_check(w, c >= 0 && c < w.cand_cap, 13, c, w.cand_cap))
+            continue;
         const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
         v3 pa, pb, nn;
-        int iters = run.it;
-        const int r = epa_tiny(w, S, L, t, A, B, run, 65, pa, pb, nn, iters);
-        tiny_finish(w, c, r, iters, pa, pb, nn);
+        int iters = 0;
+        const int r =
+            epa_tiny(w, S, t, A, B, reinterpret_cast<const float *>(w.s_k + 9 * (size_t)c), pa, pb, nn, iters);
+        const int pidx = w.cand_pidx[c];
+        if (dev_check(w, pidx >= 0 && pidx < w.n_words * 32, 11, pidx, (long long)w.n_words * 32))
+            w.epa_hist[pidx] = (unsigned char)(r == EPA_OVERFLOW ? 255 : iters);
+        if (r == EPA_OVERFLOW)
+            escalate(w, c, false);
+        else
+            write_result(w, c, r, pa, pb, nn);
     }
 }
 
@@ -1193,11 +1013,7 @@ void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w)
     k_gjk<<<grid, kGjkThreads, 0, st>>>(w);
     k_gjk_long<<<grid, kGjkThreads, 0, st>>>(w);
     k_epa_tiny<<<w.tiny_blocks, kTinyThreads, 0, st>>>(w);
-    if (w.tiny_budget < 65)
-        k_epa_tiny_resume<<<w.tiny_blocks, kTinyThreads, 0, st>>>(w);
 }
-
-size_t epa_resume_words() { return (size_t)kResWords; }
 
 int tier_priority()
 {

@@ -36,6 +36,8 @@ enum StatusBits
     ST_EPA_EMPTY = 1u << 3,      // EPA face list emptied (reference would read a stale face)
     ST_SOLVER_BODIES = 1u << 4,  // scene too large for the solver's wave table
     ST_EPA_TIMEOUT = 1u << 5,    // a giant-tier grid barrier timed out (pair: no contact)
+    ST_CHECK = 1u << 6,          // a device bounds check failed and the access was skipped
+                                 // (the first failure is recorded in DevWorld::check)
 };
 
 struct EpaHandover; // nans_kernels.cuh
@@ -87,22 +89,21 @@ struct DevWorld
                                         // [8] giant-EPA queue length, [9] giant-EPA head,
                                         // [10] per-thread EPA queue length (queue: s_order),
                                         // [11] per-thread EPA head, [12] late-solve head,
-                                        // [13] late-scene count, [14] resume slots taken,
-                                        // [15] resume head
+                                        // [13] late-scene count
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
     int2 *long_cand;                    // candidates whose GJK needs the long pass: (c, n | it << 8)
     int medium_blocks;                  // warp-tier grid
     int tiny_blocks;                    // per-thread EPA grid (resident blocks on every SM)
-    int tiny_budget;                    // per-thread EPA iterations before an EPA is set aside
-                                        // for the resume pass (65: no budget)
-    unsigned *epa_res;                  // resume slots of budgeted per-thread EPAs
-    int res_cap;                        // resume slots
     int ovf_cap;                        // block-EPA queue capacity
     int *ovf_cand;                      // candidates queued for the block tier
     unsigned char *blk_arena;           // block-tier polytope buffers, one per block
     int blk_blocks;                     // block-tier grid
     int blk_face_limit;                 // block-tier face capacity (lowered only by a test flag)
+    long long barrier_spins;            // grid-wide tier: polls before a barrier wait gives up
+    unsigned barrier_extra;             // grid-wide tier: arrivals beyond the grid a barrier waits
+                                        // for (0; 1 only under a test flag, an arrival that never
+                                        // comes)
     int giant_cap;                      // giant-EPA queue capacity
     EpaHandover *handover;              // warp-tier states for the block tier (kHandoverSlots)
     int4 *giant_cand;                   // queued for the giant tier: candidate, state (it | bank << 8 |
@@ -129,6 +130,7 @@ struct DevWorld
     unsigned char *epa_hist;            // per pair-space index: iterations of its last per-thread EPA
     int *s_maxw;                        // per scene: highest wave of the last solve, or null
     unsigned *status;
+    int *check;                         // first failed bounds check: site, index, bound
 };
 
 // ------------------------------------------------------------------------------------
@@ -175,6 +177,21 @@ struct Shape
     float radius;
     int off, npts; // hull vertices; npts == 0 -> sphere
 };
+
+// A bounds check that records the first failure (site, index, bound) and lets the caller skip
+// the access instead of faulting.
+__device__ __forceinline__ bool dev_check(const DevWorld &w, bool ok, int site, long long idx, long long bound)
+{
+    if (ok)
+        return true;
+    if (!(atomicOr(w.status, (unsigned)ST_CHECK) & (unsigned)ST_CHECK))
+    {
+        w.check[0] = site;
+        w.check[1] = (int)idx;
+        w.check[2] = (int)bound;
+    }
+    return false;
+}
 
 __device__ __forceinline__ Shape load_shape(const DevWorld &w, int b)
 {

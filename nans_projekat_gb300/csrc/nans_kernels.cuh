@@ -58,6 +58,8 @@ struct EpaHandover
     float fnx[kEpaFastFaces], fny[kEpaFastFaces], fnz[kEpaFastFaces], fd[kEpaFastFaces];
 };
 constexpr int kGiantQueueCap = 4096;   // tier-4 EPAs queued per step
+constexpr long long kBarrierSpins = 1ll << 24; // grid barrier polls (64 ns sleeps) before it gives up
+constexpr long long kBarrierSpinsTest = 1ll << 12;
 constexpr int kWorkCounters = 16;
 constexpr int kEpaMediumCap = 1 << 20; // tier-2 EPAs queued per step
 
@@ -84,9 +86,6 @@ void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
 int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaError_t
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
 int epa_tiny_grid(int sm_count);   // resident blocks of the per-thread EPA on sm_count SMs
-size_t epa_resume_words();         // 32-bit words per resume slot of the per-thread EPA
-constexpr int kResumeSlotsMax = 1 << 19;
-constexpr int kTinyBudgetDefault = 4;
 int narrow_kernel_attrs();         // per-device kernel attributes (cudaError_t), set at world creation
 int large_kernel_attrs();
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);

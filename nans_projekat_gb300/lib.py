@@ -32,6 +32,7 @@ WORLD_ALL_PAIRS = 1
 WORLD_STRICT_EPA = 2
 WORLD_TEST_GIANT_TIER = 4
 WORLD_WARM_START = 8
+WORLD_TEST_BARRIER_TIMEOUT = 16
 
 # Every symbol include/nans_gb300.h declares.
 EXPORTS = (
@@ -143,10 +144,11 @@ class World:
     """
 
     def __init__(self, device=0, all_pairs=False, max_candidates=0, strict_epa=False, giant_tier_only=False,
-                 warm_start=False):
+                 warm_start=False, barrier_timeout_test=False):
         self.lib = load()
         flags = (WORLD_ALL_PAIRS if all_pairs else 0) | (WORLD_STRICT_EPA if strict_epa else 0) | \
-            (WORLD_TEST_GIANT_TIER if giant_tier_only else 0) | (WORLD_WARM_START if warm_start else 0)
+            (WORLD_TEST_GIANT_TIER if giant_tier_only else 0) | (WORLD_WARM_START if warm_start else 0) | \
+            (WORLD_TEST_BARRIER_TIMEOUT if barrier_timeout_test else 0)
         d = WorldDesc(device, flags, max_candidates)
         h = _P()
         _check(self.lib.nans_world_create(ctypes.byref(d), ctypes.byref(h)))
@@ -292,14 +294,13 @@ class World:
 
     def tuning(self):
         """The launch parameters in use (nans_batch_autotune's choice, or the defaults)."""
-        out = np.zeros(6, np.int32)
+        out = np.zeros(5, np.int32)
         _check(self.lib.nans_world_tuning(self.h, _ptr(out)))
-        return {"epa_budget": int(out[0]), "gjk_blocks_per_sm": int(out[1]), "solve_threads": int(out[2]),
-                "solve_threads_late": int(out[3]), "candidates_timed": int(out[4]),
-                "us_per_step": int(out[5])}
+        return {"gjk_blocks_per_sm": int(out[0]), "solve_threads": int(out[1]), "solve_threads_late": int(out[2]),
+                "candidates_timed": int(out[3]), "us_per_step": int(out[4])}
 
-    def set_tuning(self, epa_budget, gjk_blocks_per_sm, solve_threads, solve_threads_late):
-        a = np.array([epa_budget, gjk_blocks_per_sm, solve_threads, solve_threads_late], np.int32)
+    def set_tuning(self, gjk_blocks_per_sm, solve_threads, solve_threads_late):
+        a = np.array([gjk_blocks_per_sm, solve_threads, solve_threads_late], np.int32)
         _check(self.lib.nans_world_set_tuning(self.h, _ptr(a)))
 
     def path_counts(self):

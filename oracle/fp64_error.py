@@ -45,11 +45,12 @@ def errors(scene_list, checkpoints, threads=8):
 def table():
     rows = []
     rows.append(("C0 stack8 (8 cubes + sphere)", errors([scenes.stack_scene(0)], [1, 10, 60, 600])))
-    rows.append(("C1 random4608 (4,096 boxes + 512 spheres)", errors([scenes.random_scene(1)], [1, 5])))
+    rows.append(("C1 random4608 (4,096 boxes + 512 spheres)", errors([scenes.random_scene(1)], [1, 5, 20])))
     rows.append(("C2 stack_batch (64 of 16,384 scenes)",
                  errors(scenes.stack_batch(16384, seed=2)[::256], [1, 10, 60, 600])))
-    rows.append(("C3 grid33 (16 of 1,024 scenes)", errors(scenes.grid_stack_batch(16, seed=3), [1, 10, 120])))
-    rows.append(("C4 mixed (16 of 4,096 scenes)", errors(scenes.mixed_batch(16, seed=4), [1, 10, 240])))
+    rows.append(("C3 grid33 (64 of 1,024 scenes)",
+                 errors(scenes.grid_stack_batch(1024, seed=3)[::16], [1, 10, 120])))
+    rows.append(("C4 mixed (64 of 4,096 scenes)", errors(scenes.mixed_batch(4096, seed=4)[::64], [1, 10, 240])))
     return rows
 
 

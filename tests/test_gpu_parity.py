@@ -417,11 +417,10 @@ def test_full_size_batch_samples_match_oracle(nl, oracle_lib):
         assert same_fields(o.pairs(j), w.pairs(i), PAIR_FIELDS)[0], i
 
 
-@pytest.mark.parametrize("tuning", [(65, 0, 32, 128), (1, 0, 32, 128), (2, 4, 64, 256), (4, 0, 32, 128)])
+@pytest.mark.parametrize("tuning", [(0, 32, 128), (4, 64, 256), (2, 32, 64)])
 def test_results_do_not_depend_on_launch_parameters(nl, oracle_lib, tuning):
-    """The per-thread EPA's iteration budget (1: nearly every EPA goes through the resume pass; 65:
-    none), the GJK blocks per SM and the solver's threads per scene change the schedule, never the
-    result: 256 workload scenes for 40 steps against the oracle, bit for bit."""
+    """The GJK blocks per SM and the solver's threads per scene (both passes) change the schedule,
+    never the result: 256 workload scenes for 40 steps against the oracle, bit for bit."""
     batch = scenes.stack_batch(16384, seed=2)[:256]
     dt = np.float32(1 / 60)
     w = nl.World()
@@ -430,7 +429,7 @@ def test_results_do_not_depend_on_launch_parameters(nl, oracle_lib, tuning):
     w.batch_step(dt, 40, graph_steps=20)
     assert w.status() == 0
     t = w.tuning()
-    assert (t["epa_budget"], t["gjk_blocks_per_sm"], t["solve_threads"], t["solve_threads_late"]) == tuning
+    assert (t["gjk_blocks_per_sm"], t["solve_threads"], t["solve_threads_late"]) == tuning
     state = w.download()
     o = _oracle_states(batch, 40, dt)
     for i in range(len(batch)):
@@ -442,35 +441,6 @@ def test_results_do_not_depend_on_launch_parameters(nl, oracle_lib, tuning):
     w.close()
 
 
-def test_epa_resume_slots_exhausted(nl, oracle_lib):
-    """With fewer resume slots than budgeted EPAs (a world keeps resume slots for half its
-    candidate capacity; with a one-iteration budget nearly every EPA asks for one), the EPAs
-    without a slot finish in the first pass: the same result, bit for bit."""
-    batch = scenes.stack_batch(16384, seed=2)[:8]
-    dt = np.float32(1 / 60)
-    probe = nl.World()
-    probe.upload_batch(batch)
-    cap = 0
-    for _ in range(20):
-        probe.batch_step(dt, 1, 1)
-        cap = max(cap, probe.counts()[0])
-    probe.close()
-    w = nl.World(max_candidates=cap)
-    w.upload_batch(batch)
-    w.set_tuning(1, 0, 32, 128)
-    w.batch_step(dt, 20, graph_steps=10)
-    assert w.status() == 0
-    n_cand, n_contacts = w.counts()
-    assert n_contacts > cap // 2  # more EPAs than resume slots
-    state = w.download()
-    o = _oracle_states(batch, 20, dt)
-    for i in range(len(batch)):
-        cubes, spheres, _ = w.scene_state(i, state)
-        assert same_fields(o.state(i)[0], cubes, STATE_FIELDS)[0], i
-        assert same_fields(o.pairs(i), w.pairs(i), PAIR_FIELDS)[0], i
-    w.close()
-
-
 def test_autotuner_times_every_candidate(nl):
     batch = scenes.stack_batch(16384, seed=2)[:512]
     w = nl.World()
@@ -478,6 +448,41 @@ def test_autotuner_times_every_candidate(nl):
     w.step(np.float32(1 / 60), 2)
     w.autotune(np.float32(1 / 60))
     t = w.tuning()
-    assert t["candidates_timed"] == 10 and t["us_per_step"] > 0
-    assert t["epa_budget"] in (3, 4, 6, 65) and t["solve_threads"] in (32, 64)
+    assert t["candidates_timed"] == 6 and t["us_per_step"] > 0
+    assert t["gjk_blocks_per_sm"] in (0, 4) and t["solve_threads"] in (32, 64)
+    w.close()
+
+
+def test_giant_tier_barrier_timeout_is_reported(nl, oracle_lib):
+    """The grid-wide EPA tier's barrier waits are bounded. With NANS_WORLD_TEST_BARRIER_TIMEOUT a
+    barrier waits for one arrival more than the grid has (an arrival that never comes) and gives
+    up after 4,096 polls: the step must return NANS_ERR_EPA_CAPACITY with the timeout bit set,
+    and the GPU must keep answering (a following world steps bit-exactly against the oracle)."""
+    raised = 0
+    for case in LARGE_EPA_CASES:
+        scene, meta, _, _ = load_golden(case)
+        dt = np.float32(scene.constants.dt)
+        probe = nl.World(giant_tier_only=True)
+        probe.upload(scene)
+        probe.step(dt, meta["nsteps"])
+        ran = probe.epa_stats()["giant_tier"]
+        probe.close()
+        if ran == 0:
+            continue
+        w = nl.World(giant_tier_only=True, barrier_timeout_test=True)
+        w.upload(scene)
+        with pytest.raises(nl.NansError) as e:
+            for _ in range(meta["nsteps"]):
+                w.step(dt, 1)
+        assert e.value.code == 5 and "timed out" in str(e.value)
+        assert w.status() & (1 << 5)
+        w.close()
+        raised += 1
+    assert raised >= 1
+    sc = scenes.stack_scene(0)
+    w = nl.World()
+    w.upload(sc)
+    w.step(np.float32(1 / 60), 30)
+    o = _oracle_states([sc], 30, np.float32(1 / 60))
+    assert same_fields(o.state(0)[0], w.download()[0], STATE_FIELDS)[0]
     w.close()
