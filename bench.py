@@ -352,11 +352,31 @@ def single_scene_line(lib, device, scene, name, gpu_steps, cpu_steps):
     return out
 
 
+def gjk_schedule_ab(lib, batch, device, warm=25, n=10):
+    """A/B of the GJK schedule on identical windows of the workload: one thread per candidate
+    pair (32 pairs per warp; the library's default) against one warp per pair (the supports
+    evaluated across the lanes). Both worlds step the same scenes to the same state, then the
+    per-stage device time of n eager steps is taken (nans_profile_steps): the narrowphase stage
+    holds GJK and the per-thread EPA, which is the same kernel in both."""
+    names = ["sweep", "cull", "gjk_and_thread_epa", "warp_epa", "large_epa", "solve"]
+    out = {}
+    for key, flag in (("thread_per_pair", False), ("warp_per_pair", True)):
+        w = lib.World(device=device, gjk_warp=flag)
+        w.upload_batch(batch)
+        w.batch_step(DT, warm, 1)
+        ms = w.profile(DT, n) / n
+        out[key] = {nm: float(x) for nm, x in zip(names, ms)}
+        w.close()
+    out["window"] = "steps %d-%d of the workload, %d eager steps each" % (warm + 1, warm + n, n)
+    return out
+
+
 def secondary_measurements(lib, batch, device):
     """Plain path vs batched path on the same scenes, and the single large scene."""
     import torch
     from nans_projekat_gb300 import scenes
     out = {}
+    out["gjk_schedule_ab"] = gjk_schedule_ab(lib, batch, device)
     out["c0_plain"] = single_scene_line(lib, device, scenes.stack_scene(0), "stack8: 8 unit cubes + 1 sphere",
                                         600, 600)
     out["c1_plain"] = single_scene_line(lib, device, scenes.random_scene(1),

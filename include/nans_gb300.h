@@ -126,6 +126,10 @@ typedef struct nans_contact_pair
                                       NANS_ERR_EPA_CAPACITY with the timeout status bit. Use with
                                       NANS_WORLD_TEST_GIANT_TIER. The reference caps its loops
                                       instead (code/nans.cpp:804, 915). */
+#define NANS_WORLD_GJK_WARP 32u    /* GJK with one warp per candidate pair, the support maps
+                                      evaluated across the lanes; default: one thread per pair,
+                                      32 pairs per warp (faster on the benchmark workload).
+                                      Results are the same. */
 #define NANS_WORLD_WARM_START 8u   /* warm starting, the reference's TODO at its pair dedupe
                                       (code/nans.cpp:1386-1389): a pair (type, IndexA,
                                       IndexB) that was in contact at the previous step starts

@@ -473,6 +473,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     w->gjk_cap_blocks = upto(128, INT32_MAX);
     d.medium_blocks = upto(4, 2 * w->sm_count);
     d.tiny_blocks = upto(64, epa_tiny_grid(w->sm_count));
+    d.gjk_warp = (w->flags & NANS_WORLD_GJK_WARP) ? 1 : 0;
+    d.sm_count = w->sm_count;
     d.giant_blocks = std::min(giant_grid(w->sm_count), upto(1, INT32_MAX) < 4096 ? 16 : INT32_MAX);
     d.blk_blocks = upto(1, kBlockPerSm * w->sm_count);
     d.blk_face_limit = (w->flags & NANS_WORLD_TEST_GIANT_TIER) ? 0 : kBlockFaces;

@@ -895,6 +895,125 @@ __global__ void __launch_bounds__(kGjkThreads, 6) k_gjk_long(DevWorld w)
     }
 }
 
+// ---------------------------------------------------------------------------------------
+// GJK with one warp per candidate pair: the support maps evaluated across the warp (lanes
+// 0-15 hold shape A's vertices, lanes 16-31 shape B's, each half reduced to the first maximum
+// by shuffles), the simplex cases run by every lane on the broadcast values. The same result
+// as k_gjk bit for bit; an alternative schedule for the A/B against one thread per pair
+// (NANS_WORLD_GJK_WARP), which keeps 32 pairs per warp instruction stream instead of one.
+// ---------------------------------------------------------------------------------------
+struct WarpSupport
+{
+    const float *verts;
+    const Shape &A, &B;
+    v3 v;      // this lane's vertex: A's vertex lane (lanes 0-15) or B's vertex lane - 16
+    bool have; // this lane holds a vertex of its half's shape
+    int lane;
+
+    // First maximum of dot(vertex, d) over a half's lanes (NaN and values not above -FLT_MAX
+    // never win; ties go to the lower index): the sequential scan's vertex.
+    __device__ __forceinline__ int half_support(v3 d) const
+    {
+        float best = -FLT_MAX;
+        int bi = -1;
+        if (have)
+        {
+            const float dist = dot3(v, d);
+            if (dist > best)
+            {
+                best = dist;
+                bi = lane & 15;
+            }
+        }
+        for (int o = 8; o > 0; o >>= 1)
+        {
+            const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+            const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+            if (oi >= 0 && (bi < 0 || ob > best || (ob == best && oi < bi)))
+            {
+                best = ob;
+                bi = oi;
+            }
+        }
+        return bi; // the vertex's index in the half, -1 for none; the caller fetches the vertex
+    }
+
+    __device__ __forceinline__ GV operator()(v3 d) const
+    {
+        const v3 nd = -1.0f * d;
+        // both halves reduce in the same instructions, each against its own direction
+        const v3 mine = (lane < 16) ? d : nd;
+        const int bi = half_support(mine);
+        const int ia = __shfl_sync(0xffffffffu, bi, 0), ib = __shfl_sync(0xffffffffu, bi, 16);
+        const float ax = __shfl_sync(0xffffffffu, v.x, ia < 0 ? 0 : ia), ay = __shfl_sync(0xffffffffu, v.y, ia < 0 ? 0 : ia),
+                    az = __shfl_sync(0xffffffffu, v.z, ia < 0 ? 0 : ia);
+        const float bx = __shfl_sync(0xffffffffu, v.x, 16 + (ib < 0 ? 0 : ib)),
+                    by = __shfl_sync(0xffffffffu, v.y, 16 + (ib < 0 ? 0 : ib)),
+                    bz = __shfl_sync(0xffffffffu, v.z, 16 + (ib < 0 ? 0 : ib));
+        GV r;
+        if (A.npts == 0)
+            r.sa = sphere_support(A.p, A.radius, d);
+        else if (A.npts > 16)
+            r.sa = hull_support(verts, A.off, A.npts, d);
+        else
+            r.sa = ia >= 0 ? mk3(ax, ay, az) : mk3(0.0f, 0.0f, 0.0f);
+        if (B.npts == 0)
+            r.sb = sphere_support(B.p, B.radius, nd);
+        else if (B.npts > 16)
+            r.sb = hull_support(verts, B.off, B.npts, nd);
+        else
+            r.sb = ib >= 0 ? mk3(bx, by, bz) : mk3(0.0f, 0.0f, 0.0f);
+        r.p = r.sa - r.sb;
+        return r;
+    }
+};
+
+constexpr int kGjkWarpThreads = 128;
+__global__ void __launch_bounds__(kGjkWarpThreads) k_gjk_warp(DevWorld w)
+{
+    const int lane = threadIdx.x & 31;
+    const int n = *w.n_cand;
+    for (;;)
+    {
+        int c = 0;
+        if (lane == 0)
+            c = atomicAdd(w.work_counter, 1);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= n)
+            break;
+        if (lane == 0)
+        {
+            const int sc = w.cand_meta[c] >> 3;
+            if (c == 0 || (w.cand_meta[c - 1] >> 3) != sc)
+                w.cand_begin[sc] = c;
+            if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
+                w.cand_end[sc] = c + 1;
+        }
+        const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
+        const Shape &S = lane < 16 ? A : B;
+        const int t = lane & 15;
+        const bool have = S.npts > 0 && S.npts <= 16 && t < S.npts;
+        v3 v = mk3(0.0f, 0.0f, 0.0f);
+        if (have)
+            v = mk3(__ldg(w.verts + S.off + 3 * t), __ldg(w.verts + S.off + 3 * t + 1), __ldg(w.verts + S.off + 3 * t + 2));
+        GV s0 = {}, s1 = {}, s2 = {}, s3 = {};
+        int np = 0, it = 0;
+        const int g = gjk_from_with(WarpSupport{w.verts, A, B, v, have, lane}, A, B, s0, s1, s2, s3, np, it, 65);
+        if (lane == 0)
+        {
+            if (g == G_FOUND)
+            {
+                store_simplex(w, c, s0, s1, s2, s3);
+                const bool lng = w.epa_hist[w.cand_pidx[c]] > kEpaLongIters;
+                const int k = atomicAdd(w.work_counter + (lng ? 9 : 10), 1);
+                w.s_order[lng ? w.cand_cap - 1 - k : k] = c;
+            }
+            else
+                w.hit[c] = 0;
+        }
+    }
+}
+
 // Tier 1 EPA: one thread per hit from the queue; EPAs that outgrow the per-thread polytope
 // are queued for the warp tier.
 __global__ void __launch_bounds__(kTinyThreads) k_epa_tiny(DevWorld w)
@@ -1001,6 +1120,15 @@ int narrow_blocks_per_sm(int warps)
     return per;
 }
 
+// Resident blocks of the warp-per-pair GJK on every SM, no more than the pairs need.
+static int gjk_warp_grid(const DevWorld &w)
+{
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_gjk_warp, kGjkWarpThreads, 0);
+    const long long need = (w.pair_total + kGjkWarpThreads / 32 - 1) / (kGjkWarpThreads / 32);
+    return (int)std::max(1LL, std::min<long long>((long long)std::max(1, per) * w.sm_count, need));
+}
+
 int epa_tiny_grid(int sm_count)
 {
     int per = 0;
@@ -1010,8 +1138,13 @@ int epa_tiny_grid(int sm_count)
 
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w)
 {
-    k_gjk<<<grid, kGjkThreads, 0, st>>>(w);
-    k_gjk_long<<<grid, kGjkThreads, 0, st>>>(w);
+    if (w.gjk_warp)
+        k_gjk_warp<<<gjk_warp_grid(w), kGjkWarpThreads, 0, st>>>(w);
+    else
+    {
+        k_gjk<<<grid, kGjkThreads, 0, st>>>(w);
+        k_gjk_long<<<grid, kGjkThreads, 0, st>>>(w);
+    }
     k_epa_tiny<<<w.tiny_blocks, kTinyThreads, 0, st>>>(w);
 }
 

@@ -19,8 +19,9 @@ __device__ __forceinline__ v3 triple_cross(v3 a, v3 b, v3 c) { return (dot3(c, a
 // CheckCollision's GJK loop (at most 65 EvolveSimplex calls) from call `it` with the simplex
 // (s0..s3, n points). With budget < 65 it stops before call `budget` and returns G_BUDGET if
 // the simplex is still evolving; (simplex, n, it) then resume it exactly.
-__device__ __forceinline__ int gjk_from(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,
-                                        GV &s3, int &n, int &it, int budget)
+template <class Support>
+__device__ __forceinline__ int gjk_from_with(const Support &support, const Shape &A, const Shape &B, GV &s0, GV &s1,
+                                             GV &s2, GV &s3, int &n, int &it, int budget)
 {
     const v3 dir0 = normalize3(B.p - A.p);
     int res = G_EVOLVING;
@@ -144,7 +145,7 @@ __device__ __forceinline__ int gjk_from(const float *verts, const Shape &A, cons
         }
         if (len3(dir) <= 0.0001f)
             return G_NOHIT;
-        GV nv = minkowski_support(verts, A, B, dir);
+        GV nv = support(dir);
         if (n == 0)
             s0 = nv;
         else if (n == 1)
@@ -159,6 +160,20 @@ __device__ __forceinline__ int gjk_from(const float *verts, const Shape &A, cons
             return res;
     }
     return G_NOHIT; // iteration cap reached while still evolving: no collision
+}
+
+// The support of one thread: minkowski_support over the shapes' vertices in global memory.
+struct ThreadSupport
+{
+    const float *verts;
+    const Shape &A, &B;
+    __device__ __forceinline__ GV operator()(v3 d) const { return minkowski_support(verts, A, B, d); }
+};
+
+__device__ __forceinline__ int gjk_from(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,
+                                        GV &s3, int &n, int &it, int budget)
+{
+    return gjk_from_with(ThreadSupport{verts, A, B}, A, B, s0, s1, s2, s3, n, it, budget);
 }
 
 __device__ __forceinline__ int gjk(const float *verts, const Shape &A, const Shape &B, GV &s0, GV &s1, GV &s2,

@@ -95,6 +95,8 @@ struct DevWorld
     int2 *long_cand;                    // candidates whose GJK needs the long pass: (c, n | it << 8)
     int medium_blocks;                  // warp-tier grid
     int tiny_blocks;                    // per-thread EPA grid (resident blocks on every SM)
+    int gjk_warp;                       // 1: GJK with one warp per pair (NANS_WORLD_GJK_WARP)
+    int sm_count;
     int ovf_cap;                        // block-EPA queue capacity
     int *ovf_cand;                      // candidates queued for the block tier
     unsigned char *blk_arena;           // block-tier polytope buffers, one per block

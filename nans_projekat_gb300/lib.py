@@ -33,6 +33,7 @@ WORLD_STRICT_EPA = 2
 WORLD_TEST_GIANT_TIER = 4
 WORLD_WARM_START = 8
 WORLD_TEST_BARRIER_TIMEOUT = 16
+WORLD_GJK_WARP = 32
 
 # Every symbol include/nans_gb300.h declares.
 EXPORTS = (
@@ -144,11 +145,11 @@ class World:
     """
 
     def __init__(self, device=0, all_pairs=False, max_candidates=0, strict_epa=False, giant_tier_only=False,
-                 warm_start=False, barrier_timeout_test=False):
+                 warm_start=False, barrier_timeout_test=False, gjk_warp=False):
         self.lib = load()
         flags = (WORLD_ALL_PAIRS if all_pairs else 0) | (WORLD_STRICT_EPA if strict_epa else 0) | \
             (WORLD_TEST_GIANT_TIER if giant_tier_only else 0) | (WORLD_WARM_START if warm_start else 0) | \
-            (WORLD_TEST_BARRIER_TIMEOUT if barrier_timeout_test else 0)
+            (WORLD_TEST_BARRIER_TIMEOUT if barrier_timeout_test else 0) | (WORLD_GJK_WARP if gjk_warp else 0)
         d = WorldDesc(device, flags, max_candidates)
         h = _P()
         _check(self.lib.nans_world_create(ctypes.byref(d), ctypes.byref(h)))

@@ -9,7 +9,7 @@ through oracle/refbind.py and records, per case:
   states     full body records at a few steps
   pairs      the contact lists at the same steps
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [stack_bigepa_<scene>]
 """
 import json
 import os
@@ -97,7 +97,20 @@ def main():
         run_world("stack_emptied_%d" % idx, batch[idx], 20, {20}, "refbig")
     for idx in (3029, 7755, 6880):
         run_world("stack_bigepa_%d" % idx, batch[idx], 30, {30}, "refbig")
+    # scene 897 grows an EPA polytope beyond 256 faces (1,150) within 60 steps: it reaches the
+    # block-wide tier (and, in worlds that route those to it, the grid-wide tier)
+    run_world("stack_bigepa_897", batch[897], 60, {60}, "refbig")
+
+
+def main_one(name):
+    """Regenerates one fixture of the stack workload by its scene index (stack_bigepa_<i>)."""
+    batch = scenes.stack_batch(16384, seed=2)
+    idx = int(name.rsplit("_", 1)[1])
+    run_world(name, batch[idx], 60 if idx == 897 else 30, {60 if idx == 897 else 30}, "refbig")
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1:
+        main_one(sys.argv[1])
+    else:
+        main()

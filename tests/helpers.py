@@ -67,7 +67,7 @@ def first_difference(a, b, fields):
 GOLDEN_CASES = ("stack8_seed0", "stack8_refconst", "demo_frames", "stack_random_5", "stack_random_12",
                 "stack_random_40", "stack_random_90", "random_mixed72", "random_dense16",
                 "stack_emptied_6663", "stack_emptied_5642", "stack_bigepa_3029", "stack_bigepa_7755",
-                "stack_bigepa_6880")
+                "stack_bigepa_6880", "stack_bigepa_897")
 
 
 def load_golden(name):

@@ -467,6 +467,8 @@ def test_giant_tier_barrier_timeout_is_reported(nl, oracle_lib):
         probe.step(dt, meta["nsteps"])
         ran = probe.epa_stats()["giant_tier"]
         probe.close()
+        if case == "stack_bigepa_897":
+            assert ran >= 1  # its 1,150-face EPA leaves the warp tier
         if ran == 0:
             continue
         w = nl.World(giant_tier_only=True, barrier_timeout_test=True)
@@ -486,3 +488,24 @@ def test_giant_tier_barrier_timeout_is_reported(nl, oracle_lib):
     o = _oracle_states([sc], 30, np.float32(1 / 60))
     assert same_fields(o.state(0)[0], w.download()[0], STATE_FIELDS)[0]
     w.close()
+
+
+def test_warp_per_pair_gjk_matches_oracle(nl, oracle_lib):
+    """GJK with one warp per candidate pair (NANS_WORLD_GJK_WARP: supports evaluated across the
+    lanes, first-maximum shuffle reductions) gives the one-thread-per-pair result: 256 workload
+    scenes for 40 steps against the oracle, bit for bit, with a convex-hull batch as well."""
+    dt = np.float32(1 / 60)
+    for batch in (scenes.stack_batch(16384, seed=2)[:256], scenes.mixed_batch(64, seed=4)):
+        w = nl.World(gjk_warp=True)
+        w.upload_batch(batch)
+        w.batch_step(dt, 40, graph_steps=20)
+        assert w.status() == 0
+        state = w.download()
+        o = _oracle_states(batch, 40, dt)
+        for i in range(len(batch)):
+            cubes, spheres, _ = w.scene_state(i, state)
+            assert same_fields(o.state(i)[0], cubes, STATE_FIELDS)[0], (i, first_difference(o.state(i)[0], cubes,
+                                                                                             STATE_FIELDS))
+            assert same_fields(o.state(i)[1], spheres, STATE_FIELDS)[0], i
+            assert same_fields(o.pairs(i), w.pairs(i), PAIR_FIELDS)[0], i
+        w.close()
