@@ -77,8 +77,8 @@ def parse():
     p.add_argument("--no-secondary", action="store_true",
                    help="skip the plain-path and single-large-scene measurements")
     p.add_argument("--fit-full", action="store_true",
-                   help="only the gradient fit at full size (4,096 mixed scenes x 240 steps x 50 Adam "
-                        "steps) with checkpointed rollouts; prints its own JSON line")
+                   help="only the gradient fit at full size (4,096 mixed scenes x 240 steps x 50 Adam steps "
+                        "fitting per-scene masses) with checkpointed rollouts; prints its own JSON line")
     p.add_argument("--checkpoint-every", type=int, default=20,
                    help="steps per rollout segment for --fit-full")
     return p.parse_args()
@@ -352,17 +352,19 @@ def single_scene_line(lib, device, scene, name, gpu_steps, cpu_steps):
     return out
 
 
-def gjk_schedule_ab(lib, batch, device, warm=25, n=10):
-    """A/B of the GJK schedule on identical windows of the workload: one thread per candidate
-    pair (32 pairs per warp; the library's default) against one warp per pair (the supports
-    evaluated across the lanes). Both worlds step the same scenes to the same state, then the
-    per-stage device time of n eager steps is taken (nans_profile_steps): the narrowphase stage
-    holds GJK and the per-thread EPA, which is the same kernel in both."""
+def schedule_ab(lib, batch, device, warm=25, n=10):
+    """A/B of schedules on identical windows of the workload (each world steps the same scenes to
+    the same state, then the per-stage device time of n eager steps is taken with
+    nans_profile_steps): the library's defaults (GJK one thread per candidate pair, cube-cube cull
+    by 32 x 32 tiles) against GJK with one warp per pair (the supports evaluated across the
+    lanes) and against the cull with one lane per pair. Results are the same in all three."""
     names = ["sweep", "cull", "gjk_and_thread_epa", "warp_epa", "large_epa", "solve"]
     out = {}
-    for key, flag in (("thread_per_pair", False), ("warp_per_pair", True)):
-        w = lib.World(device=device, gjk_warp=flag)
+    for key, warp, tiles in (("default", False, 1), ("gjk_warp_per_pair", True, 1), ("cull_lane_per_pair", False, 0)):
+        w = lib.World(device=device, gjk_warp=warp)
         w.upload_batch(batch)
+        t = w.tuning()
+        w.set_tuning(t["gjk_blocks_per_sm"], t["solve_threads"], t["solve_threads_late"], tiles)
         w.batch_step(DT, warm, 1)
         ms = w.profile(DT, n) / n
         out[key] = {nm: float(x) for nm, x in zip(names, ms)}
@@ -376,7 +378,7 @@ def secondary_measurements(lib, batch, device):
     import torch
     from nans_projekat_gb300 import scenes
     out = {}
-    out["gjk_schedule_ab"] = gjk_schedule_ab(lib, batch, device)
+    out["schedule_ab"] = schedule_ab(lib, batch, device)
     out["c0_plain"] = single_scene_line(lib, device, scenes.stack_scene(0), "stack8: 8 unit cubes + 1 sphere",
                                         600, 600)
     out["c1_plain"] = single_scene_line(lib, device, scenes.random_scene(1),
@@ -475,6 +477,58 @@ def fit_measurement(lib, device, n_scenes=1024, nsteps=120, iters=20, checkpoint
     if checkpoint_every:
         out["checkpoint_every"] = int(checkpoint_every)
     return out
+
+
+def mass_fit_measurement(lib, device, n_scenes=4096, nsteps=240, iters=50, checkpoint_every=20):
+    """The batched + differentiated configuration: 4,096 mixed scenes (8-128 boxes, spheres and
+    convex hulls), 240 steps, then Adam steps fitting one mass scale per scene (every body's
+    mass and moment of inertia times exp(theta_s)) so that the final positions match a target
+    rollout whose scenes have seeded mass scales exp(U[-0.2, 0.2]). Each Adam step is a forward
+    rollout and its adjoint in one batched launch sequence (checkpointed every
+    `checkpoint_every` steps, one segment's tape on the GPU at a time). Bodies whose target or
+    current position is non-finite or beyond 10 km (bodies the reference's solver flings away)
+    are left out of the loss."""
+    import torch
+    from nans_projekat_gb300 import diff, scenes
+    batch = scenes.mixed_batch(n_scenes, seed=4)
+    w = lib.World(device=device)
+    P0, A0, V0, W0, m0, cr, cf = diff.initial_state(batch)
+    scene_of = torch.tensor(np.concatenate([np.full(len(s.cubes), i) for i, s in enumerate(batch)] +
+                                           [np.full(len(s.spheres), i) for i, s in enumerate(batch)]), dtype=torch.long)
+    rng = np.random.default_rng(44)
+    theta_true = torch.tensor(rng.uniform(-0.2, 0.2, n_scenes), dtype=torch.float32)
+    with torch.no_grad():
+        target = diff.rollout(w, batch, DT, nsteps, P0, A0, V0, W0, m0 * torch.exp(theta_true)[scene_of], cr, cf,
+                              checkpoint_every=checkpoint_every)[0]
+    keep0 = torch.isfinite(target).all(dim=1) & (target.abs() < 1e4).all(dim=1)
+    theta = torch.zeros(n_scenes, requires_grad=True)
+    opt = torch.optim.Adam([theta], lr=0.02)
+    losses, errs = [], []
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        opt.zero_grad()
+        P = diff.rollout(w, batch, DT, nsteps, P0, A0, V0, W0, m0 * torch.exp(theta)[scene_of], cr, cf,
+                         checkpoint_every=checkpoint_every)[0]
+        ok = keep0 & torch.isfinite(P).all(dim=1) & (P.abs() < 1e4).all(dim=1)
+        loss = ((P[ok] - target[ok]) ** 2).sum() / max(1, int(ok.sum()))
+        loss.backward()
+        with torch.no_grad():
+            theta.grad[~torch.isfinite(theta.grad)] = 0.0
+        opt.step()
+        losses.append(float(loss.detach()))
+        errs.append(float((theta.detach() - theta_true).abs().mean()))
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    bodies = int(V0.shape[0])
+    w.close()
+    return {"workload": "mixed%d: %d scenes of 8-128 boxes, spheres and convex hulls" % (n_scenes, n_scenes),
+            "bodies": bodies, "steps": nsteps, "adam_steps": iters, "checkpoint_every": checkpoint_every,
+            "fitted": "one mass scale per scene (4,096 parameters), target scales exp(U[-0.2, 0.2])",
+            "s_per_adam_step": t / iters, "forward_backward_value": bodies * nsteps * iters / t, "unit": UNIT,
+            "loss_first": losses[0], "loss_last": losses[-1], "loss_min": min(losses),
+            "mean_abs_log_scale_error_first": errs[0], "mean_abs_log_scale_error_last": errs[-1],
+            "bodies_in_loss": int(keep0.sum()), "losses": losses[::5]}
 
 
 def differentiable_measurement(lib, device):
@@ -739,9 +793,10 @@ def run_fit_full(args):
         raise SystemExit("bench.py needs a CUDA device")
     torch.cuda.set_device(0)
     from nans_projekat_gb300 import lib
-    r = fit_measurement(lib, 0, n_scenes=4096, nsteps=240, iters=50, checkpoint_every=args.checkpoint_every)
-    emit({"metric": "body-steps/s (taped forward + adjoint, Adam fit)", "value": r["forward_backward_value"],
-          "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+    r = mass_fit_measurement(lib, 0, n_scenes=4096, nsteps=240, iters=50, checkpoint_every=args.checkpoint_every)
+    emit({"metric": "body-steps/s (taped forward + adjoint, Adam fit of per-scene masses)",
+          "value": r["forward_backward_value"], "unit": UNIT, "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+          "data": "synthetic (seeded)",
           "config": {"workload": r["workload"], "bodies": r["bodies"], "steps": r["steps"],
                      "adam_steps": r["adam_steps"], "checkpoint_every": args.checkpoint_every},
           "fit": r})

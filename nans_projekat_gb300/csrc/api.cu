@@ -91,6 +91,7 @@ struct nans_world
     long long steps_run = 0;
 
     int narrow_bpsm = 0;     // GJK blocks per SM (0 = occupancy limit)
+    int cull_tiles = 1;      // cull by tiles (1) or one lane per pair (0)
     int gjk_cap_blocks = 1;  // GJK blocks the world's pairs can keep busy
     int solve_threads0 = 0;  // solver threads per scene, first pass (0 = by the largest scene)
     int solve_threads1 = kSolveLateThreads; // solver threads per late scene
@@ -174,7 +175,7 @@ void drop_graph(nans_world *w)
 
 int cfg_id(const nans_world *w)
 {
-    return (w->narrow_bpsm * 1024 + w->solve_threads0) * 1024 + w->solve_threads1;
+    return ((w->cull_tiles * 64 + w->narrow_bpsm) * 1024 + w->solve_threads0) * 1024 + w->solve_threads1;
 }
 
 int narrow_grid(nans_world *w)
@@ -397,6 +398,17 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     if ((size_t)max_bodies * sizeof(int) > kSolveSmemMax)
         return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: a scene has more bodies than the solver's wave table holds");
 
+    // cube-cube cull tiles: 32 x 32 blocks of the upper triangle of each scene's cube pairs
+    std::vector<int4> tiles;
+    for (int s = 0; s < S; ++s)
+    {
+        const int k = (sc_nc[s] + 31) / 32;
+        if (sc_nc[s] < 2)
+            continue;
+        for (int ti = 0; ti < k; ++ti)
+            for (int tj = ti; tj < k; ++tj)
+                tiles.push_back(make_int4(s, ti, tj, 0));
+    }
     w->pair_total = pair_acc;
     w->max_scene_bodies = max_bodies;
     w->cull_blocks = (int)((word_acc + kCullThreads - 1) / kCullThreads);
@@ -408,10 +420,12 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.n_all = nall;
     d.pair_total = pair_acc;
     d.n_words = (int)word_acc;
+    d.n_tiles = (int)tiles.size();
     auto &L = w->allocs;
     int rc;
     int *p_cube0, *p_nc, *p_ns, *p_iters, *p_order, *p_bscene;
     int *p_word0, *p_wscene;
+    int4 *p_tiles;
     float *p_cr, *p_cf, *p_local;
     int4 *p_shape;
     if ((rc = dalloc(w, L, &p_cube0, S)) || (rc = dalloc(w, L, &p_nc, S)) || (rc = dalloc(w, L, &p_ns, S)) ||
@@ -425,6 +439,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &w->d_prm, nall)) || (rc = dalloc(w, L, &w->d_model_in, (size_t)4 * nall)) ||
         (rc = dalloc(w, L, &d.box_lo, nall)) || (rc = dalloc(w, L, &d.box_hi, nall)) ||
         (rc = dalloc(w, L, &d.pair_mask, (size_t)word_acc)) || (rc = dalloc(w, L, &p_wscene, (size_t)word_acc)) ||
+        (rc = dalloc(w, L, &p_tiles, tiles.size())) ||
         (rc = dalloc(w, L, &d.epa_hist, (size_t)word_acc * 32)) ||
         (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.cull_total, 1)) ||
         (rc = dalloc(w, L, &d.cull_max, 1)) ||
@@ -453,6 +468,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.sc_order = p_order;
     d.sc_word0 = p_word0;
     d.word_scene = p_wscene;
+    d.tiles = p_tiles;
     d.sc_cr = p_cr;
     d.sc_cf = p_cf;
     d.body_scene = p_bscene;
@@ -489,6 +505,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     CK(cudaMemcpyAsync(p_iters, sc_iters.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_order, sc_order.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_word0, sc_word0.data(), (S + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!tiles.empty())
+        CK(cudaMemcpyAsync(p_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
     {
         std::vector<int> wscene((size_t)word_acc);
         for (int s = 0; s < S; ++s)
@@ -554,12 +572,33 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
 }
 
 // Enqueues the cull (three kernels) on the world's stream.
+// The culled pair mask and its per-block counts (the scan's input): by tiles (cube-cube pairs
+// 32 x 32 per warp, the other pairs per scene, then the counts), or one lane per pair
+// (k_cull_mask: the all-pairs mode, and the tuning's alternative). The same mask either way.
+void enqueue_cull_mask(nans_world *w)
+{
+    cudaStream_t st = w->stream;
+    const int all_pairs = (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0;
+    if (w->cull_blocks <= 0)
+        return;
+    if (all_pairs || !w->cull_tiles)
+    {
+        k_cull_mask<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw, all_pairs);
+        return;
+    }
+    const int per_block = kCullTileThreads / 32, cap = 8 * w->sm_count;
+    cudaMemsetAsync(w->dw.pair_mask, 0, (size_t)w->dw.n_words * sizeof(unsigned), st);
+    if (w->dw.n_tiles > 0)
+        k_cull_tiles<<<std::min(cap, (w->dw.n_tiles + per_block - 1) / per_block), kCullTileThreads, 0, st>>>(w->dw);
+    k_cull_rest<<<std::min(cap, (w->n_scenes + per_block - 1) / per_block), kCullTileThreads, 0, st>>>(w->dw);
+    k_cull_count<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
+}
+
+// Enqueues the cull on the world's stream: mask, scan, ordered write.
 void enqueue_cull(nans_world *w)
 {
     cudaStream_t st = w->stream;
-    int all_pairs = (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0;
-    if (w->cull_blocks > 0)
-        k_cull_mask<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw, all_pairs);
+    enqueue_cull_mask(w);
     k_cull_scan<<<1, 1024, 0, st>>>(w->dw, w->cull_blocks);
     if (w->cull_blocks > 0)
         k_cull_write<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
@@ -655,10 +694,7 @@ int step_eager(nans_world *w, float dt, bool check_capacity)
                 return rc;
             // the block counts were turned into offsets by the scan: count again
             CK(cudaMemsetAsync(d.status, 0, sizeof(unsigned), st));
-            const int all_pairs = (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0;
-            k_cull_mask<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw, all_pairs);
-            k_cull_scan<<<1, 1024, 0, st>>>(w->dw, w->cull_blocks);
-            k_cull_write<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
+            enqueue_cull(w);
             CK(cudaGetLastError());
         }
     }
@@ -1254,9 +1290,9 @@ int nans_batch_autotune(nans_world *w, float dt)
         w->steps_run = s_steps;
         return r;
     };
-    // coordinate descent over the launch parameters, one at a time from the defaults: the GJK
-    // pass's blocks per SM, and the solver's threads per scene in its first pass (1 or 2 warps)
-    // and for the late scenes (4 or 8 warps)
+    // coordinate descent over the launch parameters, one at a time from the defaults: the cull
+    // method (tiles or one lane per pair), the GJK pass's blocks per SM, and the solver's threads
+    // per scene in its first pass (1 or 2 warps) and for the late scenes (4 or 8 warps)
     struct Axis
     {
         int *field;
@@ -1265,6 +1301,7 @@ int nans_batch_autotune(nans_world *w, float dt)
     };
     const int solve0_auto = solve_threads(w->max_scene_bodies);
     Axis axes[] = {
+        {&w->cull_tiles, {1, 0, 0, 0}, (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 2},
         {&w->narrow_bpsm, {0, 4, 0, 0}, 2},
         {&w->solve_threads0, {solve0_auto, 64, 0, 0}, solve0_auto == 32 ? 2 : 1},
         {&w->solve_threads1, {kSolveLateThreads, 256, 0, 0}, 2},
@@ -1303,14 +1340,15 @@ int nans_world_set_tuning(nans_world *w, const int32_t *in)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: null world or input");
     const bool threads_ok =
         in[1] >= 32 && in[1] <= 256 && in[1] % 32 == 0 && in[2] >= 32 && in[2] <= 256 && in[2] % 32 == 0;
-    if (in[0] < 0 || in[0] > 32 || !threads_ok)
-        return fail(NANS_ERR_INVALID_ARGUMENT,
-                    "set_tuning: GJK blocks per SM in [0, 32], solver threads multiples of 32 in [32, 256]");
+    if (in[0] < 0 || in[0] > 32 || !threads_ok || (in[3] != 0 && in[3] != 1))
+        return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: GJK blocks per SM in [0, 32], solver threads multiples of "
+                                               "32 in [32, 256], cull method 0 or 1");
     if (in[1] < 256 && w->max_scene_bodies > 512)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: scenes above 512 bodies need 256 solver threads");
     w->narrow_bpsm = in[0];
     w->solve_threads0 = in[1];
     w->solve_threads1 = in[2];
+    w->cull_tiles = in[3];
     return NANS_OK;
 }
 
@@ -1321,8 +1359,9 @@ int nans_world_tuning(nans_world *w, int32_t *out)
     out[0] = w->narrow_bpsm;
     out[1] = w->solve_threads0 ? w->solve_threads0 : solve_threads(w->max_scene_bodies);
     out[2] = w->solve_threads1;
-    out[3] = w->tune_trials;
-    out[4] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
+    out[3] = w->cull_tiles;
+    out[4] = w->tune_trials;
+    out[5] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
     return NANS_OK;
 }
 

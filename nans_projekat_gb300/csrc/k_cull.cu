@@ -136,6 +136,120 @@ __global__ void __launch_bounds__(kCullThreads) k_cull_mask(DevWorld w, int all_
         w.block_hits[blockIdx.x] = total;
 }
 
+// ---------------------------------------------------------------------------------------
+// The culled pair mask by tiles (the default; k_cull_mask serves the all-pairs mode). The mask
+// is cleared, then:
+//   k_cull_tiles  cube-cube pairs of a scene in 32 x 32 tiles (rows i, columns j > i), one warp
+//                 per tile: each lane holds one column's box, the rows' boxes are broadcast by
+//                 shuffles, a row's 32 tests are one ballot, and the row's bits are ORed into the
+//                 mask at the row's pair indices (row i of the triangle is contiguous in j)
+//   k_cull_rest   the scene's other pairs (CF, SF, CS, SS), one warp per scene, one lane per pair
+//   k_cull_count  per block of kCullThreads mask words, the number of culled pairs (the scan and
+//                 the write pass use the same blocks as with k_cull_mask)
+// The box test and the pair numbering are k_cull_mask's, so the mask is the same bit for bit.
+// ---------------------------------------------------------------------------------------
+
+// ORs the row bits m (bit c = pair index base + c of the scene starting at bit wbit0) into the
+// mask, from the first set bit on (so that no word before the scene's first is touched).
+__device__ __forceinline__ void or_bits(unsigned *mask, long long wbit0, long long base, unsigned m)
+{
+    if (!m)
+        return;
+    const int c = __ffs(m) - 1;
+    const long long b = wbit0 + base + c;
+    m >>= c;
+    const long long word = b >> 5;
+    const int sh = (int)(b & 31);
+    atomicOr(mask + word, m << sh);
+    if (sh && (m >> (32 - sh)))
+        atomicOr(mask + word + 1, m >> (32 - sh));
+}
+
+__global__ void __launch_bounds__(kCullTileThreads) k_cull_tiles(DevWorld w)
+{
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < w.n_tiles; t += nwarps)
+    {
+        const int4 tile = __ldg(w.tiles + t); // scene, row block, column block
+        const int s = tile.x, r0 = 32 * tile.y, k0 = 32 * tile.z;
+        const int nc = __ldg(w.sc_nc + s), c0 = __ldg(w.sc_cube0 + s);
+        const long long wbit0 = (long long)__ldg(w.sc_word0 + s) * 32;
+        const int j = k0 + lane, ir = r0 + lane;
+        float4 cl = make_float4(0.f, 0.f, 0.f, 0.f), ch = cl, rl = cl, rh = cl;
+        if (j < nc)
+        {
+            cl = __ldg(w.box_lo + c0 + j);
+            ch = __ldg(w.box_hi + c0 + j);
+        }
+        if (ir < nc)
+        {
+            rl = __ldg(w.box_lo + c0 + ir);
+            rh = __ldg(w.box_hi + c0 + ir);
+        }
+        const int rows = min(32, nc - r0);
+        unsigned mine = 0u; // lane r: the bits of row r0 + r
+        for (int r = 0; r < rows; ++r)
+        {
+            const int i = r0 + r;
+            const float lx = __shfl_sync(0xffffffffu, rl.x, r), ly = __shfl_sync(0xffffffffu, rl.y, r),
+                        lz = __shfl_sync(0xffffffffu, rl.z, r);
+            const float hx = __shfl_sync(0xffffffffu, rh.x, r), hy = __shfl_sync(0xffffffffu, rh.y, r),
+                        hz = __shfl_sync(0xffffffffu, rh.z, r);
+            const bool hit = j < nc && j > i && lx <= ch.x && cl.x <= hx && ly <= ch.y && cl.y <= hy &&
+                             lz <= ch.z && cl.z <= hz;
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (lane == r)
+                mine = m;
+        }
+        if (lane < rows && mine)
+        {
+            const long long i = ir;
+            // pair index of (i, k0): row i starts at i*nc - i*(i+1)/2 with column i + 1
+            or_bits(w.pair_mask, wbit0, i * nc - i * (i + 1) / 2 + (k0 - i - 1), mine);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kCullTileThreads) k_cull_rest(DevWorld w)
+{
+    const int lane = threadIdx.x & 31;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < w.n_scenes; s += nwarps)
+    {
+        const int nc = __ldg(w.sc_nc + s), ns = __ldg(w.sc_ns + s), c0 = __ldg(w.sc_cube0 + s);
+        const long long wbit0 = (long long)__ldg(w.sc_word0 + s) * 32;
+        const long long ncc = (long long)nc * (nc - 1) / 2, np = scene_pair_count(nc, ns);
+        for (long long k0 = ncc; k0 < np; k0 += 32)
+        {
+            const long long k = k0 + lane;
+            bool hit = false;
+            if (k < np)
+            {
+                int type, i, j, a, b;
+                decode_pair(k, nc, ns, type, i, j);
+                pair_ids(w, s, c0, nc, type, i, j, a, b);
+                const float4 la = __ldg(w.box_lo + a), ha = __ldg(w.box_hi + a);
+                const float4 lb = __ldg(w.box_lo + b), hb = __ldg(w.box_hi + b);
+                hit = la.x <= hb.x && lb.x <= ha.x && la.y <= hb.y && lb.y <= ha.y && la.z <= hb.z && lb.z <= ha.z;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0)
+                or_bits(w.pair_mask, wbit0, k0, m);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kCullThreads) k_cull_count(DevWorld w)
+{
+    __shared__ int sh[32];
+    const int wo = blockIdx.x * kCullThreads + threadIdx.x;
+    const unsigned m = (wo < w.n_words) ? w.pair_mask[wo] : 0u;
+    const int total = block_sum(__popc(m), sh);
+    if (threadIdx.x == 0)
+        w.block_hits[blockIdx.x] = total;
+}
+
 // One block of 1024 threads: exclusive scan of the per-block counts in place; the total and
 // the capacity check.
 __global__ void __launch_bounds__(1024) k_cull_scan(DevWorld w, int nblocks)

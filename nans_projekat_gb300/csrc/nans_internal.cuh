@@ -71,6 +71,8 @@ struct DevWorld
     int *cand_a, *cand_b, *cand_meta; // meta = scene << 3 | type
     int *n_cand;                        // device counter
     unsigned *pair_mask;                // one bit per pair, words aligned per scene
+    const int4 *tiles;                  // cube-cube cull tiles: (scene, row block, column block)
+    int n_tiles;
     const int *word_scene;              // scene of each mask word
     int n_words;
     int *block_hits;                    // per cull block: culled pairs, then candidate offset

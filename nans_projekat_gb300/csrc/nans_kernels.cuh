@@ -17,6 +17,7 @@ enum SweepFlags
 };
 
 constexpr int kCullThreads = 256;
+constexpr int kCullTileThreads = 256;
 constexpr int kSolveLateThreads = 128; // solver blocks of the second pass (late scenes)
 
 // EPA capacities. Vertices: the GJK tetrahedron plus one support per EPA iteration (at most
@@ -76,6 +77,9 @@ __global__ void k_state_out(DevWorld w, float *stage, const int *body_rec, int n
 __global__ void k_cull_mask(DevWorld w, int all_pairs);
 __global__ void k_cull_scan(DevWorld w, int nblocks);
 __global__ void k_cull_write(DevWorld w);
+__global__ void k_cull_tiles(DevWorld w);
+__global__ void k_cull_rest(DevWorld w);
+__global__ void k_cull_count(DevWorld w);
 
 int narrow_blocks_per_sm(int warps);
 size_t epa_big_bytes();

@@ -295,13 +295,13 @@ class World:
 
     def tuning(self):
         """The launch parameters in use (nans_batch_autotune's choice, or the defaults)."""
-        out = np.zeros(5, np.int32)
+        out = np.zeros(6, np.int32)
         _check(self.lib.nans_world_tuning(self.h, _ptr(out)))
         return {"gjk_blocks_per_sm": int(out[0]), "solve_threads": int(out[1]), "solve_threads_late": int(out[2]),
-                "candidates_timed": int(out[3]), "us_per_step": int(out[4])}
+                "cull_tiles": int(out[3]), "candidates_timed": int(out[4]), "us_per_step": int(out[5])}
 
-    def set_tuning(self, gjk_blocks_per_sm, solve_threads, solve_threads_late):
-        a = np.array([gjk_blocks_per_sm, solve_threads, solve_threads_late], np.int32)
+    def set_tuning(self, gjk_blocks_per_sm, solve_threads, solve_threads_late, cull_tiles=1):
+        a = np.array([gjk_blocks_per_sm, solve_threads, solve_threads_late, cull_tiles], np.int32)
         _check(self.lib.nans_world_set_tuning(self.h, _ptr(a)))
 
     def path_counts(self):
