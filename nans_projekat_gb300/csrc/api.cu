@@ -92,7 +92,6 @@ struct nans_world
 
     int narrow_bpsm = 0;     // GJK blocks per SM (0 = occupancy limit)
     int cull_tiles = 1;      // cull by tiles (1) or one lane per pair (0)
-    int rest_chunks = 0;     // 32-pair chunks of the pairs that are not cube-cube
     int gjk_cap_blocks = 1;  // GJK blocks the world's pairs can keep busy
     int solve_threads0 = 0;  // solver threads per scene, first pass (0 = by the largest scene)
     int solve_threads1 = kSolveLateThreads; // solver threads per late scene
@@ -401,17 +400,17 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
 
     // cube-cube cull tiles: 32 x 32 blocks of the upper triangle of each scene's cube pairs
     std::vector<int4> tiles;
-    std::vector<int> rest_chunk0(S + 1, 0); // chunks of 32 of each scene's other pairs
-    long long rest_acc = 0;
+    // cull tasks for the other pairs: each scene's chunks of 32, at most kRestChunksPerTask a task
+    std::vector<int4> rest_tasks;
     for (int s = 0; s < S; ++s)
     {
-        rest_chunk0[s] = (int)std::min<long long>(rest_acc, INT32_MAX);
         const long long ncc = (long long)sc_nc[s] * (sc_nc[s] - 1) / 2;
-        rest_acc += (scene_pair_count(sc_nc[s], sc_ns[s]) - ncc + 31) / 32;
+        const long long chunks = (scene_pair_count(sc_nc[s], sc_ns[s]) - ncc + 31) / 32;
+        for (long long c = 0; c < chunks; c += kRestChunksPerTask)
+            rest_tasks.push_back(make_int4(s, (int)c, (int)std::min<long long>(kRestChunksPerTask, chunks - c), 0));
     }
-    rest_chunk0[S] = (int)std::min<long long>(rest_acc, INT32_MAX);
-    if (rest_acc > INT32_MAX)
-        return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: more than 2^31 chunks of non-cube-cube pairs");
+    if (rest_tasks.size() > (size_t)INT32_MAX)
+        return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: more than 2^31 cull tasks of non-cube-cube pairs");
     for (int s = 0; s < S; ++s)
     {
         const int k = (sc_nc[s] + 31) / 32;
@@ -422,7 +421,6 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
                 tiles.push_back(make_int4(s, ti, tj, 0));
     }
     w->pair_total = pair_acc;
-    w->rest_chunks = (int)rest_acc;
     w->max_scene_bodies = max_bodies;
     w->cull_blocks = (int)((word_acc + kCullThreads - 1) / kCullThreads);
 
@@ -439,7 +437,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     int *p_cube0, *p_nc, *p_ns, *p_iters, *p_order, *p_bscene;
     int *p_word0, *p_wscene;
     int4 *p_tiles;
-    int *p_rest0;
+    int4 *p_rest;
     float *p_cr, *p_cf, *p_local;
     int4 *p_shape;
     if ((rc = dalloc(w, L, &p_cube0, S)) || (rc = dalloc(w, L, &p_nc, S)) || (rc = dalloc(w, L, &p_ns, S)) ||
@@ -453,7 +451,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         (rc = dalloc(w, L, &w->d_prm, nall)) || (rc = dalloc(w, L, &w->d_model_in, (size_t)4 * nall)) ||
         (rc = dalloc(w, L, &d.box_lo, nall)) || (rc = dalloc(w, L, &d.box_hi, nall)) ||
         (rc = dalloc(w, L, &d.pair_mask, (size_t)word_acc)) || (rc = dalloc(w, L, &p_wscene, (size_t)word_acc)) ||
-        (rc = dalloc(w, L, &p_tiles, tiles.size())) || (rc = dalloc(w, L, &p_rest0, (size_t)S + 1)) ||
+        (rc = dalloc(w, L, &p_tiles, tiles.size())) || (rc = dalloc(w, L, &p_rest, rest_tasks.size())) ||
         (rc = dalloc(w, L, &d.epa_hist, (size_t)word_acc * 32)) ||
         (rc = dalloc(w, L, &d.block_hits, std::max(1, w->cull_blocks))) || (rc = dalloc(w, L, &d.cull_total, 1)) ||
         (rc = dalloc(w, L, &d.cull_max, 1)) ||
@@ -483,7 +481,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.sc_word0 = p_word0;
     d.word_scene = p_wscene;
     d.tiles = p_tiles;
-    d.rest_chunk0 = p_rest0;
+    d.rest_tasks = p_rest;
+    d.n_rest_tasks = (int)rest_tasks.size();
     d.sc_cr = p_cr;
     d.sc_cf = p_cf;
     d.body_scene = p_bscene;
@@ -522,7 +521,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     CK(cudaMemcpyAsync(p_word0, sc_word0.data(), (S + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
     if (!tiles.empty())
         CK(cudaMemcpyAsync(p_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
-    CK(cudaMemcpyAsync(p_rest0, rest_chunk0.data(), ((size_t)S + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
+    if (!rest_tasks.empty())
+        CK(cudaMemcpyAsync(p_rest, rest_tasks.data(), rest_tasks.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
     {
         std::vector<int> wscene((size_t)word_acc);
         for (int s = 0; s < S; ++s)
@@ -606,8 +606,9 @@ void enqueue_cull_mask(nans_world *w)
     cudaMemsetAsync(w->dw.pair_mask, 0, (size_t)w->dw.n_words * sizeof(unsigned), st);
     if (w->dw.n_tiles > 0)
         k_cull_tiles<<<std::min(cap, (w->dw.n_tiles + per_block - 1) / per_block), kCullTileThreads, 0, st>>>(w->dw);
-    k_cull_rest<<<std::max(1, std::min(cap, (w->rest_chunks + per_block - 1) / per_block)), kCullTileThreads, 0,
-                  st>>>(w->dw);
+    if (w->dw.n_rest_tasks > 0)
+        k_cull_rest<<<std::min(cap, (w->dw.n_rest_tasks + per_block - 1) / per_block), kCullTileThreads, 0, st>>>(
+            w->dw);
     k_cull_count<<<w->cull_blocks, kCullThreads, 0, st>>>(w->dw);
 }
 

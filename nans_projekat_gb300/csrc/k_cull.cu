@@ -143,7 +143,8 @@ __global__ void __launch_bounds__(kCullThreads) k_cull_mask(DevWorld w, int all_
 //                 per tile: each lane holds one column's box, the rows' boxes are broadcast by
 //                 shuffles, a row's 32 tests are one ballot, and the row's bits are ORed into the
 //                 mask at the row's pair indices (row i of the triangle is contiguous in j)
-//   k_cull_rest   the other pairs (CF, SF, CS, SS), one warp per 32 consecutive pairs of a scene
+//   k_cull_rest   the other pairs (CF, SF, CS, SS), one warp per task of up to 64 chunks of 32
+//                 consecutive pairs of a scene
 //   k_cull_count  per block of kCullThreads mask words, the number of culled pairs (the scan and
 //                 the write pass use the same blocks as with k_cull_mask)
 // The box test and the pair numbering are k_cull_mask's, so the mask is the same bit for bit.
@@ -211,45 +212,41 @@ __global__ void __launch_bounds__(kCullTileThreads) k_cull_tiles(DevWorld w)
     }
 }
 
-// The pairs that are not cube-cube, in chunks of 32 consecutive pair indices of one scene, one
-// warp per chunk: scene s owns chunks [rest_chunk0[s], rest_chunk0[s + 1]) (a scene of many
-// spheres has millions of cube-sphere pairs, spread over the whole grid).
+// The pairs that are not cube-cube, in chunks of 32 consecutive pair indices of one scene: one
+// warp per task of at most kRestChunksPerTask chunks (rest_tasks: scene, first chunk, chunks),
+// so that a scene of many spheres (millions of cube-sphere pairs) spreads over the grid while a
+// small scene is one task.
 __global__ void __launch_bounds__(kCullTileThreads) k_cull_rest(DevWorld w)
 {
     const int lane = threadIdx.x & 31;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    const int total = w.rest_chunk0[w.n_scenes];
-    for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < total; g += nwarps)
+    for (int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; g < w.n_rest_tasks; g += nwarps)
     {
-        // the scene whose chunk range holds g: the last s with rest_chunk0[s] <= g
-        int lo = 0, hi = w.n_scenes;
-        while (hi - lo > 1)
-        {
-            const int mid = (lo + hi) >> 1;
-            if (__ldg(w.rest_chunk0 + mid) <= g)
-                lo = mid;
-            else
-                hi = mid;
-        }
-        const int s = lo;
+        const int4 task = __ldg(w.rest_tasks + g);
+        const int s = task.x;
         const int nc = __ldg(w.sc_nc + s), ns = __ldg(w.sc_ns + s), c0 = __ldg(w.sc_cube0 + s);
         const long long wbit0 = (long long)__ldg(w.sc_word0 + s) * 32;
         const long long np = scene_pair_count(nc, ns);
-        const long long k0 = (long long)nc * (nc - 1) / 2 + 32LL * (g - __ldg(w.rest_chunk0 + s));
-        const long long k = k0 + lane;
-        bool hit = false;
-        if (k < np)
+        const long long ncc = (long long)nc * (nc - 1) / 2;
+        for (int q = 0; q < task.z; ++q)
         {
-            int type, i, j, a, b;
-            decode_pair(k, nc, ns, type, i, j);
-            pair_ids(w, s, c0, nc, type, i, j, a, b);
-            const float4 la = __ldg(w.box_lo + a), ha = __ldg(w.box_hi + a);
-            const float4 lb = __ldg(w.box_lo + b), hb = __ldg(w.box_hi + b);
-            hit = la.x <= hb.x && lb.x <= ha.x && la.y <= hb.y && lb.y <= ha.y && la.z <= hb.z && lb.z <= ha.z;
+            const long long k0 = ncc + 32LL * (task.y + q);
+            const long long k = k0 + lane;
+            bool hit = false;
+            if (k < np)
+            {
+                int type, i, j, a, b;
+                decode_pair(k, nc, ns, type, i, j);
+                pair_ids(w, s, c0, nc, type, i, j, a, b);
+                const float4 la = __ldg(w.box_lo + a), ha = __ldg(w.box_hi + a);
+                const float4 lb = __ldg(w.box_lo + b), hb = __ldg(w.box_hi + b);
+                hit = la.x <= hb.x && lb.x <= ha.x && la.y <= hb.y && lb.y <= ha.y && la.z <= hb.z &&
+                      lb.z <= ha.z;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0)
+                or_bits(w.pair_mask, wbit0, k0, m);
         }
-        const unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (lane == 0)
-            or_bits(w.pair_mask, wbit0, k0, m);
     }
 }
 

@@ -73,7 +73,8 @@ struct DevWorld
     unsigned *pair_mask;                // one bit per pair, words aligned per scene
     const int4 *tiles;                  // cube-cube cull tiles: (scene, row block, column block)
     int n_tiles;
-    const int *rest_chunk0;             // per scene (+1): first 32-pair chunk of its other pairs
+    const int4 *rest_tasks;             // cull of the other pairs: (scene, first chunk, chunks)
+    int n_rest_tasks;
     const int *word_scene;              // scene of each mask word
     int n_words;
     int *block_hits;                    // per cull block: culled pairs, then candidate offset

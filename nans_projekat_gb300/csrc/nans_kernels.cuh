@@ -18,6 +18,7 @@ enum SweepFlags
 
 constexpr int kCullThreads = 256;
 constexpr int kCullTileThreads = 256;
+constexpr int kRestChunksPerTask = 64; // 32-pair chunks of non-cube-cube pairs per cull task
 constexpr int kSolveLateThreads = 128; // solver blocks of the second pass (late scenes)
 
 // EPA capacities. Vertices: the GJK tetrahedron plus one support per EPA iteration (at most
