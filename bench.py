@@ -356,15 +356,18 @@ def schedule_ab(lib, batch, device, warm=25, n=10):
     """A/B of schedules on identical windows of the workload (each world steps the same scenes to
     the same state, then the per-stage device time of n eager steps is taken with
     nans_profile_steps): the library's defaults (GJK one thread per candidate pair, cube-cube cull
-    by 32 x 32 tiles) against GJK with one warp per pair (the supports evaluated across the
-    lanes) and against the cull with one lane per pair. Results are the same in all three."""
+    by 32 x 32 tiles, six late-scene solver blocks per SM) against GJK with one warp per pair (the
+    supports evaluated across the lanes), the cull with one lane per pair, and two late-scene
+    solver blocks per SM. Results are the same in all of them."""
     names = ["sweep", "cull", "gjk_and_thread_epa", "warp_epa", "large_epa", "solve"]
     out = {}
-    for key, warp, tiles in (("default", False, 1), ("gjk_warp_per_pair", True, 1), ("cull_lane_per_pair", False, 0)):
+    for key, warp, tiles, late in (("default", False, 1, None), ("gjk_warp_per_pair", True, 1, None),
+                                   ("cull_lane_per_pair", False, 0, None), ("late_solve_2_blocks_per_sm", False, 1, 2)):
         w = lib.World(device=device, gjk_warp=warp)
         w.upload_batch(batch)
         t = w.tuning()
-        w.set_tuning(t["gjk_blocks_per_sm"], t["solve_threads"], t["solve_threads_late"], tiles)
+        w.set_tuning(t["gjk_blocks_per_sm"], t["solve_threads"], t["solve_threads_late"], tiles,
+                     late or t["solve_late_blocks_per_sm"])
         w.batch_step(DT, warm, 1)
         ms = w.profile(DT, n) / n
         out[key] = {nm: float(x) for nm, x in zip(names, ms)}

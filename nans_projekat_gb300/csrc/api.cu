@@ -95,6 +95,7 @@ struct nans_world
     int gjk_cap_blocks = 1;  // GJK blocks the world's pairs can keep busy
     int solve_threads0 = 0;  // solver threads per scene, first pass (0 = by the largest scene)
     int solve_threads1 = kSolveLateThreads; // solver threads per late scene
+    int solve_late_bpsm = kSolveLateBlocksPerSm; // late-scene solver blocks per SM
     int tune_trials = 0;
     float tune_ms = 0.0f;
     unsigned char *d_snap_hist = nullptr;
@@ -175,7 +176,8 @@ void drop_graph(nans_world *w)
 
 int cfg_id(const nans_world *w)
 {
-    return ((w->cull_tiles * 64 + w->narrow_bpsm) * 1024 + w->solve_threads0) * 1024 + w->solve_threads1;
+    return (((w->solve_late_bpsm * 2 + w->cull_tiles) * 64 + w->narrow_bpsm) * 512 + w->solve_threads0) * 512 +
+           w->solve_threads1;
 }
 
 int narrow_grid(nans_world *w)
@@ -654,7 +656,8 @@ cudaError_t enqueue_narrow_solve(nans_world *w, float dt, cudaEvent_t *tl)
         e2 = cudaStreamWaitEvent(st, w->ev_join, 0);
     // the late scenes (few, and mostly the larger ones) solve with wider blocks: their waves
     // are on the step's critical path
-    launch_solve(w->dw, std::min(w->n_scenes, 2 * w->sm_count), w->solve_threads1, solve_smem(w), st, dt, 1);
+    launch_solve(w->dw, std::min(w->n_scenes, w->solve_late_bpsm * w->sm_count), w->solve_threads1, solve_smem(w), st,
+                 dt, 1);
     if (tl)
         cudaEventRecord(tl[4], st);
     return e != cudaSuccess ? e : e2;
@@ -1309,8 +1312,9 @@ int nans_batch_autotune(nans_world *w, float dt)
         return r;
     };
     // coordinate descent over the launch parameters, one at a time from the defaults: the cull
-    // method (tiles or one lane per pair), the GJK pass's blocks per SM, and the solver's threads
-    // per scene in its first pass (1 or 2 warps) and for the late scenes (4 or 8 warps)
+    // method (tiles or one lane per pair), the GJK pass's blocks per SM, the solver's threads per
+    // scene in its first pass (1 or 2 warps), its blocks per SM for the late scenes (6 or 2) and
+    // their threads per scene (4 or 2 warps)
     struct Axis
     {
         int *field;
@@ -1322,7 +1326,8 @@ int nans_batch_autotune(nans_world *w, float dt)
         {&w->cull_tiles, {1, 0, 0, 0}, (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 2},
         {&w->narrow_bpsm, {0, 4, 0, 0}, 2},
         {&w->solve_threads0, {solve0_auto, 64, 0, 0}, solve0_auto == 32 ? 2 : 1},
-        {&w->solve_threads1, {kSolveLateThreads, 256, 0, 0}, 2},
+        {&w->solve_late_bpsm, {kSolveLateBlocksPerSm, 2, 0, 0}, 2},
+        {&w->solve_threads1, {kSolveLateThreads, 64, 0, 0}, 2},
     };
     w->tune_trials = 0;
     for (Axis &ax : axes)
@@ -1358,15 +1363,17 @@ int nans_world_set_tuning(nans_world *w, const int32_t *in)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: null world or input");
     const bool threads_ok =
         in[1] >= 32 && in[1] <= 256 && in[1] % 32 == 0 && in[2] >= 32 && in[2] <= 256 && in[2] % 32 == 0;
-    if (in[0] < 0 || in[0] > 32 || !threads_ok || (in[3] != 0 && in[3] != 1))
+    if (in[0] < 0 || in[0] > 32 || !threads_ok || (in[3] != 0 && in[3] != 1) || in[4] < 1 || in[4] > 32)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: GJK blocks per SM in [0, 32], solver threads multiples of "
-                                               "32 in [32, 256], cull method 0 or 1");
+                                               "32 in [32, 256], cull method 0 or 1, late solver blocks per SM in "
+                                               "[1, 32]");
     if (in[1] < 256 && w->max_scene_bodies > 512)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: scenes above 512 bodies need 256 solver threads");
     w->narrow_bpsm = in[0];
     w->solve_threads0 = in[1];
     w->solve_threads1 = in[2];
     w->cull_tiles = in[3];
+    w->solve_late_bpsm = in[4];
     return NANS_OK;
 }
 
@@ -1378,8 +1385,9 @@ int nans_world_tuning(nans_world *w, int32_t *out)
     out[1] = w->solve_threads0 ? w->solve_threads0 : solve_threads(w->max_scene_bodies);
     out[2] = w->solve_threads1;
     out[3] = w->cull_tiles;
-    out[4] = w->tune_trials;
-    out[5] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
+    out[4] = w->solve_late_bpsm;
+    out[5] = w->tune_trials;
+    out[6] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
     return NANS_OK;
 }
 
@@ -1836,7 +1844,8 @@ int nans_profile_steps(nans_world *w, float dt, uint32_t nsteps, float *stage_ms
         CK(cudaEventRecord(ev[5], st));
         launch_solve(w->dw, w->n_scenes, w->solve_threads0 ? w->solve_threads0 : solve_threads(w->max_scene_bodies),
                  solve_smem(w), st, dt, 0);
-        launch_solve(w->dw, std::min(w->n_scenes, 2 * w->sm_count), w->solve_threads1, solve_smem(w), st, dt, 1);
+        launch_solve(w->dw, std::min(w->n_scenes, w->solve_late_bpsm * w->sm_count), w->solve_threads1, solve_smem(w), st,
+                 dt, 1);
         CK(cudaEventRecord(ev[6], st));
         CK(cudaGetLastError());
         after_step(w, dt);
