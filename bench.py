@@ -357,17 +357,19 @@ def schedule_ab(lib, batch, device, warm=25, n=10):
     the same state, then the per-stage device time of n eager steps is taken with
     nans_profile_steps): the library's defaults (GJK one thread per candidate pair, cube-cube cull
     by 32 x 32 tiles, six late-scene solver blocks per SM) against GJK with one warp per pair (the
-    supports evaluated across the lanes), the cull with one lane per pair, and two late-scene
-    solver blocks per SM. Results are the same in all of them."""
+    supports evaluated across the lanes), the cull with one lane per pair, two late-scene solver
+    blocks per SM, and three warp-tier EPA blocks per SM. Results are the same in all of them."""
     names = ["sweep", "cull", "gjk_and_thread_epa", "warp_epa", "large_epa", "solve"]
     out = {}
-    for key, warp, tiles, late in (("default", False, 1, None), ("gjk_warp_per_pair", True, 1, None),
-                                   ("cull_lane_per_pair", False, 0, None), ("late_solve_2_blocks_per_sm", False, 1, 2)):
+    for key, warp, tiles, late, med in (("default", False, 1, None, None), ("gjk_warp_per_pair", True, 1, None, None),
+                                        ("cull_lane_per_pair", False, 0, None, None),
+                                        ("late_solve_2_blocks_per_sm", False, 1, 2, None),
+                                        ("warp_epa_3_blocks_per_sm", False, 1, None, 3)):
         w = lib.World(device=device, gjk_warp=warp)
         w.upload_batch(batch)
         t = w.tuning()
         w.set_tuning(t["gjk_blocks_per_sm"], t["solve_threads"], t["solve_threads_late"], tiles,
-                     late or t["solve_late_blocks_per_sm"])
+                     late or t["solve_late_blocks_per_sm"], med or t["warp_epa_blocks_per_sm"])
         w.batch_step(DT, warm, 1)
         ms = w.profile(DT, n) / n
         out[key] = {nm: float(x) for nm, x in zip(names, ms)}
@@ -635,6 +637,7 @@ def run_ours(args):
     bodies = w.n_bodies
     if not args.no_autotune:
         w.autotune(DT)
+    tuning = w.tuning()
     # one CUDA graph covers gsteps steps; with fewer timed steps than that the graph is cut to the
     # timed step count, so that the timed region always replays graphs
     gsteps = max(1, min(args.graph_steps, args.steps))
@@ -751,6 +754,7 @@ def run_ours(args):
                 "bodies_per_gpu": bodies, "body_counts": "log-uniform [4, 256]", "dt": float(DT),
                 "iterations": 10, "restitution": 0.2, "friction": 0.5, "graph_steps": gsteps,
                 "path": path, "timed_graph_steps": timed_graph, "timed_eager_steps": timed_eager,
+                "tuning": tuning,
                 "warmup_steps_run": warm_steps,
                 "l2": "working set larger than L2 (%.0f MB of state, vertices and candidates)"
                       % ((bodies * 64 + n_boxes * 96 + n_cand * 60) / 1e6),

@@ -271,11 +271,12 @@ int nans_launches_per_step(nans_world *world, uint32_t *batched, uint32_t *plain
 /* The launch parameters nans_batch_autotune chose (or the defaults): out[0] GJK blocks per SM
  * (0 = as many as fit), out[1] solver threads per scene in the first solve pass, out[2] solver
  * threads per late scene, out[3] the cull method (1: cube-cube pairs by 32 x 32 tiles, 0: one
- * lane per pair), out[4] late-scene solver blocks per SM, out[5] candidates the autotuner
- * timed, out[6] the chosen candidate's microseconds per step. No reference counterpart. */
+ * lane per pair), out[4] late-scene solver blocks per SM, out[5] warp-tier EPA blocks per SM,
+ * out[6] candidates the autotuner timed, out[7] the chosen candidate's microseconds per step.
+ * No reference counterpart. */
 int nans_world_tuning(nans_world *world, int32_t *out);
 
-/* Sets the launch parameters out[0..4] of nans_world_tuning (for instance a choice of the
+/* Sets the launch parameters out[0..5] of nans_world_tuning (for instance a choice of the
  * autotuner kept from an earlier run); results do not depend on them. No reference
  * counterpart. */
 int nans_world_set_tuning(nans_world *world, const int32_t *in);

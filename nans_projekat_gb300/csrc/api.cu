@@ -96,6 +96,8 @@ struct nans_world
     int solve_threads0 = 0;  // solver threads per scene, first pass (0 = by the largest scene)
     int solve_threads1 = kSolveLateThreads; // solver threads per late scene
     int solve_late_bpsm = kSolveLateBlocksPerSm; // late-scene solver blocks per SM
+    int medium_bpsm = kMediumBlocksPerSm;        // warp-tier EPA blocks per SM
+    int medium_cap_blocks = 1;                   // warp-tier blocks the world's pairs can keep busy
     int tune_trials = 0;
     float tune_ms = 0.0f;
     unsigned char *d_snap_hist = nullptr;
@@ -176,8 +178,8 @@ void drop_graph(nans_world *w)
 
 int cfg_id(const nans_world *w)
 {
-    return (((w->solve_late_bpsm * 2 + w->cull_tiles) * 64 + w->narrow_bpsm) * 512 + w->solve_threads0) * 512 +
-           w->solve_threads1;
+    return ((((w->medium_bpsm * 33 + w->solve_late_bpsm) * 2 + w->cull_tiles) * 33 + w->narrow_bpsm) * 9 +
+            w->solve_threads0 / 32) * 9 + w->solve_threads1 / 32;
 }
 
 int narrow_grid(nans_world *w)
@@ -503,7 +505,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         return (int)std::max(1LL, std::min<long long>(resident, (maxc + per_block - 1) / per_block));
     };
     w->gjk_cap_blocks = upto(128, INT32_MAX);
-    d.medium_blocks = upto(4, 2 * w->sm_count);
+    w->medium_cap_blocks = upto(4, INT32_MAX);
+    d.medium_blocks = std::min(w->medium_bpsm * w->sm_count, w->medium_cap_blocks);
     d.tiny_blocks = upto(64, epa_tiny_grid(w->sm_count));
     d.gjk_warp = (w->flags & NANS_WORLD_GJK_WARP) ? 1 : 0;
     d.sm_count = w->sm_count;
@@ -1313,8 +1316,8 @@ int nans_batch_autotune(nans_world *w, float dt)
     };
     // coordinate descent over the launch parameters, one at a time from the defaults: the cull
     // method (tiles or one lane per pair), the GJK pass's blocks per SM, the solver's threads per
-    // scene in its first pass (1 or 2 warps), its blocks per SM for the late scenes (6 or 2) and
-    // their threads per scene (4 or 2 warps)
+    // scene in its first pass (1 or 2 warps), its blocks per SM for the late scenes (6 or 2),
+    // the warp-tier EPA's blocks per SM (2 or 3) and the late scenes' threads (4 or 2 warps)
     struct Axis
     {
         int *field;
@@ -1327,6 +1330,7 @@ int nans_batch_autotune(nans_world *w, float dt)
         {&w->narrow_bpsm, {0, 4, 0, 0}, 2},
         {&w->solve_threads0, {solve0_auto, 64, 0, 0}, solve0_auto == 32 ? 2 : 1},
         {&w->solve_late_bpsm, {kSolveLateBlocksPerSm, 2, 0, 0}, 2},
+        {&w->medium_bpsm, {kMediumBlocksPerSm, 3, 0, 0}, 2},
         {&w->solve_threads1, {kSolveLateThreads, 64, 0, 0}, 2},
     };
     w->tune_trials = 0;
@@ -1337,6 +1341,7 @@ int nans_batch_autotune(nans_world *w, float dt)
         for (int c = 0; c < ax.ncand && rc == NANS_OK; ++c)
         {
             *ax.field = ax.cands[c];
+            w->dw.medium_blocks = std::min(w->medium_bpsm * w->sm_count, w->medium_cap_blocks);
             float ms = 0.0f;
             rc = trial(ms);
             ++w->tune_trials;
@@ -1347,6 +1352,7 @@ int nans_batch_autotune(nans_world *w, float dt)
             }
         }
         *ax.field = bestv;
+        w->dw.medium_blocks = std::min(w->medium_bpsm * w->sm_count, w->medium_cap_blocks);
         w->tune_ms = best / kTuneSteps;
     }
     cudaEventDestroy(e0);
@@ -1363,10 +1369,11 @@ int nans_world_set_tuning(nans_world *w, const int32_t *in)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: null world or input");
     const bool threads_ok =
         in[1] >= 32 && in[1] <= 256 && in[1] % 32 == 0 && in[2] >= 32 && in[2] <= 256 && in[2] % 32 == 0;
-    if (in[0] < 0 || in[0] > 32 || !threads_ok || (in[3] != 0 && in[3] != 1) || in[4] < 1 || in[4] > 32)
+    if (in[0] < 0 || in[0] > 32 || !threads_ok || (in[3] != 0 && in[3] != 1) || in[4] < 1 || in[4] > 32 ||
+        in[5] < 1 || in[5] > 3)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: GJK blocks per SM in [0, 32], solver threads multiples of "
                                                "32 in [32, 256], cull method 0 or 1, late solver blocks per SM in "
-                                               "[1, 32]");
+                                               "[1, 32], warp-tier blocks per SM in [1, 3]");
     if (in[1] < 256 && w->max_scene_bodies > 512)
         return fail(NANS_ERR_INVALID_ARGUMENT, "set_tuning: scenes above 512 bodies need 256 solver threads");
     w->narrow_bpsm = in[0];
@@ -1374,6 +1381,8 @@ int nans_world_set_tuning(nans_world *w, const int32_t *in)
     w->solve_threads1 = in[2];
     w->cull_tiles = in[3];
     w->solve_late_bpsm = in[4];
+    w->medium_bpsm = in[5];
+    w->dw.medium_blocks = std::min(w->medium_bpsm * w->sm_count, w->medium_cap_blocks);
     return NANS_OK;
 }
 
@@ -1386,8 +1395,9 @@ int nans_world_tuning(nans_world *w, int32_t *out)
     out[2] = w->solve_threads1;
     out[3] = w->cull_tiles;
     out[4] = w->solve_late_bpsm;
-    out[5] = w->tune_trials;
-    out[6] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
+    out[5] = w->medium_bpsm;
+    out[6] = w->tune_trials;
+    out[7] = (int32_t)(1000.0f * w->tune_ms); // microseconds per step of the chosen candidate
     return NANS_OK;
 }
 

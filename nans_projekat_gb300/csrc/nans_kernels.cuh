@@ -21,6 +21,7 @@ constexpr int kCullTileThreads = 256;
 constexpr int kRestChunksPerTask = 64; // 32-pair chunks of non-cube-cube pairs per cull task
 constexpr int kSolveLateThreads = 128; // solver blocks of the second pass (late scenes)
 constexpr int kSolveLateBlocksPerSm = 6; // second-pass solver blocks per SM (registers allow six)
+constexpr int kMediumBlocksPerSm = 2;    // warp-tier EPA blocks per SM (shared memory allows three)
 
 // EPA capacities. Vertices: the GJK tetrahedron plus one support per EPA iteration (at most
 // 65, code/nans.cpp:804). Faces grow by two per iteration on a convex polytope, but the

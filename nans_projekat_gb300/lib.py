@@ -295,15 +295,16 @@ class World:
 
     def tuning(self):
         """The launch parameters in use (nans_batch_autotune's choice, or the defaults)."""
-        out = np.zeros(7, np.int32)
+        out = np.zeros(8, np.int32)
         _check(self.lib.nans_world_tuning(self.h, _ptr(out)))
         return {"gjk_blocks_per_sm": int(out[0]), "solve_threads": int(out[1]), "solve_threads_late": int(out[2]),
-                "cull_tiles": int(out[3]), "solve_late_blocks_per_sm": int(out[4]), "candidates_timed": int(out[5]),
-                "us_per_step": int(out[6])}
+                "cull_tiles": int(out[3]), "solve_late_blocks_per_sm": int(out[4]), "warp_epa_blocks_per_sm": int(out[5]),
+                "candidates_timed": int(out[6]), "us_per_step": int(out[7])}
 
-    def set_tuning(self, gjk_blocks_per_sm, solve_threads, solve_threads_late, cull_tiles=1, solve_late_blocks_per_sm=6):
-        a = np.array([gjk_blocks_per_sm, solve_threads, solve_threads_late, cull_tiles, solve_late_blocks_per_sm],
-                     np.int32)
+    def set_tuning(self, gjk_blocks_per_sm, solve_threads, solve_threads_late, cull_tiles=1, solve_late_blocks_per_sm=6,
+                   warp_epa_blocks_per_sm=2):
+        a = np.array([gjk_blocks_per_sm, solve_threads, solve_threads_late, cull_tiles, solve_late_blocks_per_sm,
+                      warp_epa_blocks_per_sm], np.int32)
         _check(self.lib.nans_world_set_tuning(self.h, _ptr(a)))
 
     def path_counts(self):

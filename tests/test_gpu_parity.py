@@ -417,11 +417,13 @@ def test_full_size_batch_samples_match_oracle(nl, oracle_lib):
         assert same_fields(o.pairs(j), w.pairs(i), PAIR_FIELDS)[0], i
 
 
-@pytest.mark.parametrize("tuning", [(0, 32, 128, 1, 6), (4, 64, 256, 0, 2), (2, 32, 64, 1, 12), (0, 32, 128, 0, 1)])
+@pytest.mark.parametrize("tuning", [(0, 32, 128, 1, 6, 2), (4, 64, 256, 0, 2, 3), (2, 32, 64, 1, 12, 1),
+                                    (0, 32, 128, 0, 1, 3)])
 def test_results_do_not_depend_on_launch_parameters(nl, oracle_lib, tuning):
     """The GJK blocks per SM, the solver's threads per scene (both passes), its late-pass blocks
-    per SM and the cull method (tiles or one lane per pair) change the schedule, never the
-    result: 256 workload scenes for 40 steps against the oracle, bit for bit."""
+    per SM, the warp-tier EPA's blocks per SM and the cull method (tiles or one lane per pair)
+    change the schedule, never the result: 256 workload scenes for 40 steps against the oracle,
+    bit for bit."""
     batch = scenes.stack_batch(16384, seed=2)[:256]
     dt = np.float32(1 / 60)
     w = nl.World()
@@ -431,7 +433,7 @@ def test_results_do_not_depend_on_launch_parameters(nl, oracle_lib, tuning):
     assert w.status() == 0
     t = w.tuning()
     assert (t["gjk_blocks_per_sm"], t["solve_threads"], t["solve_threads_late"], t["cull_tiles"],
-            t["solve_late_blocks_per_sm"]) == tuning
+            t["solve_late_blocks_per_sm"], t["warp_epa_blocks_per_sm"]) == tuning
     state = w.download()
     o = _oracle_states(batch, 40, dt)
     for i in range(len(batch)):
@@ -450,7 +452,7 @@ def test_autotuner_times_every_candidate(nl):
     w.step(np.float32(1 / 60), 2)
     w.autotune(np.float32(1 / 60))
     t = w.tuning()
-    assert t["candidates_timed"] == 10 and t["us_per_step"] > 0
+    assert t["candidates_timed"] == 12 and t["us_per_step"] > 0
     assert t["gjk_blocks_per_sm"] in (0, 4) and t["solve_threads"] in (32, 64)
     w.close()
 
