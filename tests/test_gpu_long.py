@@ -110,3 +110,32 @@ def test_plain_path_graph_replay_matches_reference(nl):
     graph_steps, eager_steps = w.path_counts()
     assert (graph_steps, eager_steps) == (599, 1)
     w.close()
+
+
+@pytest.mark.parametrize("config", ["grid_stack_1024x120", "mixed_4096x240"])
+def test_differentiated_configurations_at_full_size_match_oracle(nl, oracle_lib, config):
+    """The differentiated configurations' forward step at their full size and horizon on the
+    batched path: 1,024 4x4x2 stacks for 120 steps, and 4,096 mixed scenes of boxes, spheres and
+    convex hulls for 240 steps (hulls have no reference counterpart, so the oracle is the
+    checker); 64 scenes sampled with SplitMix64(77), bit for bit at the last step."""
+    from oracle.portbind import OracleWorld
+    if config == "grid_stack_1024x120":
+        batch, nsteps = scenes.grid_stack_batch(1024, seed=3), 120
+    else:
+        batch, nsteps = scenes.mixed_batch(4096, seed=4), 240
+    rng = scenes.SplitMix64(77)
+    pick = sorted({int(x) for x in rng.uniform(64, 0, len(batch))})
+    dt = np.float32(batch[0].constants.dt)
+    w = nl.World()
+    w.upload_batch(batch)
+    w.batch_step(dt, nsteps, 60)
+    assert w.status() == 0
+    state = w.download()
+    o = OracleWorld([batch[i] for i in pick])
+    o.step(dt, nsteps, 16)
+    for j, i in enumerate(pick):
+        cubes, spheres, _ = w.scene_state(i, state)
+        oc, os_, _ = o.state(j)
+        assert step_digest(cubes, spheres, w.pairs(i)) == step_digest(oc, os_, o.pairs(j)), \
+            "%s: scene %d differs from the oracle at step %d" % (config, i, nsteps)
+    w.close()
