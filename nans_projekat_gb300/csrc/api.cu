@@ -210,7 +210,7 @@ int alloc_candidates(nans_world *w, int cap)
         (rc = dalloc(w, L, &d.cand_meta, cap)) || (rc = dalloc(w, L, &d.hit, cap)) ||
         (rc = dalloc(w, L, &d.c_pa, cap)) || (rc = dalloc(w, L, &d.c_pb, cap)) || (rc = dalloc(w, L, &d.c_n, cap)) ||
         (rc = dalloc(w, L, &d.s_order, cap)) || (rc = dalloc(w, L, &d.s_wave, cap)) ||
-        (rc = dalloc(w, L, &d.s_perm, cap)) || (rc = dalloc(w, L, &d.s_wcnt, (size_t)cap + 1)) ||
+        (rc = dalloc(w, L, &d.s_ids, cap)) || (rc = dalloc(w, L, &d.s_wcnt, (size_t)cap + 1)) ||
         (rc = dalloc(w, L, &d.s_k, (size_t)9 * cap)) || (rc = dalloc(w, L, &d.long_cand, cap)))
         return rc;
     if (w->tape_on)

@@ -41,13 +41,14 @@ __global__ void k_tape_copy(DevWorld w, TapeStep t)
         const int nh = mw > 0 ? w.s_wcnt[cb + mw - 1] : 0;
         if (j - cb >= nh)
             continue;
-        const int c = w.s_perm[j];
-        t.a[j] = w.cand_a[c];
-        t.b[j] = w.cand_b[c];
+        const int4 id = w.s_ids[j];
+        const int c = id.x;
+        t.a[j] = id.y;
+        t.b[j] = id.z >= 0 ? id.z : -1 - id.z;
         t.type[j] = w.cand_meta[c] & 7;
 #pragma unroll
         for (int q = 0; q < 9; ++q)
-            t.k[(size_t)9 * j + q] = w.s_k[(size_t)9 * c + q];
+            t.k[(size_t)9 * j + q] = w.s_k[(size_t)9 * j + q];
         t.fwd[2 * (size_t)j] = w.s_fwd[2 * (size_t)c];
         t.fwd[2 * (size_t)j + 1] = w.s_fwd[2 * (size_t)c + 1];
     }

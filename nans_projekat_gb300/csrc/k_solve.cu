@@ -104,13 +104,21 @@ __device__ __forceinline__ float friction_bound(double c2, float sum) { return (
 // attached (w.s_fwd) it also records, per contact, what the adjoint needs: the relative
 // normal / tangent velocities, the applied impulses and the active set of the closed form
 // (normal impulse max(Ln, 0), tangent impulses clamp(Lt, -mu*Ln, mu*Ln)).
+//
+// id = the slot's (candidate, body A, body B or -1 - B for the floor, pair-space index) and kp
+// its constants: every load of a contact depends only on the slot, so the constants and the
+// four velocity vectors are fetched in one round trip.
 template <bool WARM>
-__device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const float4 *k, float cr, float cf,
+__device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const float4 *kp, float cr, float cf,
                                               double c2, int iters)
 {
-    int a = w.cand_a[c], b = w.cand_b[c];
-    int type = w.cand_meta[c] & 7;
-    bool writes_b = !type_b_is_floor(type);
+    const int c = id.x, a = id.y;
+    const bool writes_b = id.z >= 0;
+    const int b = writes_b ? id.z : -1 - id.z;
+    float4 k[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q)
+        k[q] = __ldcg(kp + q);
     v3 n = xyz(k[0]), t1 = xyz(k[1]), t2 = xyz(k[2]);
     float jn = k[0].w, jt1 = k[1].w, jt2 = k[2].w, bias0 = k[3].w;
     float invm1 = k[4].w, invm2 = k[5].w, invi1 = k[6].w, invi2 = k[7].w;
@@ -127,7 +135,7 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
         // warm starting (the reference's TODO at its pair dedupe, code/nans.cpp:1386-1389): a
         // pair in contact at the previous step starts from that step's accumulators
         step = *w.warm_step;
-        pidx = w.cand_pidx[c];
+        pidx = id.w;
         const float4 e = w.warm[pidx];
         if (__float_as_int(e.w) == step - 1)
         {
@@ -212,7 +220,7 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int c, const fl
 // pass 0 solves every scene whose contacts are all known after the per-thread EPA tier
 // (largest first, a block per scene); pass 1 the scenes with a candidate in the later EPA
 // tiers (a persistent grid over the late list), so that pass 0 can run while those tiers do.
-template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve(DevWorld w, float dt, int pass)
+template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax, 3) k_solve(DevWorld w, float dt, int pass)
 {
     extern __shared__ int s_last[];
     __shared__ int sh[32];
@@ -342,40 +350,47 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
                 __syncthreads();
             }
         }
+        // (4) placement in wave order with the velocity-independent constants: slot cb + pos
+        // gets the contact's ids and constants. The slots are the scene's own candidate slots
+        // (nh <= ce - cb), whose narrowphase use (the simplex of a hit) ended with the per-thread
+        // EPA; the order of the contacts inside a wave is immaterial (they commute exactly).
         for (int i = tid; i < nh; i += blockDim.x)
         {
-            int pos = atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i] - 1, 1);
-            w.s_perm[cb + pos] = w.s_order[cb + i];
-        }
-        // (4) velocity-independent constants
-        for (int i = tid; i < nh; i += blockDim.x)
-        {
-            int c = w.s_order[cb + i];
+            const int c = w.s_order[cb + i];
+            const int pos = cb + atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i] - 1, 1);
             float4 k[9];
             contact_constants(w, c, dt, k);
 #pragma unroll
             for (int q = 0; q < 9; ++q)
-                w.s_k[(size_t)9 * c + q] = k[q];
+                w.s_k[(size_t)9 * pos + q] = k[q];
+            const int b = w.cand_b[c];
+            w.s_ids[pos] = make_int4(c, w.cand_a[c], type_b_is_floor(w.cand_meta[c] & 7) ? -1 - b : b,
+                                     w.cand_pidx ? w.cand_pidx[c] : 0);
         }
         __threadfence_block();
         __syncthreads();
-        // (5) waves in order
+        // (5) waves in order. A wave's bound and a thread's first slot id of the next wave are
+        // fetched a wave ahead, so a wave waits for one round trip (constants and velocities
+        // together) before its iterations.
         const float cr = w.sc_cr[s], cf = w.sc_cf[s];
         const double c2 = friction_scale(cf);
         const int iters = w.sc_iters[s];
+        int lo = 0, hi = __ldcg(w.s_wcnt + cb);
+        int hin = maxw > 1 ? __ldcg(w.s_wcnt + cb + 1) : hi;
+        int4 id = tid < hi ? __ldcg(w.s_ids + cb + tid) : make_int4(-1, 0, 0, 0);
         for (int wv = 1; wv <= maxw; ++wv)
         {
-            int lo = (wv == 1) ? 0 : __ldcg(w.s_wcnt + cb + wv - 2), hi = __ldcg(w.s_wcnt + cb + wv - 1);
-            for (int i = lo + tid; i < hi; i += blockDim.x)
-            {
-                int c = __ldcg(w.s_perm + cb + i);
-                float4 k[9];
-#pragma unroll
-                for (int q = 0; q < 9; ++q)
-                    k[q] = __ldcg(w.s_k + (size_t)9 * c + q);
-                contact_apply<WARM>(w, c, k, cr, cf, c2, iters);
-            }
+            const int4 idn = (wv < maxw && hi + tid < hin) ? __ldcg(w.s_ids + cb + hi + tid) : make_int4(-1, 0, 0, 0);
+            const int hinn = wv + 1 < maxw ? __ldcg(w.s_wcnt + cb + wv + 1) : hin;
+            if (id.x >= 0)
+                contact_apply<WARM>(w, id, w.s_k + (size_t)9 * (cb + lo + tid), cr, cf, c2, iters);
+            for (int i = lo + tid + blockDim.x; i < hi; i += blockDim.x)
+                contact_apply<WARM>(w, __ldcg(w.s_ids + cb + i), w.s_k + (size_t)9 * (cb + i), cr, cf, c2, iters);
             __syncthreads();
+            lo = hi;
+            hi = hin;
+            hin = hinn;
+            id = idn;
         }
     }
 }

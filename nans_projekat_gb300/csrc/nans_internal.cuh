@@ -123,9 +123,11 @@ struct DevWorld
                                         // EPAs escalated to the warp tier, [7] EPAs escalated to
                                         // the giant tier
     // solver scratch, per candidate slot
-    int *s_order, *s_wave, *s_perm, *s_wcnt; // s_order doubles as the narrowphase's EPA queue
-    float4 *s_k;                        // 9 float4 of per-contact constants; during the
-                                        // narrowphase the GJK simplex of a hit
+    int *s_order, *s_wave, *s_wcnt;     // s_order doubles as the narrowphase's EPA queue
+    int4 *s_ids;                        // per solve slot (wave order): candidate, body A,
+                                        // body B (-1 - B when B is the floor), pair-space index
+    float4 *s_k;                        // per solve slot: 9 float4 of contact constants; during
+                                        // the narrowphase, per candidate: the GJK simplex of a hit
     int *s_last;                        // per body: last wave touching it
     float4 *s_fwd;                      // adjoint tape of the solve (2 float4 per slot) or null
     // warm starting (null when off): per pair of the pair space (index 32 * word + bit) the
