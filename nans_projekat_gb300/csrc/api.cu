@@ -52,7 +52,6 @@ namespace
 {
 constexpr int kSweepThreads = 256;
 constexpr int kTuneSteps = 20;       // timed steps per autotuner candidate
-constexpr size_t kSolveSmemMax = 200 * 1024;
 } // namespace
 
 struct nans_world
@@ -192,7 +191,7 @@ int narrow_grid(nans_world *w)
     return std::min(per * w->sm_count, w->gjk_cap_blocks);
 }
 
-size_t solve_smem(const nans_world *w) { return (size_t)std::max(1, w->max_scene_bodies) * sizeof(int); }
+size_t solve_smem(const nans_world *w) { return nans::solve_smem(w->max_scene_bodies, w->dw.solve_cache); }
 
 
 int alloc_candidates(nans_world *w, int cap)
@@ -399,7 +398,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         sc_order[s] = s;
     std::stable_sort(sc_order.begin(), sc_order.end(),
                      [&](int x, int y) { return sc_nc[x] + sc_ns[x] > sc_nc[y] + sc_ns[y]; });
-    if ((size_t)max_bodies * sizeof(int) > kSolveSmemMax)
+    if (4 * kWaveChunk * sizeof(int) + (size_t)max_bodies * sizeof(int) > kSolveSmemMax)
         return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: a scene has more bodies than the solver's wave table holds");
 
     // cube-cube cull tiles: 32 x 32 blocks of the upper triangle of each scene's cube pairs
@@ -432,6 +431,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d = DevWorld{};
     d.n_scenes = S;
     d.n_dyn = ndyn;
+    d.solve_cache = solve_cache_bodies(max_bodies);
     d.n_all = nall;
     d.pair_total = pair_acc;
     d.n_words = (int)word_acc;
@@ -577,8 +577,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     if ((rc = alloc_candidates(w, std::max(1, cap))))
         return rc;
     // the attribute is per device and per kernel, shared by every world on the device: set it to
-    // the largest wave table any world may use, so that one world never lowers another's limit
-    if ((size_t)max_bodies * sizeof(int) > 48 * 1024)
+    // the largest table any world may use, so that one world never lowers another's limit
+    if (nans::solve_smem(max_bodies, d.solve_cache) > 48 * 1024)
         CK(cudaFuncSetAttribute(solve_kernel(d), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmemMax));
     CK(cudaStreamSynchronize(st));
     w->uploaded = true;

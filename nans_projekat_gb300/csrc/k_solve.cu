@@ -13,6 +13,9 @@
 // not depend on velocities (normal, tangents, lever arms, effective masses, the Baumgarte
 // term) in parallel, (5) per wave: the 'iterations'-step accumulate/clamp loop and the
 // impulse application, in the reference's operation order.
+#include <algorithm>
+
+#include "nans_fbound.cuh"
 #include "nans_kernels.cuh"
 
 namespace nans
@@ -22,7 +25,6 @@ namespace nans
 // so worlds of small scenes use 32-thread blocks (many scenes share an SM) and worlds with a
 // scene above 512 bodies 256-thread blocks (its waves hold more contacts).
 constexpr int kSolveThreadsMax = 256;
-constexpr int kWaveChunk = 512;
 
 __device__ __forceinline__ int block_scan_excl(int v, int *sh, int *total)
 {
@@ -57,10 +59,10 @@ __device__ __forceinline__ int block_scan_excl(int v, int *sh, int *total)
     return pre;
 }
 
-// Velocity-independent part of Constraint (code/nans.cpp:1023-1174).
-__device__ __forceinline__ void contact_constants(const DevWorld &w, int c, float dt, float4 *k)
+// Velocity-independent part of Constraint (code/nans.cpp:1023-1174) for candidate c between
+// bodies a and b.
+__device__ __forceinline__ void contact_constants(const DevWorld &w, int c, int a, int b, float dt, float4 *k)
 {
-    int a = w.cand_a[c], b = w.cand_b[c];
     v3 n = normalize3(xyz(w.c_n[c]));
     v3 pa = xyz(w.pos[a]), pb = xyz(w.pos[b]);
     float4 pra = w.prm[a], prb = w.prm[b];
@@ -98,32 +100,100 @@ __device__ __forceinline__ void contact_constants(const DevWorld &w, int c, floa
 // sqrt(2) * Cf * Sum in double, stored to float (code/nans.cpp:1199, 1214). The product is
 // evaluated left to right, so sqrt(2) * Cf (c2) is computed once per scene.
 __device__ __forceinline__ double friction_scale(float cf) { return 1.4142135623730951 * (double)cf; }
-__device__ __forceinline__ float friction_bound(double c2, float sum) { return (float)(c2 * (double)sum); }
+
+// The accumulate/clamp loop of Constraint (code/nans.cpp:1176-1230): `iters` rounds of the
+// normal impulse (its sum clamped at 0) and the two tangent impulses (their sums clamped to
+// the friction bound, which the reference computes once per tangent from the same operands).
+// On a GB300 a warp's double-precision instruction holds the FP64 pipe for tens of cycles and
+// the bound's multiply and conversions are on the loop's critical path, so the bound comes
+// from the certified single-precision product of nans_fbound.cuh (SP_BOUND); when a product
+// of the loop is not certified the loop reports false and the caller runs it again with the
+// double product. Both give the same values.
+template <bool SP_BOUND>
+__device__ __forceinline__ bool impulse_loop(float jdvn, float jdvt1, float jdvt2, float bias, float jn, float jt1,
+                                             float jt2, double c2, const FBound &fb, int iters, float &sn, float &st1,
+                                             float &st2, float &dn, float &dt1, float &dt2)
+{
+    bool certified = true;
+    for (int it = 0; it < iters; ++it)
+    {
+        float ln = (-jdvn + bias) * jn;
+        float old = sn;
+        sn = sn + ln;
+        if (sn < 0.0f)
+            sn = 0.0f;
+        dn = sn - old;
+        float m;
+        if (SP_BOUND)
+        {
+            bool cert;
+            m = fbound_mul(fb, sn, &cert);
+            certified = certified && cert;
+        }
+        else
+            m = (float)(c2 * (double)sn);
+        float lt1 = (-jdvt1) * jt1;
+        old = st1;
+        st1 = st1 + lt1;
+        if (st1 < -m)
+            st1 = -m;
+        if (st1 > m)
+            st1 = m;
+        dt1 = st1 - old;
+        float lt2 = (-jdvt2) * jt2;
+        old = st2;
+        st2 = st2 + lt2;
+        if (st2 < -m)
+            st2 = -m;
+        if (st2 > m)
+            st2 = m;
+        dt2 = st2 - old;
+    }
+    return certified;
+}
 
 // Velocity-dependent part of Constraint (code/nans.cpp:1149-1156, 1171-1328). With a tape
 // attached (w.s_fwd) it also records, per contact, what the adjoint needs: the relative
 // normal / tangent velocities, the applied impulses and the active set of the closed form
 // (normal impulse max(Ln, 0), tangent impulses clamp(Lt, -mu*Ln, mu*Ln)).
 //
-// id = the slot's (candidate, body A, body B or -1 - B for the floor, pair-space index) and kp
-// its constants: every load of a contact depends only on the slot, so the constants and the
-// four velocity vectors are fetched in one round trip.
-template <bool WARM>
-__device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const float4 *kp, float cr, float cf,
-                                              double c2, int iters)
+// id = the slot's (candidate, body A, body B or -1 - B for the floor, pair-space index), kp its
+// constants, hd their first part (read a wave ahead), vel / omg the velocities (the scene's
+// shared-memory copy or the world's arrays) at ia / ib.
+struct KHead
 {
-    const int c = id.x, a = id.y;
+    float4 n, t1, t2; // (N, Jn), (T1, Jt1), (T2, Jt2)
+    float bias0;
+};
+__device__ __forceinline__ KHead load_head(const float4 *kp)
+{
+    KHead h;
+    h.n = __ldcg(kp);
+    h.t1 = __ldcg(kp + 1);
+    h.t2 = __ldcg(kp + 2);
+    h.bias0 = __ldcg(reinterpret_cast<const float *>(kp + 3) + 3);
+    return h;
+}
+
+template <bool WARM>
+__device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const float4 *kp, const KHead &hd,
+                                              float4 *vel, float4 *omg, int ia, int ib, float cr, float cf,
+                                              double c2, const FBound &fb, int iters)
+{
+    const int c = id.x;
     const bool writes_b = id.z >= 0;
-    const int b = writes_b ? id.z : -1 - id.z;
     float4 k[9];
 #pragma unroll
-    for (int q = 0; q < 9; ++q)
+    for (int q = 3; q < 9; ++q)
         k[q] = __ldcg(kp + q);
+    k[0] = hd.n;
+    k[1] = hd.t1;
+    k[2] = hd.t2;
     v3 n = xyz(k[0]), t1 = xyz(k[1]), t2 = xyz(k[2]);
-    float jn = k[0].w, jt1 = k[1].w, jt2 = k[2].w, bias0 = k[3].w;
+    float jn = k[0].w, jt1 = k[1].w, jt2 = k[2].w, bias0 = hd.bias0;
     float invm1 = k[4].w, invm2 = k[5].w, invi1 = k[6].w, invi2 = k[7].w;
-    v3 V1 = xyz(__ldcg(w.vel + a)), W1 = xyz(__ldcg(w.omg + a));
-    v3 V2 = xyz(__ldcg(w.vel + b)), W2 = xyz(__ldcg(w.omg + b));
+    v3 V1 = xyz(vel[ia]), W1 = xyz(omg[ia]);
+    v3 V2 = xyz(vel[ib]), W2 = xyz(omg[ib]);
     float jdvn = dot3(((V1 + cross3(W1, n)) - V2) - cross3(W2, n), n);
     float jdvt1 = dot3(((V1 + cross3(W1, t1)) - V2) - cross3(W2, t1), t1);
     float jdvt2 = dot3(((V1 + cross3(W1, t2)) - V2) - cross3(W2, t2), t2);
@@ -144,32 +214,17 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const 
             st2 = e.z;
         }
     }
-    for (int it = 0; it < iters; ++it)
     {
-        float ln = (-jdvn + bias) * jn;
-        float old = sn;
-        sn = sn + ln;
-        if (sn < 0.0f)
-            sn = 0.0f;
-        dn = sn - old;
-        float lt1 = (-jdvt1) * jt1;
-        old = st1;
-        st1 = st1 + lt1;
-        float m1 = friction_bound(c2, sn);
-        if (st1 < -m1)
-            st1 = -m1;
-        if (st1 > m1)
-            st1 = m1;
-        dt1 = st1 - old;
-        float lt2 = (-jdvt2) * jt2;
-        old = st2;
-        st2 = st2 + lt2;
-        float m2 = friction_bound(c2, sn);
-        if (st2 < -m2)
-            st2 = -m2;
-        if (st2 > m2)
-            st2 = m2;
-        dt2 = st2 - old;
+        const float sn0 = sn, st10 = st1, st20 = st2;
+        if (!(fb.ok && impulse_loop<true>(jdvn, jdvt1, jdvt2, bias, jn, jt1, jt2, c2, fb, iters, sn, st1, st2, dn, dt1,
+                                          dt2)))
+        {
+            sn = sn0;
+            st1 = st10;
+            st2 = st20;
+            dn = dt1 = dt2 = 0.0f;
+            impulse_loop<false>(jdvn, jdvt1, jdvt2, bias, jn, jt1, jt2, c2, fb, iters, sn, st1, st2, dn, dt1, dt2);
+        }
     }
     if (WARM)
         w.warm[pidx] = make_float4(sn, st1, st2, __int_as_float(step));
@@ -201,8 +256,8 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const 
     W1 = W1 + invi1 * ai1t1;
     V1 = V1 + invm1 * lt2;
     W1 = W1 + invi1 * ai1t2;
-    __stcg(w.vel + a, f4(V1, 0.0f));
-    __stcg(w.omg + a, f4(W1, 0.0f));
+    vel[ia] = f4(V1, 0.0f);
+    omg[ia] = f4(W1, 0.0f);
     if (writes_b)
     {
         V2 = V2 - invm2 * li;
@@ -211,21 +266,26 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const 
         W2 = W2 - invi2 * ai2t1;
         V2 = V2 - invm2 * lt2;
         W2 = W2 - invi2 * ai2t2;
-        __stcg(w.vel + b, f4(V2, 0.0f));
-        __stcg(w.omg + b, f4(W2, 0.0f));
+        vel[ib] = f4(V2, 0.0f);
+        omg[ib] = f4(W2, 0.0f);
     }
 }
 
-// Dynamic shared memory: int last[max_scene_bodies] (wave of the last contact per body).
+// Dynamic shared memory (solve_smem): during phases 1-4 the chunk's hits (candidate, bodies,
+// wave), the wave counts and, per body, the wave of its last contact; during phase 5 the
+// scene's velocities V and W (bodies, then the floor) when the scene has at most w.solve_cache
+// bodies, else the waves work on the world's arrays.
 // pass 0 solves every scene whose contacts are all known after the per-thread EPA tier
 // (largest first, a block per scene); pass 1 the scenes with a candidate in the later EPA
 // tiers (a persistent grid over the late list), so that pass 0 can run while those tiers do.
-template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax, 3) k_solve(DevWorld w, float dt, int pass)
+template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve(DevWorld w, float dt, int pass)
 {
-    extern __shared__ int s_last[];
+    extern __shared__ float4 s_dyn[];
+    int *const s_c = reinterpret_cast<int *>(s_dyn), *const s_ab = s_c + kWaveChunk, *const s_wv = s_ab + kWaveChunk,
+               *const s_cnt = s_wv + kWaveChunk, *const s_last = s_cnt + kWaveChunk;
+    float4 *const s_vel = s_dyn, *const s_omg = s_dyn + w.solve_cache + 1;
     __shared__ int sh[32];
     __shared__ int s_scene, s_maxw;
-    __shared__ int s_la[kWaveChunk], s_lb[kWaveChunk];
     const int tid = threadIdx.x;
     for (int round = 0;; ++round)
     {
@@ -259,22 +319,76 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax, 3) k_so
         const int cb = w.cand_begin[s], ce = w.cand_end[s];
         const int c0 = w.sc_cube0[s];
         const int nb = w.sc_nc[s] + w.sc_ns[s];
-        // (1) ordered compaction of the scene's hits, 8 consecutive candidates per thread
+        // (1) the scene's hits in candidate order, in chunks of `span` <= kWaveChunk candidates
+        // (`per` consecutive candidates a thread), each hit with its bodies (scene-local A and
+        // B + 1, B = -1 for the floor, 16 bits each), loaded with the hit flags; and (2) their
+        // wave labels: thread 0 labels a chunk's hits in order from shared memory, then the wave
+        // sizes are counted in s_cnt (waves <= kWaveChunk).
+        for (int i = tid; i < nb; i += blockDim.x)
+            s_last[i] = 0;
+        for (int i = tid; i < kWaveChunk; i += blockDim.x)
+            s_cnt[i] = 0;
+        if (tid == 0)
+            s_maxw = 0;
+        const int per = kWaveChunk / blockDim.x, span = per * blockDim.x;
         int nh = 0;
-        for (int base = cb; base < ce; base += blockDim.x * 8)
+        for (int base = cb; base < ce; base += span)
         {
-            const int i0 = base + tid * 8;
+            const int i0 = base + tid * per;
             unsigned hv = 0u;
+            int ab[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k)
-                if (i0 + k < ce && w.hit[i0 + k])
-                    hv |= 1u << k;
+            {
+                ab[k] = 0;
+                if (k < per && i0 + k < ce)
+                {
+                    const int c = i0 + k;
+                    if (w.hit[c])
+                        hv |= 1u << k;
+                    const int lb = type_b_is_floor(w.cand_meta[c] & 7) ? -1 : w.cand_b[c] - c0;
+                    ab[k] = (w.cand_a[c] - c0) | ((lb + 1) << 16);
+                }
+            }
             int tot;
-            int pos = cb + nh + block_scan_excl(__popc(hv), sh, &tot);
+            int p = block_scan_excl(__popc(hv), sh, &tot);
 #pragma unroll
             for (int k = 0; k < 8; ++k)
                 if (hv & (1u << k))
-                    w.s_order[pos++] = i0 + k;
+                {
+                    w.s_order[cb + nh + p] = i0 + k;
+                    s_c[p] = i0 + k;
+                    s_ab[p] = ab[k];
+                    ++p;
+                }
+            __syncthreads();
+            if (tid == 0)
+            {
+                int maxw = s_maxw;
+                for (int i = 0; i < tot; ++i)
+                {
+                    const int v = s_ab[i];
+                    const int la = v & 0xffff, lb = (v >> 16) - 1;
+                    int wv = s_last[la];
+                    if (lb >= 0)
+                        wv = max(wv, s_last[lb]);
+                    wv += 1;
+                    s_last[la] = wv;
+                    if (lb >= 0)
+                        s_last[lb] = wv;
+                    s_wv[i] = wv;
+                    maxw = max(maxw, wv);
+                }
+                s_maxw = maxw;
+            }
+            __syncthreads();
+            for (int i = tid; i < tot; i += blockDim.x)
+            {
+                const int wv = s_wv[i];
+                w.s_wave[cb + nh + i] = wv;
+                if (wv <= kWaveChunk)
+                    atomicAdd(s_cnt + wv - 1, 1);
+            }
             nh += tot;
         }
         if (nh == 0)
@@ -284,68 +398,43 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax, 3) k_so
             __syncthreads();
             continue;
         }
-        // (2) wave labels
-        for (int i = tid; i < nb; i += blockDim.x)
-            s_last[i] = 0;
-        if (tid == 0)
-            s_maxw = 0;
         __syncthreads();
-        for (int base = 0; base < nh; base += kWaveChunk)
-        {
-            int cnt = min(kWaveChunk, nh - base);
-            for (int i = tid; i < cnt; i += blockDim.x)
-            {
-                int c = w.s_order[cb + base + i];
-                int type = w.cand_meta[c] & 7;
-                s_la[i] = w.cand_a[c] - c0;
-                s_lb[i] = type_b_is_floor(type) ? -1 : w.cand_b[c] - c0;
-            }
-            __syncthreads();
-            if (tid == 0)
-            {
-                int maxw = s_maxw;
-                for (int i = 0; i < cnt; ++i)
-                {
-                    int la = s_la[i], lb = s_lb[i];
-                    int wv = s_last[la];
-                    if (lb >= 0)
-                        wv = max(wv, s_last[lb]);
-                    wv += 1;
-                    s_last[la] = wv;
-                    if (lb >= 0)
-                        s_last[lb] = wv;
-                    s_la[i] = wv;
-                    maxw = max(maxw, wv);
-                }
-                s_maxw = maxw;
-            }
-            __syncthreads();
-            for (int i = tid; i < cnt; i += blockDim.x)
-                w.s_wave[cb + base + i] = s_la[i];
-            __syncthreads();
-        }
         const int maxw = s_maxw;
         if (tid == 0 && w.s_maxw)
             w.s_maxw[s] = maxw;
-        // (3) counting sort by wave. Wave v (1..maxw) counts at s_wcnt[cb + v - 1]: maxw entries,
-        // and maxw <= nh <= the scene's candidate slots, so scenes never share an entry. After
-        // the placement s_wcnt[cb + v - 1] is the end of wave v (wave 1 starts at 0).
-        for (int i = tid; i < maxw; i += blockDim.x)
-            w.s_wcnt[cb + i] = 0;
-        __syncthreads();
-        for (int i = tid; i < nh; i += blockDim.x)
-            atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i] - 1, 1);
-        __syncthreads();
+        // (3) counting sort by wave. With maxw <= kWaveChunk the wave sizes were counted in
+        // s_cnt; their exclusive prefix goes to s_cnt (the placement's cursors) and their ends
+        // to s_wcnt[cb + v - 1]. Above that, the counts are made in s_wcnt (maxw entries, and
+        // maxw <= nh <= the scene's candidate slots, so scenes never share an entry). Either
+        // way, after the placement s_wcnt[cb + v - 1] is the end of wave v (wave 1 starts at 0).
+        const bool wide = maxw > kWaveChunk;
+        if (wide)
+        {
+            for (int i = tid; i < maxw; i += blockDim.x)
+                w.s_wcnt[cb + i] = 0;
+            __syncthreads();
+            for (int i = tid; i < nh; i += blockDim.x)
+                atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i] - 1, 1);
+            __syncthreads();
+        }
         {
             int carry = 0;
             for (int base = 0; base < maxw; base += blockDim.x)
             {
                 int i = base + tid;
-                int v = (i < maxw) ? w.s_wcnt[cb + i] : 0;
+                int v = (i < maxw) ? (wide ? w.s_wcnt[cb + i] : s_cnt[i]) : 0;
                 int tot;
                 int pre = block_scan_excl(v, sh, &tot);
                 if (i < maxw)
-                    w.s_wcnt[cb + i] = carry + pre;
+                {
+                    if (wide)
+                        w.s_wcnt[cb + i] = carry + pre;
+                    else
+                    {
+                        s_cnt[i] = carry + pre;
+                        w.s_wcnt[cb + i] = carry + pre + v;
+                    }
+                }
                 carry += tot;
                 __syncthreads();
             }
@@ -353,44 +442,104 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax, 3) k_so
         // (4) placement in wave order with the velocity-independent constants: slot cb + pos
         // gets the contact's ids and constants. The slots are the scene's own candidate slots
         // (nh <= ce - cb), whose narrowphase use (the simplex of a hit) ended with the per-thread
-        // EPA; the order of the contacts inside a wave is immaterial (they commute exactly).
+        // EPA; the order of the contacts inside a wave is immaterial (they commute exactly). A
+        // scene of one chunk takes its hits from shared memory, a larger one from s_order.
+        const bool single = ce - cb <= span;
         for (int i = tid; i < nh; i += blockDim.x)
         {
-            const int c = w.s_order[cb + i];
-            const int pos = cb + atomicAdd(w.s_wcnt + cb + w.s_wave[cb + i] - 1, 1);
+            int c, a, b, wv;
+            if (single)
+            {
+                const int v = s_ab[i], lb = (v >> 16) - 1;
+                c = s_c[i];
+                wv = s_wv[i];
+                a = c0 + (v & 0xffff);
+                b = lb >= 0 ? c0 + lb : w.n_dyn + s;
+            }
+            else
+            {
+                c = w.s_order[cb + i];
+                wv = w.s_wave[cb + i];
+                a = w.cand_a[c];
+                b = w.cand_b[c];
+            }
+            const int pos = cb + (wide ? atomicAdd(w.s_wcnt + cb + wv - 1, 1) : atomicAdd(s_cnt + wv - 1, 1));
             float4 k[9];
-            contact_constants(w, c, dt, k);
+            contact_constants(w, c, a, b, dt, k);
 #pragma unroll
             for (int q = 0; q < 9; ++q)
                 w.s_k[(size_t)9 * pos + q] = k[q];
-            const int b = w.cand_b[c];
-            w.s_ids[pos] = make_int4(c, w.cand_a[c], type_b_is_floor(w.cand_meta[c] & 7) ? -1 - b : b,
-                                     w.cand_pidx ? w.cand_pidx[c] : 0);
+            w.s_ids[pos] = make_int4(c, a, b >= w.n_dyn ? -1 - b : b, w.cand_pidx ? w.cand_pidx[c] : 0);
         }
         __threadfence_block();
         __syncthreads();
-        // (5) waves in order. A wave's bound and a thread's first slot id of the next wave are
-        // fetched a wave ahead, so a wave waits for one round trip (constants and velocities
-        // together) before its iterations.
+        // (5) waves in order, on the scene's velocities in shared memory when they fit. A wave's
+        // bound, a thread's first slot id of the next wave and that slot's first constants are
+        // fetched a wave ahead.
         const float cr = w.sc_cr[s], cf = w.sc_cf[s];
         const double c2 = friction_scale(cf);
+        const FBound fb = fbound_split(c2);
         const int iters = w.sc_iters[s];
+        const bool cached = nb <= w.solve_cache;
+        if (cached)
+        {
+            for (int i = tid; i < nb; i += blockDim.x)
+            {
+                s_vel[i] = __ldcg(w.vel + c0 + i);
+                s_omg[i] = __ldcg(w.omg + c0 + i);
+            }
+            if (tid == 0)
+            {
+                s_vel[nb] = __ldcg(w.vel + w.n_dyn + s);
+                s_omg[nb] = __ldcg(w.omg + w.n_dyn + s);
+            }
+            __syncthreads();
+        }
+        float4 *const vel = cached ? s_vel : w.vel;
+        float4 *const omg = cached ? s_omg : w.omg;
+        const int off = cached ? c0 : 0;
         int lo = 0, hi = __ldcg(w.s_wcnt + cb);
         int hin = maxw > 1 ? __ldcg(w.s_wcnt + cb + 1) : hi;
-        int4 id = tid < hi ? __ldcg(w.s_ids + cb + tid) : make_int4(-1, 0, 0, 0);
+        int4 id = make_int4(-1, 0, 0, 0);
+        KHead hd = {};
+        if (tid < hi)
+        {
+            id = __ldcg(w.s_ids + cb + tid);
+            hd = load_head(w.s_k + (size_t)9 * (cb + tid));
+        }
         for (int wv = 1; wv <= maxw; ++wv)
         {
-            const int4 idn = (wv < maxw && hi + tid < hin) ? __ldcg(w.s_ids + cb + hi + tid) : make_int4(-1, 0, 0, 0);
+            int4 idn = make_int4(-1, 0, 0, 0);
+            KHead hdn = {};
+            if (wv < maxw && hi + tid < hin)
+            {
+                idn = __ldcg(w.s_ids + cb + hi + tid);
+                hdn = load_head(w.s_k + (size_t)9 * (cb + hi + tid));
+            }
             const int hinn = wv + 1 < maxw ? __ldcg(w.s_wcnt + cb + wv + 1) : hin;
-            if (id.x >= 0)
-                contact_apply<WARM>(w, id, w.s_k + (size_t)9 * (cb + lo + tid), cr, cf, c2, iters);
-            for (int i = lo + tid + blockDim.x; i < hi; i += blockDim.x)
-                contact_apply<WARM>(w, __ldcg(w.s_ids + cb + i), w.s_k + (size_t)9 * (cb + i), cr, cf, c2, iters);
+            for (int i = lo + tid; i < hi; i += blockDim.x)
+            {
+                const int4 d = i == lo + tid ? id : __ldcg(w.s_ids + cb + i);
+                const float4 *kp = w.s_k + (size_t)9 * (cb + i);
+                const int b = d.z >= 0 ? d.z : -1 - d.z;
+                const int ib = (cached && d.z < 0) ? nb : b - off;
+                contact_apply<WARM>(w, d, kp, i == lo + tid ? hd : load_head(kp), vel, omg, d.y - off, ib, cr, cf, c2,
+                                    fb, iters);
+            }
             __syncthreads();
             lo = hi;
             hi = hin;
             hin = hinn;
             id = idn;
+            hd = hdn;
+        }
+        if (cached)
+        {
+            for (int i = tid; i < nb; i += blockDim.x)
+            {
+                __stcg(w.vel + c0 + i, s_vel[i]);
+                __stcg(w.omg + c0 + i, s_omg[i]);
+            }
         }
     }
 }
@@ -441,6 +590,17 @@ __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int 
 }
 
 int solve_threads(int max_scene_bodies) { return max_scene_bodies > 512 ? kSolveThreadsMax : 32; }
+
+int solve_cache_bodies(int max_scene_bodies)
+{
+    return std::min(max_scene_bodies, (int)(kSolveSmemMax / (2 * sizeof(float4))) - 1);
+}
+
+size_t solve_smem(int max_scene_bodies, int cache)
+{
+    return std::max((size_t)4 * kWaveChunk * sizeof(int) + (size_t)std::max(1, max_scene_bodies) * sizeof(int),
+                    (size_t)(cache + 1) * 2 * sizeof(float4));
+}
 
 // Warm starting keeps its own instantiation so that the default solve keeps its registers.
 const void *solve_kernel(const DevWorld &w)

@@ -129,6 +129,8 @@ struct DevWorld
     float4 *s_k;                        // per solve slot: 9 float4 of contact constants; during
                                         // the narrowphase, per candidate: the GJK simplex of a hit
     int *s_last;                        // per body: last wave touching it
+    int solve_cache;                    // scenes of up to this many bodies solve their waves on
+                                        // a shared-memory copy of their velocities
     float4 *s_fwd;                      // adjoint tape of the solve (2 float4 per slot) or null
     // warm starting (null when off): per pair of the pair space (index 32 * word + bit) the
     // accumulators (sn, st1, st2) of its last solve and that solve's step number

@@ -21,6 +21,8 @@ constexpr int kCullTileThreads = 256;
 constexpr int kRestChunksPerTask = 64; // 32-pair chunks of non-cube-cube pairs per cull task
 constexpr int kSolveLateThreads = 128; // solver blocks of the second pass (late scenes)
 constexpr int kSolveLateBlocksPerSm = 6; // second-pass solver blocks per SM (registers allow six)
+constexpr int kWaveChunk = 256;     // solver: candidates compacted and labelled per chunk
+constexpr size_t kSolveSmemMax = 200 * 1024; // solver: dynamic shared memory per block, at most
 constexpr int kMediumBlocksPerSm = 2;    // warp-tier EPA blocks per SM (shared memory allows three)
 
 // EPA capacities. Vertices: the GJK tetrahedron plus one support per EPA iteration (at most
@@ -98,6 +100,10 @@ int large_kernel_attrs();
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
 int tier_priority(); // the device's greatest stream priority
 int solve_threads(int max_scene_bodies);
+// scenes of up to this many bodies solve on a shared-memory copy of their velocities
+int solve_cache_bodies(int max_scene_bodies);
+// the solver's dynamic shared memory (chunk arrays and per-body waves, or the velocity copy)
+size_t solve_smem(int max_scene_bodies, int cache);
 int render_scene(const DevWorld &w, int scene, const float eye[3], const float target[3], float fov_deg, int width,
                  int height, unsigned long long *fb, unsigned char *rgb, cudaStream_t st);
 const void *solve_kernel(const DevWorld &w);
