@@ -90,9 +90,9 @@ struct DevWorld
     int *work_counter;                  // [0] narrowphase head, [1] solver head, [2] block-EPA
                                         // head, [3] block-EPA queue length, [5] warp-EPA queue
                                         // length, [6] warp-EPA head, [7] long-GJK queue length,
-                                        // [8] giant-EPA queue length, [9] giant-EPA head,
-                                        // [10] per-thread EPA queue length (queue: s_order),
-                                        // [11] per-thread EPA head, [12] late-solve head,
+                                        // [8] giant-EPA queue length, per-thread EPA queue
+                                        // (s_order): [9] its long part (from the back), [10]
+                                        // the others, [11] its head; [12] late-solve head,
                                         // [13] late-scene count
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
