@@ -438,14 +438,14 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.n_tiles = (int)tiles.size();
     auto &L = w->allocs;
     int rc;
-    int *p_cube0, *p_nc, *p_ns, *p_iters, *p_order, *p_bscene;
+    int *p_cube0, *p_nc, *p_ns, *p_iters, *p_order, *p_rank, *p_bscene;
     int *p_word0, *p_wscene;
     int4 *p_tiles;
     int4 *p_rest;
     float *p_cr, *p_cf, *p_local;
     int4 *p_shape;
     if ((rc = dalloc(w, L, &p_cube0, S)) || (rc = dalloc(w, L, &p_nc, S)) || (rc = dalloc(w, L, &p_ns, S)) ||
-        (rc = dalloc(w, L, &p_iters, S)) || (rc = dalloc(w, L, &p_order, S)) || (rc = dalloc(w, L, &p_word0, S + 1)) ||
+        (rc = dalloc(w, L, &p_iters, S)) || (rc = dalloc(w, L, &p_order, S)) || (rc = dalloc(w, L, &p_rank, S)) || (rc = dalloc(w, L, &p_word0, S + 1)) ||
         (rc = dalloc(w, L, &p_cr, S)) || (rc = dalloc(w, L, &p_cf, S)) || (rc = dalloc(w, L, &p_bscene, nall)) ||
         (rc = dalloc(w, L, &w->d_body_rec, nall)) || (rc = dalloc(w, L, &p_shape, nall)) ||
         (rc = dalloc(w, L, &w->d_scl, nall)) || (rc = dalloc(w, L, &w->d_size_moi, nall)) ||
@@ -482,6 +482,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     d.sc_ns = p_ns;
     d.sc_iters = p_iters;
     d.sc_order = p_order;
+    d.sc_rank = p_rank;
     d.sc_word0 = p_word0;
     d.word_scene = p_wscene;
     d.tiles = p_tiles;
@@ -523,6 +524,10 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     CK(cudaMemcpyAsync(p_ns, sc_ns.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_iters, sc_iters.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_order, sc_order.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
+    std::vector<int> sc_rank(S);
+    for (int r = 0; r < S; ++r)
+        sc_rank[sc_order[r]] = r;
+    CK(cudaMemcpyAsync(p_rank, sc_rank.data(), S * sizeof(int), cudaMemcpyHostToDevice, st));
     CK(cudaMemcpyAsync(p_word0, sc_word0.data(), (S + 1) * sizeof(int), cudaMemcpyHostToDevice, st));
     if (!tiles.empty())
         CK(cudaMemcpyAsync(p_tiles, tiles.data(), tiles.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
@@ -579,7 +584,7 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
     // the attribute is per device and per kernel, shared by every world on the device: set it to
     // the largest table any world may use, so that one world never lowers another's limit
     if (nans::solve_smem(max_bodies, d.solve_cache) > 48 * 1024)
-        CK(cudaFuncSetAttribute(solve_kernel(d), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmemMax));
+        CK((cudaError_t)solve_kernel_attrs(d, (int)kSolveSmemMax));
     CK(cudaStreamSynchronize(st));
     w->uploaded = true;
     w->graph_steps_run = 0;

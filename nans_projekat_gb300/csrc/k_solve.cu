@@ -160,6 +160,9 @@ __device__ __forceinline__ bool impulse_loop(float jdvn, float jdvt1, float jdvt
 // id = the slot's (candidate, body A, body B or -1 - B for the floor, pair-space index), kp its
 // constants, hd their first part (read a wave ahead), vel / omg the velocities (the scene's
 // shared-memory copy or the world's arrays) at ia / ib.
+// The iteration loop's operands (N, T1, T2 with their effective masses, and the Baumgarte
+// term), read a wave ahead; the rest of the record is read at the wave's start and needed after
+// the loop. (All nine vectors ahead cost the late pass more in resident blocks than it saved.)
 struct KHead
 {
     float4 n, t1, t2; // (N, Jn), (T1, Jt1), (T2, Jt2)
@@ -176,7 +179,7 @@ __device__ __forceinline__ KHead load_head(const float4 *kp)
 }
 
 template <bool WARM>
-__device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const float4 *kp, const KHead &hd,
+__device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const KHead &hd, const float4 *kp,
                                               float4 *vel, float4 *omg, int ia, int ib, float cr, float cf,
                                               double c2, const FBound &fb, int iters)
 {
@@ -301,10 +304,20 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
                 if (s_scene >= 0 && w.scene_late[s_scene])
                     s_scene = -2;
             }
+            else if (round == 0)
+            {
+                // the late scenes among the gridDim.x largest, one per block, first (the largest
+                // scenes' waves are the pass's critical path); then the others from the late list
+                s_scene = ((int)blockIdx.x < w.n_scenes) ? w.sc_order[blockIdx.x] : -2;
+                if (s_scene >= 0 && !w.scene_late[s_scene])
+                    s_scene = -2;
+            }
             else
             {
                 int q = atomicAdd(w.work_counter + 12, 1);
                 s_scene = (q < min(w.work_counter[13], w.n_scenes)) ? w.late_list[q] : -1;
+                if (s_scene >= 0 && w.sc_rank[s_scene] < (int)gridDim.x)
+                    s_scene = -2;
             }
         }
         __syncthreads();
@@ -520,10 +533,10 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
             for (int i = lo + tid; i < hi; i += blockDim.x)
             {
                 const int4 d = i == lo + tid ? id : __ldcg(w.s_ids + cb + i);
-                const float4 *kp = w.s_k + (size_t)9 * (cb + i);
                 const int b = d.z >= 0 ? d.z : -1 - d.z;
                 const int ib = (cached && d.z < 0) ? nb : b - off;
-                contact_apply<WARM>(w, d, kp, i == lo + tid ? hd : load_head(kp), vel, omg, d.y - off, ib, cr, cf, c2,
+                const float4 *kp = w.s_k + (size_t)9 * (cb + i);
+                contact_apply<WARM>(w, d, i == lo + tid ? hd : load_head(kp), kp, vel, omg, d.y - off, ib, cr, cf, c2,
                                     fb, iters);
             }
             __syncthreads();
@@ -603,9 +616,10 @@ size_t solve_smem(int max_scene_bodies, int cache)
 }
 
 // Warm starting keeps its own instantiation so that the default solve keeps its registers.
-const void *solve_kernel(const DevWorld &w)
+int solve_kernel_attrs(const DevWorld &w, int smem)
 {
-    return w.warm ? (const void *)k_solve<true> : (const void *)k_solve<false>;
+    const void *k = w.warm ? (const void *)k_solve<true> : (const void *)k_solve<false>;
+    return (int)cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
 }
 
 void launch_solve(const DevWorld &w, int grid, int threads, size_t smem, cudaStream_t st, float dt, int pass)

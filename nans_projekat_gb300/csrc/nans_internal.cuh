@@ -56,6 +56,7 @@ struct DevWorld
     const float *sc_cf;
     const int *sc_iters;
     const int *sc_order;      // scenes by decreasing body count (solver queue order)
+    const int *sc_rank;       // per scene: its position in sc_order
     // per body
     float4 *pos, *ang, *vel, *omg, *frc, *trq;
     const float4 *prm, *scl;

@@ -106,7 +106,8 @@ int solve_cache_bodies(int max_scene_bodies);
 size_t solve_smem(int max_scene_bodies, int cache);
 int render_scene(const DevWorld &w, int scene, const float eye[3], const float target[3], float fov_deg, int width,
                  int height, unsigned long long *fb, unsigned char *rgb, cudaStream_t st);
-const void *solve_kernel(const DevWorld &w);
+// the solver kernels' dynamic shared memory limit (cudaFuncAttributeMaxDynamicSharedMemorySize)
+int solve_kernel_attrs(const DevWorld &w, int smem);
 void launch_solve(const DevWorld &w, int grid, int threads, size_t smem, cudaStream_t st, float dt, int pass);
 __global__ void k_pairs_out(DevWorld w, int scene, float *out_rec, int cap, int *count);
 
