@@ -163,6 +163,8 @@ __device__ __forceinline__ bool impulse_loop(float jdvn, float jdvt1, float jdvt
 // The iteration loop's operands (N, T1, T2 with their effective masses, and the Baumgarte
 // term), read a wave ahead; the rest of the record is read at the wave's start and needed after
 // the loop. (All nine vectors ahead cost the late pass more in resident blocks than it saved.)
+// The block wrote these slots itself (placement), so the wave loop reads them with ordinary
+// loads, which the SM's L1 may serve: after the block's barrier they see the block's writes.
 struct KHead
 {
     float4 n, t1, t2; // (N, Jn), (T1, Jt1), (T2, Jt2)
@@ -171,10 +173,10 @@ struct KHead
 __device__ __forceinline__ KHead load_head(const float4 *kp)
 {
     KHead h;
-    h.n = __ldcg(kp);
-    h.t1 = __ldcg(kp + 1);
-    h.t2 = __ldcg(kp + 2);
-    h.bias0 = __ldcg(reinterpret_cast<const float *>(kp + 3) + 3);
+    h.n = kp[0];
+    h.t1 = kp[1];
+    h.t2 = kp[2];
+    h.bias0 = reinterpret_cast<const float *>(kp + 3)[3];
     return h;
 }
 
@@ -188,7 +190,7 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const 
     float4 k[9];
 #pragma unroll
     for (int q = 3; q < 9; ++q)
-        k[q] = __ldcg(kp + q);
+        k[q] = kp[q];
     k[0] = hd.n;
     k[1] = hd.t1;
     k[2] = hd.t2;
@@ -511,13 +513,13 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
         float4 *const vel = cached ? s_vel : w.vel;
         float4 *const omg = cached ? s_omg : w.omg;
         const int off = cached ? c0 : 0;
-        int lo = 0, hi = __ldcg(w.s_wcnt + cb);
-        int hin = maxw > 1 ? __ldcg(w.s_wcnt + cb + 1) : hi;
+        int lo = 0, hi = w.s_wcnt[cb];
+        int hin = maxw > 1 ? w.s_wcnt[cb + 1] : hi;
         int4 id = make_int4(-1, 0, 0, 0);
         KHead hd = {};
         if (tid < hi)
         {
-            id = __ldcg(w.s_ids + cb + tid);
+            id = w.s_ids[cb + tid];
             hd = load_head(w.s_k + (size_t)9 * (cb + tid));
         }
         for (int wv = 1; wv <= maxw; ++wv)
@@ -526,13 +528,13 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
             KHead hdn = {};
             if (wv < maxw && hi + tid < hin)
             {
-                idn = __ldcg(w.s_ids + cb + hi + tid);
+                idn = w.s_ids[cb + hi + tid];
                 hdn = load_head(w.s_k + (size_t)9 * (cb + hi + tid));
             }
-            const int hinn = wv + 1 < maxw ? __ldcg(w.s_wcnt + cb + wv + 1) : hin;
+            const int hinn = wv + 1 < maxw ? w.s_wcnt[cb + wv + 1] : hin;
             for (int i = lo + tid; i < hi; i += blockDim.x)
             {
-                const int4 d = i == lo + tid ? id : __ldcg(w.s_ids + cb + i);
+                const int4 d = i == lo + tid ? id : w.s_ids[cb + i];
                 const int b = d.z >= 0 ? d.z : -1 - d.z;
                 const int ib = (cached && d.z < 0) ? nb : b - off;
                 const float4 *kp = w.s_k + (size_t)9 * (cb + i);
