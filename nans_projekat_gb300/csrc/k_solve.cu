@@ -513,40 +513,61 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
         float4 *const vel = cached ? s_vel : w.vel;
         float4 *const omg = cached ? s_omg : w.omg;
         const int off = cached ? c0 : 0;
+        // A thread's items are its slots lo + tid, lo + tid + nt, ... of each wave in turn; the
+        // record (ids and loop operands) of its next item, in the same wave or the next one, is
+        // read while the current one runs.
+        const int nt = blockDim.x;
         int lo = 0, hi = w.s_wcnt[cb];
         int hin = maxw > 1 ? w.s_wcnt[cb + 1] : hi;
+        int i = tid;       // the thread's current slot
+        bool have = false; // id / hd hold slot i's record
         int4 id = make_int4(-1, 0, 0, 0);
         KHead hd = {};
-        if (tid < hi)
-        {
-            id = w.s_ids[cb + tid];
-            hd = load_head(w.s_k + (size_t)9 * (cb + tid));
-        }
         for (int wv = 1; wv <= maxw; ++wv)
         {
-            int4 idn = make_int4(-1, 0, 0, 0);
-            KHead hdn = {};
-            if (wv < maxw && hi + tid < hin)
-            {
-                idn = w.s_ids[cb + hi + tid];
-                hdn = load_head(w.s_k + (size_t)9 * (cb + hi + tid));
-            }
             const int hinn = wv + 1 < maxw ? w.s_wcnt[cb + wv + 1] : hin;
-            for (int i = lo + tid; i < hi; i += blockDim.x)
+            const bool next_wave = wv < maxw && hi + tid < hin; // the thread has an item in wave wv + 1
+            if (i < hi && !have)
             {
-                const int4 d = i == lo + tid ? id : w.s_ids[cb + i];
-                const int b = d.z >= 0 ? d.z : -1 - d.z;
-                const int ib = (cached && d.z < 0) ? nb : b - off;
-                const float4 *kp = w.s_k + (size_t)9 * (cb + i);
-                contact_apply<WARM>(w, d, i == lo + tid ? hd : load_head(kp), kp, vel, omg, d.y - off, ib, cr, cf, c2,
-                                    fb, iters);
+                id = w.s_ids[cb + i];
+                hd = load_head(w.s_k + (size_t)9 * (cb + i));
+            }
+            else if (i >= hi)
+            {
+                // no item in this wave: read the next wave's first one now
+                have = next_wave;
+                if (next_wave)
+                {
+                    id = w.s_ids[cb + hi + tid];
+                    hd = load_head(w.s_k + (size_t)9 * (cb + hi + tid));
+                }
+            }
+            while (i < hi)
+            {
+                const bool in_wave = i + nt < hi;
+                const int nx = in_wave ? i + nt : hi + tid;
+                const bool nx_ok = in_wave || next_wave;
+                int4 idn = make_int4(-1, 0, 0, 0);
+                KHead hdn = {};
+                if (nx_ok)
+                {
+                    idn = w.s_ids[cb + nx];
+                    hdn = load_head(w.s_k + (size_t)9 * (cb + nx));
+                }
+                const int b = id.z >= 0 ? id.z : -1 - id.z;
+                const int ib = (cached && id.z < 0) ? nb : b - off;
+                contact_apply<WARM>(w, id, hd, w.s_k + (size_t)9 * (cb + i), vel, omg, id.y - off, ib, cr, cf, c2, fb,
+                                    iters);
+                id = idn;
+                hd = hdn;
+                have = nx_ok;
+                i = nx;
             }
             __syncthreads();
             lo = hi;
             hi = hin;
             hin = hinn;
-            id = idn;
-            hd = hdn;
+            i = lo + tid;
         }
         if (cached)
         {
