@@ -276,6 +276,45 @@ __device__ __forceinline__ void contact_apply(const DevWorld &w, int4 id, const 
     }
 }
 
+// Wave labels of a scene's hits b0 .. b0 + n - 1, whose bodies are in s_ab[0 .. n) (A and B + 1,
+// 16 bits each; B = -1 for the floor, which orders nothing): thread 0 gives each, in list
+// order, wave = 1 + max(last wave of A, last wave of B) (s_last per body, from the scene's
+// earlier hits), then the waves go to s_wv and s_wave and their sizes are counted in s_cnt
+// (waves <= kWaveChunk). Called by the whole block after a barrier.
+__device__ __forceinline__ void label_chunk(const DevWorld &w, int cb, int b0, int n, const int *s_ab, int *s_wv,
+                                            int *s_cnt, int *s_last, int *s_maxw)
+{
+    const int tid = threadIdx.x;
+    if (tid == 0)
+    {
+        int maxw = *s_maxw;
+        for (int i = 0; i < n; ++i)
+        {
+            const int v = s_ab[i];
+            const int la = v & 0xffff, lb = (v >> 16) - 1;
+            int wv = s_last[la];
+            if (lb >= 0)
+                wv = max(wv, s_last[lb]);
+            wv += 1;
+            s_last[la] = wv;
+            if (lb >= 0)
+                s_last[lb] = wv;
+            s_wv[i] = wv;
+            maxw = max(maxw, wv);
+        }
+        *s_maxw = maxw;
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += blockDim.x)
+    {
+        const int wv = s_wv[i];
+        w.s_wave[cb + b0 + i] = wv;
+        if (wv <= kWaveChunk)
+            atomicAdd(s_cnt + wv - 1, 1);
+    }
+    __syncthreads();
+}
+
 // Dynamic shared memory (solve_smem): during phases 1-4 the chunk's hits (candidate, bodies,
 // wave), the wave counts and, per body, the wave of its last contact; during phase 5 the
 // scene's velocities V and W (bodies, then the floor) when the scene has at most w.solve_cache
@@ -334,11 +373,12 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
         const int cb = w.cand_begin[s], ce = w.cand_end[s];
         const int c0 = w.sc_cube0[s];
         const int nb = w.sc_nc[s] + w.sc_ns[s];
-        // (1) the scene's hits in candidate order, in chunks of `span` <= kWaveChunk candidates
-        // (`per` consecutive candidates a thread), each hit with its bodies (scene-local A and
-        // B + 1, B = -1 for the floor, 16 bits each), loaded with the hit flags; and (2) their
-        // wave labels: thread 0 labels a chunk's hits in order from shared memory, then the wave
-        // sizes are counted in s_cnt (waves <= kWaveChunk).
+        // (1) the scene's hits in candidate order and (2) their wave labels. A scene whose
+        // candidates fit one chunk (`span` <= kWaveChunk of them, `per` consecutive ones a
+        // thread) loads each candidate's hit flag and bodies (scene-local A and B + 1, B = -1
+        // for the floor, 16 bits each) at once and keeps its hits in shared memory. A larger
+        // scene (whose candidates may be mostly misses) compacts its hits into s_order, eight
+        // candidates a thread, then labels them in chunks of kWaveChunk reloaded from there.
         for (int i = tid; i < nb; i += blockDim.x)
             s_last[i] = 0;
         for (int i = tid; i < kWaveChunk; i += blockDim.x)
@@ -346,10 +386,11 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
         if (tid == 0)
             s_maxw = 0;
         const int per = kWaveChunk / blockDim.x, span = per * blockDim.x;
+        const bool single = ce - cb <= span;
         int nh = 0;
-        for (int base = cb; base < ce; base += span)
+        if (single)
         {
-            const int i0 = base + tid * per;
+            const int i0 = cb + tid * per;
             unsigned hv = 0u;
             int ab[8];
 #pragma unroll
@@ -365,46 +406,52 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
                     ab[k] = (w.cand_a[c] - c0) | ((lb + 1) << 16);
                 }
             }
-            int tot;
-            int p = block_scan_excl(__popc(hv), sh, &tot);
+            int p = block_scan_excl(__popc(hv), sh, &nh);
 #pragma unroll
             for (int k = 0; k < 8; ++k)
                 if (hv & (1u << k))
                 {
-                    w.s_order[cb + nh + p] = i0 + k;
+                    w.s_order[cb + p] = i0 + k;
                     s_c[p] = i0 + k;
                     s_ab[p] = ab[k];
                     ++p;
                 }
             __syncthreads();
-            if (tid == 0)
+            label_chunk(w, cb, 0, nh, s_ab, s_wv, s_cnt, s_last, &s_maxw);
+        }
+        else
+        {
+            for (int base = cb; base < ce; base += blockDim.x * 8)
             {
-                int maxw = s_maxw;
-                for (int i = 0; i < tot; ++i)
+                const int i0 = base + tid * 8;
+                unsigned hv = 0u;
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (i0 + k < ce && w.hit[i0 + k])
+                        hv |= 1u << k;
+                int tot;
+                int pos = cb + nh + block_scan_excl(__popc(hv), sh, &tot);
+#pragma unroll
+                for (int k = 0; k < 8; ++k)
+                    if (hv & (1u << k))
+                        w.s_order[pos++] = i0 + k;
+                nh += tot;
+            }
+            __syncthreads(); // the compaction's last writes to s_order, read back below by other threads
+            for (int b0 = 0; b0 < nh; b0 += kWaveChunk)
+            {
+                const int cnt = min(kWaveChunk, nh - b0);
+                for (int i = tid; i < cnt; i += blockDim.x)
                 {
-                    const int v = s_ab[i];
-                    const int la = v & 0xffff, lb = (v >> 16) - 1;
-                    int wv = s_last[la];
-                    if (lb >= 0)
-                        wv = max(wv, s_last[lb]);
-                    wv += 1;
-                    s_last[la] = wv;
-                    if (lb >= 0)
-                        s_last[lb] = wv;
-                    s_wv[i] = wv;
-                    maxw = max(maxw, wv);
+                    int c = w.s_order[cb + b0 + i];
+                    if (!dev_check(w, c >= cb && c < ce, 15, c, ce))
+                        c = cb;
+                    const int lb = type_b_is_floor(w.cand_meta[c] & 7) ? -1 : w.cand_b[c] - c0;
+                    s_ab[i] = (w.cand_a[c] - c0) | ((lb + 1) << 16);
                 }
-                s_maxw = maxw;
+                __syncthreads();
+                label_chunk(w, cb, b0, cnt, s_ab, s_wv, s_cnt, s_last, &s_maxw);
             }
-            __syncthreads();
-            for (int i = tid; i < tot; i += blockDim.x)
-            {
-                const int wv = s_wv[i];
-                w.s_wave[cb + nh + i] = wv;
-                if (wv <= kWaveChunk)
-                    atomicAdd(s_cnt + wv - 1, 1);
-            }
-            nh += tot;
         }
         if (nh == 0)
         {
@@ -459,7 +506,6 @@ template <bool WARM> __global__ void __launch_bounds__(kSolveThreadsMax) k_solve
         // (nh <= ce - cb), whose narrowphase use (the simplex of a hit) ended with the per-thread
         // EPA; the order of the contacts inside a wave is immaterial (they commute exactly). A
         // scene of one chunk takes its hits from shared memory, a larger one from s_order.
-        const bool single = ce - cb <= span;
         for (int i = tid; i < nh; i += blockDim.x)
         {
             int c, a, b, wv;
