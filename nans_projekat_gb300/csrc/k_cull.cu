@@ -8,7 +8,7 @@
 // skipping pairs whose inflated AABBs are disjoint:
 //   k_cull_mask   one warp per word, one lane per pair: the word's bits, a count per block
 //   k_cull_scan   exclusive scan of the block counts -> candidate offsets, total, capacity
-//   k_cull_write  the pairs of each word at its prefix position, one lane per pair
+//   k_cull_write  the pairs of each word at its prefix position, one lane per word
 // all_pairs != 0 keeps every pair (the reference's exact all-pairs behaviour).
 #include "nans_kernels.cuh" // pair-space decode: nans_pairs.cuh
 
@@ -297,18 +297,16 @@ __global__ void __launch_bounds__(1024) k_cull_scan(DevWorld w, int nblocks)
 }
 
 // The culled pairs at their prefix positions (scene-major order). Thread t of the block owns
-// word blockIdx.x * kCullThreads + t: its scan position, scene data and first pair; each warp
-// then walks its non-empty words, one lane per pair, so that a word's candidates are written
-// by consecutive lanes.
+// word blockIdx.x * kCullThreads + t: its scan position, scene data and first pair, then
+// writes the word's pairs in bit order. (A warp walking its non-empty words one lane per pair
+// spent ten shuffles a word on words of two or three pairs.)
 __global__ void __launch_bounds__(kCullThreads) k_cull_write(DevWorld w)
 {
     __shared__ int sh[32];
-    const int lane = threadIdx.x & 31;
     const int wo = blockIdx.x * kCullThreads + threadIdx.x;
     const unsigned own = (wo < w.n_words) ? w.pair_mask[wo] : 0u;
     int total;
     const int own_pos = w.block_hits[blockIdx.x] + block_exclusive_scan(__popc(own), sh, &total);
-    const int w0 = wo - lane;
     int s = 0, nc = 0, ns = 0, c0 = 0, t0 = 0, i0 = 0, j0 = 0;
     long long p0 = 0;
     if (own)
@@ -321,32 +319,25 @@ __global__ void __launch_bounds__(kCullThreads) k_cull_write(DevWorld w)
         decode_pair(p0, nc, ns, t0, i0, j0);
     }
     const int cap = w.cand_cap;
-    unsigned todo = __ballot_sync(0xffffffffu, own != 0u);
-    while (todo)
+    // each lane writes its own word's pairs, in bit order, at its prefix position (the warp's 32
+    // words' positions are contiguous, so the stores stay within a few lines)
+    unsigned m = own;
+    int pos = own_pos;
+    while (m)
     {
-        const int q = __ffs(todo) - 1;
-        todo &= todo - 1u;
-        const unsigned m = __shfl_sync(0xffffffffu, own, q);
-        const int pos0 = __shfl_sync(0xffffffffu, own_pos, q);
-        const int qs = __shfl_sync(0xffffffffu, s, q);
-        const int qnc = __shfl_sync(0xffffffffu, nc, q), qns = __shfl_sync(0xffffffffu, ns, q);
-        const int qc0 = __shfl_sync(0xffffffffu, c0, q);
-        const int qt = __shfl_sync(0xffffffffu, t0, q), qi = __shfl_sync(0xffffffffu, i0, q);
-        const int qj = __shfl_sync(0xffffffffu, j0, q);
-        const long long qp0 = __shfl_sync(0xffffffffu, p0, q);
-        if (!(m & (1u << lane)))
-            continue;
-        const int pos = pos0 + __popc(m & ((1u << lane) - 1u));
+        const int bit = __ffs(m) - 1;
+        m &= m - 1u;
         if (pos >= cap)
-            continue;
+            break;
         int type, i, j, a, b;
-        pair_after(qp0, qnc, qns, qt, qi, qj, lane, type, i, j);
-        pair_ids(w, qs, qc0, qnc, type, i, j, a, b);
+        pair_after(p0, nc, ns, t0, i0, j0, bit, type, i, j);
+        pair_ids(w, s, c0, nc, type, i, j, a, b);
         w.cand_a[pos] = a;
         w.cand_b[pos] = b;
-        w.cand_meta[pos] = (qs << 3) | type;
+        w.cand_meta[pos] = (s << 3) | type;
         if (w.cand_pidx)
-            w.cand_pidx[pos] = (w0 + q) * 32 + lane;
+            w.cand_pidx[pos] = wo * 32 + bit;
+        ++pos;
     }
 }
 
