@@ -633,10 +633,63 @@ __device__ __forceinline__ bool tiny_edge(TinySmem &S, int t, unsigned long long
 // The closest-face search of the next iteration is folded into the removal pass and the face
 // creation: a running minimum with strict '<' over the kept faces, then the new ones, in list
 // order, is the reference's scan (a NaN first distance keeps face 0, as its scan does).
+// The 8 world vertices of an 8-point shape (a box) in registers: the per-thread EPA's support
+// maps read them once per EPA instead of at every iteration (the polytopes' shared memory leaves
+// the L1 little room). box_support is hull_support's scan: the same order, products and strict
+// comparison from -FLT_MAX, so the same vertex bit for bit.
+struct Verts8
+{
+    float x[8], y[8], z[8];
+};
+__device__ __forceinline__ void load_verts8(const float *verts, int off, Verts8 &r)
+{
+    const float4 *q = reinterpret_cast<const float4 *>(verts + off);
+    float v[24];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+    {
+        const float4 f = __ldg(q + i);
+        v[4 * i] = f.x;
+        v[4 * i + 1] = f.y;
+        v[4 * i + 2] = f.z;
+        v[4 * i + 3] = f.w;
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+    {
+        r.x[k] = v[3 * k];
+        r.y[k] = v[3 * k + 1];
+        r.z[k] = v[3 * k + 2];
+    }
+}
+__device__ __forceinline__ v3 box_support(const Verts8 &r, v3 d)
+{
+    float best = -FLT_MAX;
+    v3 out = mk3(0.0f, 0.0f, 0.0f);
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+    {
+        const v3 p = mk3(r.x[k], r.y[k], r.z[k]);
+        const float dist = dot3(p, d);
+        if (dist > best)
+        {
+            best = dist;
+            out = p;
+        }
+    }
+    return out;
+}
+
 __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, const Shape &B, const float *simp,
                         v3 &out_pa, v3 &out_pb, v3 &out_n, int &iters)
 {
     TinyLocal L;
+    const bool ra = A.npts == 8, rb = B.npts == 8;
+    Verts8 VA, VB;
+    if (ra)
+        load_verts8(w.verts, A.off, VA);
+    if (rb)
+        load_verts8(w.verts, B.off, VB);
     unsigned long long canon = 0ull;
     for (int i = 0; i < 4; ++i)
     {
@@ -677,7 +730,11 @@ __device__ int epa_tiny(const DevWorld &w, TinySmem &S, int t, const Shape &A, c
         if (nf == 0 && !stale)
             return EPA_NONE;
         const v3 n = mk3(S.fnx[ci][t], S.fny[ci][t], S.fnz[ci][t]);
-        const GV ns = minkowski_support(w.verts, A, B, n);
+        GV ns;
+        ns.sa = ra ? box_support(VA, n) : shape_support(w.verts, A, n);
+        const v3 nd = -1.0f * n;
+        ns.sb = rb ? box_support(VB, nd) : shape_support(w.verts, B, nd);
+        ns.p = ns.sa - ns.sb;
         if (dot3(n, ns.p) - cur < 0.001f)
         {
             unsigned fi = S.fidx[ci][t];
