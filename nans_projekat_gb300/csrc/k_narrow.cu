@@ -880,11 +880,36 @@ __device__ __forceinline__ void enqueue_epa(const DevWorld &w, int c, bool hit)
 // GJK of candidate c from call `it` with the simplex (s0..s3, n points). With a budget below
 // 65, a GJK still evolving is queued for the long pass with its state (the simplex in the
 // candidate's s_k slot, n and it in the queue), which resumes it.
+// Minkowski support with 8-point shapes' vertices in registers (Verts8), the others read from
+// memory: minkowski_support's values.
+struct RegSupport
+{
+    const float *verts;
+    const Shape &A, &B;
+    bool ra, rb;
+    const Verts8 &VA, &VB;
+    __device__ __forceinline__ GV operator()(v3 d) const
+    {
+        GV r;
+        r.sa = ra ? box_support(VA, d) : shape_support(verts, A, d);
+        const v3 nd = -1.0f * d;
+        r.sb = rb ? box_support(VB, nd) : shape_support(verts, B, nd);
+        r.p = r.sa - r.sb;
+        return r;
+    }
+};
+
 __device__ __forceinline__ void gjk_one(const DevWorld &w, int c, int budget, GV &s0, GV &s1, GV &s2, GV &s3, int n,
                                         int it)
 {
     const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
-    const int g = gjk_from(w.verts, A, B, s0, s1, s2, s3, n, it, budget);
+    const bool ra = A.npts == 8, rb = B.npts == 8;
+    Verts8 VA, VB;
+    if (ra)
+        load_verts8(w.verts, A.off, VA);
+    if (rb)
+        load_verts8(w.verts, B.off, VB);
+    const int g = gjk_from_with(RegSupport{w.verts, A, B, ra, rb, VA, VB}, A, B, s0, s1, s2, s3, n, it, budget);
     if (g == G_FOUND || g == G_BUDGET)
         store_simplex(w, c, s0, s1, s2, s3);
     if (g == G_BUDGET)
@@ -899,8 +924,9 @@ __device__ __forceinline__ void gjk_one(const DevWorld &w, int c, int budget, GV
 // long GJK runs share warps with each other instead of stalling 31 finished lanes.
 constexpr int kGjkShort = 8;
 constexpr int kGjkThreads = 128;
-// six blocks per SM (at most 85 registers): measured best against 4, 5 and 8
-__global__ void __launch_bounds__(kGjkThreads, 6) k_gjk(DevWorld w)
+// four blocks per SM (at most 128 registers, room for both shapes' vertices): measured best
+// against 5 and 6 (which spill the vertices) on the stack workload
+__global__ void __launch_bounds__(kGjkThreads, 4) k_gjk(DevWorld w)
 {
     const int lane = threadIdx.x & 31;
     const int n = *w.n_cand;
@@ -927,7 +953,7 @@ __global__ void __launch_bounds__(kGjkThreads, 6) k_gjk(DevWorld w)
 
 // The long pass: candidates whose GJK needed more than kGjkShort calls, resumed where the
 // first pass stopped.
-__global__ void __launch_bounds__(kGjkThreads, 6) k_gjk_long(DevWorld w)
+__global__ void __launch_bounds__(kGjkThreads, 4) k_gjk_long(DevWorld w)
 {
     const int n = w.work_counter[7];
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
