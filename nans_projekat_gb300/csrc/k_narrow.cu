@@ -899,10 +899,10 @@ struct RegSupport
     }
 };
 
-__device__ __forceinline__ void gjk_one(const DevWorld &w, int c, int budget, GV &s0, GV &s1, GV &s2, GV &s3, int n,
-                                        int it)
+__device__ __forceinline__ void gjk_one(const DevWorld &w, int c, int ia, int ib, int budget, GV &s0, GV &s1, GV &s2,
+                                        GV &s3, int n, int it)
 {
-    const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
+    const Shape A = load_shape(w, ia), B = load_shape(w, ib);
     const bool ra = A.npts == 8, rb = B.npts == 8;
     Verts8 VA, VB;
     if (ra)
@@ -930,24 +930,43 @@ __global__ void __launch_bounds__(kGjkThreads, 4) k_gjk(DevWorld w)
 {
     const int lane = threadIdx.x & 31;
     const int n = *w.n_cand;
-    for (;;)
+    // the warp claims its next 32 candidates and reads their bodies while it runs these
+    int base = 0;
+    if (lane == 0)
+        base = atomicAdd(w.work_counter, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    int ia = 0, ib = 0;
+    if (base + lane < n)
     {
-        int base = 0;
+        ia = w.cand_a[base + lane];
+        ib = w.cand_b[base + lane];
+    }
+    while (base < n)
+    {
+        int next = 0;
         if (lane == 0)
-            base = atomicAdd(w.work_counter, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n)
-            break;
+            next = atomicAdd(w.work_counter, 32);
+        next = __shfl_sync(0xffffffffu, next, 0);
+        int na = 0, nb = 0;
+        if (next + lane < n)
+        {
+            na = w.cand_a[next + lane];
+            nb = w.cand_b[next + lane];
+        }
         const int c = base + lane;
-        if (c >= n)
-            continue;
-        const int sc = w.cand_meta[c] >> 3;
-        if (c == 0 || (w.cand_meta[c - 1] >> 3) != sc)
-            w.cand_begin[sc] = c;
-        if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
-            w.cand_end[sc] = c + 1;
-        GV s0 = {}, s1 = {}, s2 = {}, s3 = {};
-        gjk_one(w, c, kGjkShort, s0, s1, s2, s3, 0, 0);
+        if (c < n)
+        {
+            const int sc = w.cand_meta[c] >> 3;
+            if (c == 0 || (w.cand_meta[c - 1] >> 3) != sc)
+                w.cand_begin[sc] = c;
+            if (c == n - 1 || (w.cand_meta[c + 1] >> 3) != sc)
+                w.cand_end[sc] = c + 1;
+            GV s0 = {}, s1 = {}, s2 = {}, s3 = {};
+            gjk_one(w, c, ia, ib, kGjkShort, s0, s1, s2, s3, 0, 0);
+        }
+        base = next;
+        ia = na;
+        ib = nb;
     }
 }
 
@@ -974,7 +993,7 @@ __global__ void __launch_bounds__(kGjkThreads, 4) k_gjk_long(DevWorld w)
         s3.p = mk3(k6.w, k7.x, k7.y);
         s3.sa = mk3(k7.z, k7.w, k8.x);
         s3.sb = mk3(k8.y, k8.z, k8.w);
-        gjk_one(w, q.x, 65, s0, s1, s2, s3, q.y & 0xff, q.y >> 8);
+        gjk_one(w, q.x, w.cand_a[q.x], w.cand_b[q.x], 65, s0, s1, s2, s3, q.y & 0xff, q.y >> 8);
     }
 }
 
