@@ -8,11 +8,15 @@
 // number wave = 1 + max(last wave of body A, last wave of body B); contacts of one wave run
 // in parallel and waves run in order, which reproduces the sequential result bit for bit.
 //
-// Per scene: (1) compact the scene's hits in candidate order, (2) label waves (one thread,
-// shared memory), (3) counting-sort contacts by wave, (4) precompute everything that does
-// not depend on velocities (normal, tangents, lever arms, effective masses, the Baumgarte
-// term) in parallel, (5) per wave: the 'iterations'-step accumulate/clamp loop and the
-// impulse application, in the reference's operation order.
+// Per scene: (1) compact the scene's hits in candidate order and (2) label their waves (one
+// thread, shared memory; a scene whose candidates fit one chunk keeps its hits in shared memory
+// throughout), (3) counting-sort the contacts by wave (wave sizes counted in shared memory),
+// (4) place each contact at its slot in wave order with everything that does not depend on
+// velocities (normal, tangents, lever arms, effective masses, the Baumgarte term), (5) per
+// wave, on a shared-memory copy of the scene's velocities: the 'iterations'-step
+// accumulate/clamp loop and the impulse application, in the reference's operation order, with
+// each thread's next contact read ahead. The loop's friction bound is the reference's double
+// product computed in single precision and certified (nans_fbound.cuh).
 #include <algorithm>
 
 #include "nans_fbound.cuh"
