@@ -573,20 +573,25 @@ def differentiable_measurement(lib, device):
             "forward_value": bodies * n / (t_fwd / 1e3), "unit": UNIT}
 
 
+# worlds of the overlapped end-to-end measurement: four quarter batches took 736-745 M body-steps/s
+# against 698 M for two halves, 734 M for three and 692 / 675 M for six / eight
+E2E_WORLDS = 4
+
+
 def e2e_overlapped(lib, batch, device, steps, dist):
-    """End to end through the C ABI with the scenes split over two worlds (two streams), each
-    driven by its own host thread: every step, each world's state arrays go in from pinned host
-    memory (H2D), the world steps once (nans_batch_step with a one-step CUDA graph) and its state
-    arrays come back (D2H), so that one world's copies overlap the other world's step."""
+    """End to end through the C ABI with the scenes split over E2E_WORLDS worlds (one stream
+    each), each driven by its own host thread: every step, each world's state arrays go in from
+    pinned host memory (H2D), the world steps once (nans_batch_step with a one-step CUDA graph)
+    and its state arrays come back (D2H), so that the worlds' copies overlap the others' steps."""
     import torch
 
     def pinned(shape, dtype):
         n = int(np.prod(shape)) * np.dtype(dtype).itemsize
         return torch.empty(max(1, n), dtype=torch.uint8, pin_memory=True).numpy()[:n].view(dtype).reshape(shape)
 
-    half = len(batch) // 2
     worlds, states = [], []
-    for part in (batch[:half], batch[half:]):
+    for idx in np.array_split(np.arange(len(batch)), E2E_WORLDS):
+        part = [batch[i] for i in idx]
         wd = lib.World(device=device)
         wd.upload_batch(part)
         wd.batch_step(DT, 2, 1)
@@ -775,10 +780,10 @@ def run_ours(args):
                                    "traffic": measured_traffic("k_sweep")}},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(e2e_bytes),
                     "d2h_bytes_per_step": int(e2e_bytes),
-                    "path": "two worlds of half the scenes, one host thread each: "
+                    "path": "%d worlds of 1/%d of the scenes each, one host thread each: "
                             "nans_world_set_state_arrays + nans_batch_step(1, one-step graph) + "
-                            "nans_world_get_state_arrays per step, pinned host, copies of one world "
-                            "overlapping the other's step",
+                            "nans_world_get_state_arrays per step, pinned host, each world's copies "
+                            "overlapping the others' steps" % (E2E_WORLDS, E2E_WORLDS),
                     "graph_and_eager_steps_per_world": e2e_paths,
                     "serial": e2e_serial, "records": e2e_records},
             "gpu_launches": int(launches_batched * args.steps),
