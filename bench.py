@@ -30,6 +30,7 @@ sys.path.insert(0, ROOT)
 METRIC = "body-steps/s"
 UNIT = "body-steps/s"
 DT = np.float32(1.0 / 60.0)
+FUSED_MAX_BODIES = 1024           # NANS_WORLD_FUSED_STEP: bodies per scene, at most
 ALG_BYTES_SWEEP_BODY = 68 + 72     # read P,A,V,W,m,I,extents; write P,A,V,W,AABB
 ALG_BYTES_SWEEP_BOX_VERTS = 96     # world vertices written for the narrowphase
 # per body-step with the world vertices kept in registers: read P,A,V,W,F,T (72 B), m, I (8 B),
@@ -306,31 +307,42 @@ def single_scene_line(lib, device, scene, name, gpu_steps, cpu_steps):
     reference itself at -O0 as its build script compiles it and at -O2."""
     import torch
     dt = np.float32(scene.constants.dt)
-    w = lib.World(device=device)
-    w.upload(scene)
-    w.step(dt, 2)
-    w.download()
-    w.step(dt, 1)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(gpu_steps):
-        w.step(dt, 1)
-    t_call = (time.perf_counter() - t0) / gpu_steps
-    t0 = time.perf_counter()
-    for _ in range(gpu_steps):
-        w.step(dt, 1)
+
+    def timed(fused):
+        w = lib.World(device=device, fused_step=fused)
+        w.upload(scene)
+        w.step(dt, 2)
         w.download()
-    t_frame = (time.perf_counter() - t0) / gpu_steps
-    t0 = time.perf_counter()
-    w.step(dt, gpu_steps)
-    t_batch = (time.perf_counter() - t0) / gpu_steps
-    graph_steps, eager_steps = w.path_counts()
-    w.close()
+        w.step(dt, 1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(gpu_steps):
+            w.step(dt, 1)
+        t_call = (time.perf_counter() - t0) / gpu_steps
+        t0 = time.perf_counter()
+        for _ in range(gpu_steps):
+            w.step(dt, 1)
+            w.download()
+        t_frame = (time.perf_counter() - t0) / gpu_steps
+        t0 = time.perf_counter()
+        w.step(dt, gpu_steps)
+        t_batch = (time.perf_counter() - t0) / gpu_steps
+        graph_steps, eager_steps = w.path_counts()
+        w.close()
+        return t_call, t_frame, t_batch, graph_steps, eager_steps
+
+    t_call, t_frame, t_batch, graph_steps, eager_steps = timed(False)
     out = {"workload": name, "bodies": int(scene.n_bodies),
            "gpu_us_per_step": 1e6 * t_call, "gpu_us_per_step_with_download": 1e6 * t_frame,
            "gpu_us_per_step_one_call": 1e6 * t_batch,
            "gpu_path": "nans_step; %d of %d steps replayed from one-step CUDA graphs" % (
                graph_steps, graph_steps + eager_steps)}
+    if scene.n_bodies <= FUSED_MAX_BODIES:
+        t_call, t_frame, t_batch, _, _ = timed(True)
+        out["fused_step"] = {"gpu_us_per_step": 1e6 * t_call, "gpu_us_per_step_with_download": 1e6 * t_frame,
+                             "gpu_us_per_step_one_call": 1e6 * t_batch,
+                             "gpu_path": "nans_step on a NANS_WORLD_FUSED_STEP world (sweep + one detect-and-"
+                                         "solve launch + the large-EPA tiers and late solve, in one-step graphs)"}
     from oracle.portbind import OracleWorld
     o = OracleWorld([scene])
     t0 = time.perf_counter()
@@ -378,12 +390,48 @@ def schedule_ab(lib, batch, device, warm=25, n=10):
     return out
 
 
+def fused_ab(lib, batch, device, warm=5, n=20):
+    """The staged step (12 kernels, each over the whole world) against the fused step
+    (NANS_WORLD_FUSED_STEP: after the sweep, one launch in which a block per scene culls, collides
+    and solves) on identical windows: each world steps the same scenes from the upload (the
+    results are the same bit for bit), then n steps from one CUDA graph are timed with CUDA
+    events. The whole workload and its scenes binned by size."""
+    import torch
+    bins = (("all", 0, 10 ** 9), ("4-16 bodies", 0, 16), ("17-64 bodies", 17, 64), ("65-256 bodies", 65, 10 ** 9))
+    out = {}
+    for name, lo, hi in bins:
+        sub = [sc for sc in batch if lo <= sc.n_bodies <= hi]
+        if not sub:
+            continue
+        row = {"scenes": len(sub), "bodies": int(sum(sc.n_bodies for sc in sub))}
+        for key, fused in (("staged_ms_per_step", False), ("fused_ms_per_step", True)):
+            w = lib.World(device=device, fused_step=fused)
+            w.upload_batch(sub)
+            w.batch_step(DT, warm, 1)
+            w.prepare(DT, n)
+            torch.cuda.synchronize()
+            st = torch.cuda.ExternalStream(w.stream, device=device)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            w.batch_step(DT, n, n)
+            e1.record(st)
+            torch.cuda.synchronize()
+            row[key] = e0.elapsed_time(e1) / n
+            assert w.path_counts()[0] >= n
+            w.close()
+        row["fused_over_staged"] = row["fused_ms_per_step"] / row["staged_ms_per_step"]
+        out[name] = row
+    out["window"] = "steps %d-%d after the upload, one %d-step CUDA graph each" % (warm + 1, warm + n, n)
+    return out
+
+
 def secondary_measurements(lib, batch, device):
     """Plain path vs batched path on the same scenes, and the single large scene."""
     import torch
     from nans_projekat_gb300 import scenes
     out = {}
     out["schedule_ab"] = schedule_ab(lib, batch, device)
+    out["fused_ab"] = fused_ab(lib, batch, device)
     out["c0_plain"] = single_scene_line(lib, device, scenes.stack_scene(0), "stack8: 8 unit cubes + 1 sphere",
                                         600, 600)
     out["c1_plain"] = single_scene_line(lib, device, scenes.random_scene(1),
@@ -407,6 +455,21 @@ def secondary_measurements(lib, batch, device):
     bodies = sum(s.n_bodies for s in sample)
     out["plain_path"] = {"value": bodies * n / t, "unit": UNIT, "scenes": len(sample), "steps": n,
                          "sample": "every 256th scene of the workload, one world per scene, nans_step"}
+    for wd in worlds:
+        wd.close()
+    worlds = []
+    for sc in sample:
+        wd = lib.World(device=device, fused_step=True)
+        wd.upload(sc)
+        wd.step(DT, 2)
+        worlds.append(wd)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for wd in worlds:
+        wd.step(DT, n)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    out["plain_path"]["fused_step_value"] = bodies * n / t
     for wd in worlds:
         wd.close()
     # one large scene: 4,096 boxes + 512 spheres in a 64^3 m box, plain path

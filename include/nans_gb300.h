@@ -130,6 +130,16 @@ typedef struct nans_contact_pair
                                       evaluated across the lanes; default: one thread per pair,
                                       32 pairs per warp (faster on the benchmark workload).
                                       Results are the same. */
+#define NANS_WORLD_FUSED_STEP 64u  /* one launch per step detects and solves each scene (cull,
+                                      GJK, EPA on the per-thread and warp tiers, solve; a block
+                                      per scene) after the sweep, in place of the staged
+                                      kernels; EPAs beyond the warp tier still take the large
+                                      tiers and the late solve pass. Same results. For worlds of
+                                      small scenes, where the staged step's launch chain is the
+                                      cost (the reference's own scene). Scenes of at most 1,024
+                                      bodies; the candidate buffers hold every pair (the
+                                      max_candidates request is raised to that); not with
+                                      NANS_WORLD_WARM_START. */
 #define NANS_WORLD_WARM_START 8u   /* warm starting, the reference's TODO at its pair dedupe
                                       (code/nans.cpp:1386-1389): a pair (type, IndexA,
                                       IndexB) that was in contact at the previous step starts

@@ -116,6 +116,7 @@ struct nans_world
 
     // differentiable rollout: the tape lives in a chunked device arena reused across forwards
     bool tape_on = false;           // the solve records its adjoint data (s_fwd, s_maxw)
+    bool fused = false;             // NANS_WORLD_FUSED_STEP: one detect-and-solve launch per step
     bool tape_valid = false;        // the tape describes the rollout that led to the state
     float tape_dt = 0.0f;
     float4 *fwd_buf = nullptr;      // 2 float4 per candidate slot (in cand_allocs)
@@ -400,6 +401,12 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
                      [&](int x, int y) { return sc_nc[x] + sc_ns[x] > sc_nc[y] + sc_ns[y]; });
     if (4 * kWaveChunk * sizeof(int) + (size_t)max_bodies * sizeof(int) > kSolveSmemMax)
         return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: a scene has more bodies than the solver's wave table holds");
+    w->fused = (w->flags & NANS_WORLD_FUSED_STEP) != 0;
+    if (w->fused && max_bodies > kSceneStepMaxBodies)
+        return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: the fused step takes scenes of at most " +
+                                                  std::to_string(kSceneStepMaxBodies) + " bodies");
+    if (w->fused && word_acc * 32 > INT32_MAX / 16)
+        return fail(NANS_ERR_SCENE_TOO_LARGE, "upload: the fused step needs fewer than 2^27 pairs");
 
     // cube-cube cull tiles: 32 x 32 blocks of the upper triangle of each scene's cube pairs
     std::vector<int4> tiles;
@@ -579,6 +586,8 @@ int upload_impl(nans_world *w, uint32_t nscenes, const uint32_t *snc, const uint
         CK(cudaMemsetAsync(d.warm_step, 0, sizeof(int), st));
     }
     int cap = (int)(w->max_cand_req ? w->max_cand_req : std::min<long long>(16LL * ndyn + 4096, INT32_MAX / 16));
+    if (w->fused) // the fused step places each scene's candidates in its own slots of the pair space
+        cap = std::max(cap, (int)(word_acc * 32));
     if ((rc = alloc_candidates(w, std::max(1, cap))))
         return rc;
     // the attribute is per device and per kernel, shared by every world on the device: set it to
@@ -693,12 +702,41 @@ void after_step(nans_world *w, float dt)
     ++w->steps_run;
 }
 
+// The fused step (NANS_WORLD_FUSED_STEP, not while a tape is recorded): the work counters
+// cleared, the sweep, one launch that culls, collides and solves every scene, then the large EPA
+// tiers and the late solve pass for the scenes with an EPA beyond the warp tier (in most steps
+// both find nothing to do). The candidate buffers hold every pair, so nothing is read back.
+bool use_fused(const nans_world *w) { return w->fused && !w->tape_on; }
+
+cudaError_t enqueue_fused(nans_world *w, float pending_dt, float dt, int flags)
+{
+    cudaStream_t st = w->stream;
+    DevWorld &d = w->dw;
+    cudaError_t e = cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st);
+    if (e != cudaSuccess)
+        return e;
+    k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, pending_dt, dt, flags);
+    launch_scene_step(d, solve_smem(w), dt, (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0, st);
+    e = (cudaError_t)launch_narrow_big(st, d);
+    if (e != cudaSuccess)
+        return e;
+    launch_solve(d, std::min(w->n_scenes, w->solve_late_bpsm * w->sm_count), w->solve_threads1, solve_smem(w), st,
+                 dt, 1);
+    return cudaGetLastError();
+}
+
 // One step, stage by stage. With check_capacity the candidate count is read back after the
 // scan and the candidate buffers grow if needed (the plain path).
 int step_eager(nans_world *w, float dt, bool check_capacity)
 {
     cudaStream_t st = w->stream;
     DevWorld &d = w->dw;
+    if (use_fused(w))
+    {
+        CK(enqueue_fused(w, w->pending_dt, dt, sweep_flags(w)));
+        after_step(w, dt);
+        return NANS_OK;
+    }
     CK(cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st));
     CK(cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st));
@@ -778,6 +816,11 @@ int capture_steps(nans_world *w, float dt, int gsteps, cudaGraphExec_t *exec, fl
     DevWorld &d = w->dw;
     for (int i = 0; i < gsteps; ++i)
     {
+        if (use_fused(w))
+        {
+            enqueue_fused(w, i == 0 ? pdt0 : dt, dt, i == 0 ? flags0 : (SW_INTEGRATE | SW_APPLY_VEL));
+            continue;
+        }
         cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st);
         cudaMemsetAsync(d.cand_begin, 0, w->n_scenes * sizeof(int), st);
         cudaMemsetAsync(d.cand_end, 0, w->n_scenes * sizeof(int), st);
@@ -964,13 +1007,35 @@ int status_code(nans_world *w, unsigned status)
 // copy is restored, the buffers grow (to 1.5 times the largest count seen, at least double) and
 // the steps run again the same way; after three such rounds they run synchronising after every
 // cull. Worlds with warm starting keep that synchronising loop: their contact cache is stamped
-// per step and cannot be rolled back.
+// per step and cannot be rolled back. A world whose candidate buffers hold all of its pairs (small
+// scenes, such as the reference's own) cannot overflow them and skips the copy.
 int plain_steps(nans_world *w, float dt, uint32_t nsteps)
 {
     cudaStream_t st = w->stream;
     DevWorld &d = w->dw;
     const size_t n = (size_t)w->n_all;
-    int rc = ensure_snapshot(w, false);
+    int rc;
+    if ((long long)w->cand_cap >= d.pair_total)
+    {
+        // The candidate buffers hold every pair of every scene, and the cull writes at most one
+        // candidate per pair, so no step can overflow them: no copy aside, one status read.
+        for (uint32_t i = 0; i < nsteps; ++i)
+        {
+            if (!(sweep_flags(w) & (SW_FORCES | SW_MODEL_INPUT)))
+            {
+                if ((rc = step_graph1(w, dt)))
+                    return rc;
+            }
+            else
+            {
+                if ((rc = step_eager(w, dt, false)))
+                    return rc;
+                ++w->eager_steps_run;
+            }
+        }
+        return check_status(w);
+    }
+    rc = ensure_snapshot(w, false);
     if (rc)
         return rc;
     float4 *bufs[6] = {d.pos, d.ang, d.vel, d.omg, d.frc, d.trq};
@@ -1120,6 +1185,11 @@ int nans_world_create(const nans_world_desc *desc, nans_world **out)
         w->device = desc->device;
         w->flags = desc->flags;
         w->max_cand_req = desc->max_candidates;
+    }
+    if ((w->flags & NANS_WORLD_FUSED_STEP) && (w->flags & NANS_WORLD_WARM_START))
+    {
+        delete w;
+        return fail(NANS_ERR_INVALID_ARGUMENT, "create: the fused step does not support warm starting");
     }
     cudaError_t e = cudaSetDevice(w->device);
     if (e == cudaSuccess)
@@ -1768,6 +1838,27 @@ int nans_world_counts(nans_world *w, uint32_t *candidates, uint32_t *contacts)
         return fail(NANS_ERR_NOT_UPLOADED, "counts: no scene uploaded");
     CK(cudaSetDevice(w->device));
     int nc = 0;
+    if (w->fused)
+    {
+        // the fused step's candidates: scene s's in [cand_begin[s], cand_end[s]) of its pair space
+        CK(cudaStreamSynchronize(w->stream));
+        std::vector<int> cb(w->n_scenes), ce(w->n_scenes), h((size_t)std::max(1, w->cand_cap));
+        CK(cudaMemcpy(cb.data(), w->dw.cand_begin, w->n_scenes * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(ce.data(), w->dw.cand_end, w->n_scenes * sizeof(int), cudaMemcpyDeviceToHost));
+        CK(cudaMemcpy(h.data(), w->dw.hit, (size_t)w->cand_cap * sizeof(int), cudaMemcpyDeviceToHost));
+        uint32_t t = 0;
+        for (int sc = 0; sc < w->n_scenes; ++sc)
+        {
+            nc += ce[sc] - cb[sc];
+            for (int i = cb[sc]; i < ce[sc]; ++i)
+                t += h[i] ? 1u : 0u;
+        }
+        if (candidates)
+            *candidates = (uint32_t)nc;
+        if (contacts)
+            *contacts = t;
+        return NANS_OK;
+    }
     CK(cudaMemcpyAsync(&nc, w->dw.n_cand, sizeof(int), cudaMemcpyDeviceToHost, w->stream));
     CK(cudaStreamSynchronize(w->stream));
     if (candidates)
@@ -1937,8 +2028,9 @@ int nans_launches_per_step(nans_world *w, uint32_t *batched, uint32_t *plain)
     if (!w)
         return fail(NANS_ERR_INVALID_ARGUMENT, "launches: null world");
     // sweep, [cull mask, cull write], cull scan, gjk, gjk_long, epa_tiny, epa_medium, block
-    // EPA, giant EPA, solve (two passes)
-    uint32_t k = 10 + (w->cull_blocks > 0 ? 2u : 0u);
+    // EPA, giant EPA, solve (two passes); fused: sweep, scene step, block EPA, giant EPA, late
+    // solve
+    uint32_t k = w->fused ? 5u : 10 + (w->cull_blocks > 0 ? 2u : 0u);
     if (batched)
         *batched = k;
     if (plain)

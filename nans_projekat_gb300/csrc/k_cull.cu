@@ -64,18 +64,6 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int *total)
     return warp_prefix + x - v;
 }
 
-// Global body ids of pair (type, i, j) of scene s whose cubes start at c0 (nc cubes).
-__device__ __forceinline__ void pair_ids(const DevWorld &w, int s, int c0, int nc, int type, int i, int j, int &a,
-                                         int &b)
-{
-    const int s0 = c0 + nc;
-    a = type_a_is_sphere(type) ? s0 + i : c0 + i;
-    if (type_b_is_floor(type))
-        b = w.n_dyn + s;
-    else
-        b = type_b_is_sphere(type) ? s0 + j : c0 + j;
-}
-
 // One warp per mask word, one lane per pair (bit = lane): the pairs' second boxes are read
 // coalesced and the word is a ballot. Lane q first loads the scene data of word w0 + q and
 // decodes its first pair (32 decodes side by side); the warp then walks the 32 words with

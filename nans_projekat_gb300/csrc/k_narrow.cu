@@ -30,6 +30,7 @@
 #include <algorithm>
 
 #include "nans_gjk.cuh"
+#include "nans_solve.cuh"
 
 namespace nans
 {
@@ -1203,6 +1204,220 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(
 }
 
 
+
+// ---------------------------------------------------------------------------------------
+// The fused per-scene step (NANS_WORLD_FUSED_STEP): after the sweep, one launch in which a
+// block of kSceneThreads threads takes a scene at a time (largest first) and runs its whole
+// detect-and-solve sequence, each phase on the block:
+//   (1) the cull: the scene's pairs in the reference's order (code/nans.cpp:1355-1535), kept
+//       when their inflated boxes meet (k_cull_mask's test), compacted in order by block scans
+//       into the scene's own slots of the pair space (from sc_word0 * 32: the candidate
+//       buffers of such a world hold every pair, so no scan across scenes is needed);
+//   (2) GJK, one thread per candidate, every EvolveSimplex call in one run;
+//   (3) EPA per hit on the per-thread polytope (epa_tiny);
+//   (4) the EPAs that outgrew it, one per warp on the warp tier's polytope (epa_run);
+//   (5) the solve (solve_scene), unless an EPA outgrew the warp tier: that pair goes to the
+//       block- and grid-wide tiers as in the staged step and its scene to the late solve pass.
+// The device functions are the staged kernels' own, so the results are the same bit for bit.
+// Every value the phases read from global memory was written by an earlier launch (the sweep)
+// or by the same block before a barrier.
+// ---------------------------------------------------------------------------------------
+constexpr int kSceneThreads = kTinyThreads; // the per-thread polytopes' shared-memory layout
+static_assert(kSceneThreads % 32 == 0 && kSceneThreads <= kWaveChunk, "scene step block size");
+// the block's dynamic shared memory stays within the 48 KB a launch gets without an opt-in
+static_assert(sizeof(TinySmem) <= 48 * 1024 && (kSceneThreads / 32) * sizeof(EpaFast) <= 48 * 1024 &&
+                  (size_t)(kSceneStepMaxBodies + 1) * 2 * sizeof(float4) <= 48 * 1024 &&
+                  4 * kWaveChunk * sizeof(int) + kSceneStepMaxBodies * sizeof(int) <= 48 * 1024,
+              "scene step shared memory");
+
+size_t scene_step_smem(size_t solve_bytes)
+{
+    return std::max(std::max(sizeof(TinySmem), (size_t)(kSceneThreads / 32) * sizeof(EpaFast)), solve_bytes);
+}
+
+__global__ void __launch_bounds__(kSceneThreads) k_scene_step(DevWorld w, float dt, int all_pairs)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    TinySmem &S = *reinterpret_cast<TinySmem *>(smem_raw);
+    EpaFast *const epa = reinterpret_cast<EpaFast *>(smem_raw);
+    float4 *const s_dyn = reinterpret_cast<float4 *>(smem_raw);
+    __shared__ int sh[32];
+    __shared__ int s_q, s_nq, s_nw, s_late, s_maxw;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    for (;;)
+    {
+        if (tid == 0)
+        {
+            s_q = atomicAdd(w.work_counter + 14, 1);
+            s_nq = 0;
+            s_nw = 0;
+            s_late = 0;
+        }
+        __syncthreads();
+        const int q = s_q;
+        if (q >= w.n_scenes)
+            break;
+        const int s = w.sc_order[q];
+        const int c0 = w.sc_cube0[s], nc = w.sc_nc[s], ns = w.sc_ns[s];
+        const long long np = scene_pair_count(nc, ns);
+        const int cb = w.sc_word0[s] * 32;
+        // (1) the cull, eight consecutive pairs a thread between the block scans
+        int nk = 0;
+        for (long long base = 0; base < np; base += 8 * kSceneThreads)
+        {
+            const long long k0 = base + 8ll * tid;
+            int t0 = 0, i0 = 0, j0 = 0;
+            unsigned m = 0u;
+            if (k0 < np)
+            {
+                decode_pair(k0, nc, ns, t0, i0, j0);
+                const int cnt = (int)min(8ll, np - k0);
+                for (int o = 0; o < cnt; ++o)
+                {
+                    int type, i, j, a, b;
+                    pair_after(k0, nc, ns, t0, i0, j0, o, type, i, j);
+                    pair_ids(w, s, c0, nc, type, i, j, a, b);
+                    bool keep = true;
+                    if (!all_pairs)
+                    {
+                        const float4 la = __ldg(w.box_lo + a), ha = __ldg(w.box_hi + a);
+                        const float4 lb = __ldg(w.box_lo + b), hb = __ldg(w.box_hi + b);
+                        keep = la.x <= hb.x && lb.x <= ha.x && la.y <= hb.y && lb.y <= ha.y && la.z <= hb.z &&
+                               lb.z <= ha.z;
+                    }
+                    if (keep)
+                        m |= 1u << o;
+                }
+            }
+            int tot;
+            int pos = cb + nk + block_scan_excl(__popc(m), sh, &tot);
+            while (m)
+            {
+                const int o = __ffs(m) - 1;
+                m &= m - 1u;
+                int type, i, j, a, b;
+                pair_after(k0, nc, ns, t0, i0, j0, o, type, i, j);
+                pair_ids(w, s, c0, nc, type, i, j, a, b);
+                if (dev_check(w, pos < w.cand_cap, 20, pos, w.cand_cap))
+                {
+                    w.cand_a[pos] = a;
+                    w.cand_b[pos] = b;
+                    w.cand_meta[pos] = (s << 3) | type;
+                    w.cand_pidx[pos] = cb + (int)(k0 + o);
+                }
+                ++pos;
+            }
+            nk += tot;
+        }
+        const int ce = min(cb + nk, w.cand_cap);
+        if (tid == 0)
+        {
+            w.cand_begin[s] = cb;
+            w.cand_end[s] = ce;
+            w.scene_late[s] = 0;
+        }
+        __syncthreads(); // the last chunk's candidates, written after its scan
+        // (2) GJK; the hits' simplices go to their s_k slots and the hits to s_order[cb ..)
+        for (int c = cb + tid; c < ce; c += kSceneThreads)
+        {
+            const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
+            const bool ra = A.npts == 8, rb = B.npts == 8;
+            Verts8 VA, VB;
+            if (ra)
+                load_verts8(w.verts, A.off, VA);
+            if (rb)
+                load_verts8(w.verts, B.off, VB);
+            GV s0 = {}, s1 = {}, s2 = {}, s3 = {};
+            int n = 0, it = 0;
+            const int g = gjk_from_with(RegSupport{w.verts, A, B, ra, rb, VA, VB}, A, B, s0, s1, s2, s3, n, it, 65);
+            if (g == G_FOUND)
+            {
+                store_simplex(w, c, s0, s1, s2, s3);
+                w.s_order[cb + atomicAdd(&s_nq, 1)] = c;
+            }
+            else
+                w.hit[c] = 0;
+        }
+        __syncthreads();
+        // (3) per-thread EPA; the EPAs that outgrow its polytope go to s_wave[cb ..)
+        const int nq = s_nq;
+        for (int i = tid; i < nq; i += kSceneThreads)
+        {
+            const int c = w.s_order[cb + i];
+            if (!dev_check(w, c >= cb && c < ce, 21, c, ce))
+                continue;
+            const Shape A = load_shape(w, w.cand_a[c]), B = load_shape(w, w.cand_b[c]);
+            v3 pa, pb, nn;
+            int iters = 0;
+            const int r =
+                epa_tiny(w, S, tid, A, B, reinterpret_cast<const float *>(w.s_k + 9 * (size_t)c), pa, pb, nn, iters);
+            w.epa_hist[w.cand_pidx[c]] = (unsigned char)(r == EPA_OVERFLOW ? 255 : iters);
+            if (r == EPA_OVERFLOW)
+            {
+                w.hit[c] = 0;
+                atomicAdd(w.epa_stats + 6, 1u);
+                w.s_wave[cb + atomicAdd(&s_nw, 1)] = c;
+            }
+            else
+                write_result(w, c, r, pa, pb, nn);
+        }
+        __syncthreads(); // the per-thread polytopes' memory becomes the warps' polytopes
+        // (4) warp tier, from the simplex the GJK phase stored
+        const int nw = s_nw;
+        for (int i = wid; i < nw; i += kSceneThreads / 32)
+        {
+            EpaFast &E = epa[wid];
+            int cc = w.s_wave[cb + i];
+            if (!dev_check(w, cc >= cb && cc < ce, 22, cc, ce))
+                cc = -1;
+            if (cc < 0)
+                continue;
+            const Shape A = load_shape(w, w.cand_a[cc]), B = load_shape(w, w.cand_b[cc]);
+            const float *sq = reinterpret_cast<const float *>(w.s_k + 9 * (size_t)cc);
+            GV g[4];
+            for (int v = 0; v < 4; ++v)
+            {
+                g[v].p = mk3(sq[9 * v], sq[9 * v + 1], sq[9 * v + 2]);
+                g[v].sa = mk3(sq[9 * v + 3], sq[9 * v + 4], sq[9 * v + 5]);
+                g[v].sb = mk3(sq[9 * v + 6], sq[9 * v + 7], sq[9 * v + 8]);
+            }
+            v3 pa, pb, nn;
+            int4 ovf;
+            const int r = epa_run(w, E, A, B, g[0], g[1], g[2], g[3], pa, pb, nn, lane, ovf);
+            __syncwarp();
+            int qo = -1;
+            if (lane == 0)
+            {
+                if (r == EPA_OVERFLOW)
+                {
+                    qo = escalate(w, cc, true);
+                    s_late = 1;
+                }
+                else
+                    write_result(w, cc, r, pa, pb, nn);
+            }
+            qo = __shfl_sync(0xffffffffu, qo, 0);
+            if (qo >= 0 && qo < kHandoverSlots)
+                handover_put(w, E, qo, ovf, lane);
+            __syncwarp();
+        }
+        __syncthreads(); // the warps' polytopes' memory becomes the solver's
+        // (5) the solve, unless a pair of the scene went to the large tiers (the late pass)
+        if (!s_late)
+            solve_scene<false>(w, s, dt, s_dyn, sh, s_maxw);
+        __syncthreads();
+    }
+}
+
+// The fused step's launch: resident blocks on every SM, no more than the world's scenes.
+void launch_scene_step(const DevWorld &w, size_t solve_bytes, float dt, int all_pairs, cudaStream_t st)
+{
+    const size_t smem = scene_step_smem(solve_bytes);
+    int per = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scene_step, kSceneThreads, smem);
+    const int grid = std::max(1, std::min(w.n_scenes, std::max(1, per) * std::max(1, w.sm_count)));
+    k_scene_step<<<grid, kSceneThreads, smem, st>>>(w, dt, all_pairs);
+}
 
 static size_t medium_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }
 

@@ -16,6 +16,18 @@ enum SweepFlags
     SW_FORCES = 8,      // read (then clear) external forces and torques
 };
 
+// Global body ids of pair (type, i, j) of scene s whose cubes start at c0 (nc cubes).
+__device__ __forceinline__ void pair_ids(const DevWorld &w, int s, int c0, int nc, int type, int i, int j, int &a,
+                                         int &b)
+{
+    const int s0 = c0 + nc;
+    a = type_a_is_sphere(type) ? s0 + i : c0 + i;
+    if (type_b_is_floor(type))
+        b = w.n_dyn + s;
+    else
+        b = type_b_is_sphere(type) ? s0 + j : c0 + j;
+}
+
 constexpr int kCullThreads = 256;
 constexpr int kCullTileThreads = 256;
 constexpr int kRestChunksPerTask = 64; // 32-pair chunks of non-cube-cube pairs per cull task
@@ -24,6 +36,7 @@ constexpr int kSolveLateBlocksPerSm = 6; // second-pass solver blocks per SM (re
 constexpr int kWaveChunk = 256;     // solver: candidates compacted and labelled per chunk
 constexpr size_t kSolveSmemMax = 200 * 1024; // solver: dynamic shared memory per block, at most
 constexpr int kMediumBlocksPerSm = 2;    // warp-tier EPA blocks per SM (shared memory allows three)
+constexpr int kSceneStepMaxBodies = 1024; // fused per-scene step: bodies per scene, at most
 
 // EPA capacities. Vertices: the GJK tetrahedron plus one support per EPA iteration (at most
 // 65, code/nans.cpp:804). Faces grow by two per iteration on a convex polytope, but the
@@ -98,6 +111,9 @@ int epa_tiny_grid(int sm_count);   // resident blocks of the per-thread EPA on s
 int narrow_kernel_attrs();         // per-device kernel attributes (cudaError_t), set at world creation
 int large_kernel_attrs();
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
+// the fused per-scene step (cull, GJK, per-thread and warp-tier EPA, solve) over every scene;
+// solve_bytes is the solver's dynamic shared memory (solve_smem)
+void launch_scene_step(const DevWorld &w, size_t solve_bytes, float dt, int all_pairs, cudaStream_t st);
 int tier_priority(); // the device's greatest stream priority
 int solve_threads(int max_scene_bodies);
 // scenes of up to this many bodies solve on a shared-memory copy of their velocities

@@ -34,6 +34,7 @@ WORLD_TEST_GIANT_TIER = 4
 WORLD_WARM_START = 8
 WORLD_TEST_BARRIER_TIMEOUT = 16
 WORLD_GJK_WARP = 32
+WORLD_FUSED_STEP = 64
 
 # Every symbol include/nans_gb300.h declares.
 EXPORTS = (
@@ -142,14 +143,17 @@ class World:
     upload_batch(scenes)   many scenes (the batched form)
     step(dt, n, params)    the plain path: stage-by-stage launches, synchronised
     batch_step(dt, n, g)   the batched path: persistent kernels replayed from a CUDA graph
+    fused_step=True        one detect-and-solve launch per step, a block per scene, in place of
+                           the staged kernels (same results; scenes of at most 1,024 bodies)
     """
 
     def __init__(self, device=0, all_pairs=False, max_candidates=0, strict_epa=False, giant_tier_only=False,
-                 warm_start=False, barrier_timeout_test=False, gjk_warp=False):
+                 warm_start=False, barrier_timeout_test=False, gjk_warp=False, fused_step=False):
         self.lib = load()
         flags = (WORLD_ALL_PAIRS if all_pairs else 0) | (WORLD_STRICT_EPA if strict_epa else 0) | \
             (WORLD_TEST_GIANT_TIER if giant_tier_only else 0) | (WORLD_WARM_START if warm_start else 0) | \
-            (WORLD_TEST_BARRIER_TIMEOUT if barrier_timeout_test else 0) | (WORLD_GJK_WARP if gjk_warp else 0)
+            (WORLD_TEST_BARRIER_TIMEOUT if barrier_timeout_test else 0) | (WORLD_GJK_WARP if gjk_warp else 0) | \
+            (WORLD_FUSED_STEP if fused_step else 0)
         d = WorldDesc(device, flags, max_candidates)
         h = _P()
         _check(self.lib.nans_world_create(ctypes.byref(d), ctypes.byref(h)))
