@@ -82,6 +82,10 @@ def parse():
                         "fitting per-scene masses) with checkpointed rollouts; prints its own JSON line")
     p.add_argument("--checkpoint-every", type=int, default=20,
                    help="steps per rollout segment for --fit-full")
+    p.add_argument("--single", choices=["stack8", "random4608"],
+                   help="only the single-scene drop-in line of that scene (nans_step per step, staged and, "
+                        "where the scene allows it, fused); prints its own JSON line")
+    p.add_argument("--single-steps", type=int, default=600, help="GPU steps of each --single timing")
     return p.parse_args()
 
 
@@ -877,12 +881,31 @@ def run_fit_full(args):
           "fit": r})
 
 
+def run_single(args):
+    """The single-scene drop-in line alone (also a small target for a profiler's launch list)."""
+    import torch
+    from nans_projekat_gb300 import lib, scenes
+    if not torch.cuda.is_available():
+        raise SystemExit("bench.py needs a CUDA device")
+    lib.load()
+    if args.single == "stack8":
+        sc, name, cpu_steps = scenes.stack_scene(0), "stack8: 8 unit cubes + 1 sphere", 600
+    else:
+        sc, name, cpu_steps = scenes.random_scene(1), "random4608: 4,096 boxes + 512 spheres in a 64^3 m box", 3
+    line = single_scene_line(lib, 0, sc, name, args.single_steps, cpu_steps)
+    emit({"metric": "single-scene step latency", "unit": "us/step", "higher_is_better": False,
+          "value": line["gpu_us_per_step"], "n_gpus": 1, "data": "synthetic", "config": {"workload": name},
+          "single": line})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference_arm(args)
     elif args.fit_full:
         run_fit_full(args)
+    elif args.single:
+        run_single(args)
     else:
         run_ours(args)
 

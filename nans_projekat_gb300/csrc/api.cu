@@ -117,6 +117,7 @@ struct nans_world
     // differentiable rollout: the tape lives in a chunked device arena reused across forwards
     bool tape_on = false;           // the solve records its adjoint data (s_fwd, s_maxw)
     bool fused = false;             // NANS_WORLD_FUSED_STEP: one detect-and-solve launch per step
+    bool fused_conditional = true;  // its graphs put the large tiers in a conditional node
     bool tape_valid = false;        // the tape describes the rollout that led to the state
     float tape_dt = 0.0f;
     float4 *fwd_buf = nullptr;      // 2 float4 per candidate slot (in cand_allocs)
@@ -702,27 +703,81 @@ void after_step(nans_world *w, float dt)
     ++w->steps_run;
 }
 
-// The fused step (NANS_WORLD_FUSED_STEP, not while a tape is recorded): the work counters
-// cleared, the sweep, one launch that culls, collides and solves every scene, then the large EPA
-// tiers and the late solve pass for the scenes with an EPA beyond the warp tier (in most steps
-// both find nothing to do). The candidate buffers hold every pair, so nothing is read back.
+// The fused step (NANS_WORLD_FUSED_STEP, not while a tape is recorded): the sweep (which also
+// clears the work counters), one launch that culls, collides and solves every scene, then the
+// large EPA tiers and the late solve pass for the scenes with an EPA beyond the warp tier. The
+// candidate buffers hold every pair, so nothing is read back.
 bool use_fused(const nans_world *w) { return w->fused && !w->tape_on; }
 
-cudaError_t enqueue_fused(nans_world *w, float pending_dt, float dt, int flags)
+// The large EPA tiers and the late solve pass on stream st.
+cudaError_t enqueue_fused_tail(nans_world *w, float dt, cudaStream_t st)
 {
-    cudaStream_t st = w->stream;
     DevWorld &d = w->dw;
-    cudaError_t e = cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st);
-    if (e != cudaSuccess)
-        return e;
-    k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, pending_dt, dt, flags);
-    launch_scene_step(d, solve_smem(w), dt, (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0, st);
-    e = (cudaError_t)launch_narrow_big(st, d);
+    cudaError_t e = (cudaError_t)launch_narrow_big(st, d);
     if (e != cudaSuccess)
         return e;
     launch_solve(d, std::min(w->n_scenes, w->solve_late_bpsm * w->sm_count), w->solve_threads1, solve_smem(w), st,
                  dt, 1);
     return cudaGetLastError();
+}
+
+// Eagerly, or captured with the tail launched unconditionally.
+cudaError_t enqueue_fused(nans_world *w, float pending_dt, float dt, int flags)
+{
+    cudaStream_t st = w->stream;
+    DevWorld &d = w->dw;
+    k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, pending_dt, dt,
+                                                                                       flags | SW_CLEAR_COUNTERS);
+    launch_scene_step(d, solve_smem(w), dt, (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0, st, 0, 0);
+    return enqueue_fused_tail(w, dt, st);
+}
+
+// Under stream capture: the tail in the body of a conditional (IF) node whose handle the fused
+// launch sets only when a scene went late, so that a step with no EPA beyond the warp tier (most
+// steps of small scenes) replays three nodes. The body is captured on the second stream.
+cudaError_t enqueue_fused_conditional(nans_world *w, float pending_dt, float dt, int flags)
+{
+    cudaStream_t st = w->stream;
+    DevWorld &d = w->dw;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t *deps = nullptr;
+    const cudaGraphEdgeData *edges = nullptr;
+    size_t nd = 0;
+    cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edges, &nd);
+    if (e != cudaSuccess)
+        return e;
+    if (cs != cudaStreamCaptureStatusActive)
+        return cudaErrorStreamCaptureInvalidated;
+    cudaGraphConditionalHandle h = 0;
+    if ((e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault)) != cudaSuccess)
+        return e;
+    k_sweep<<<(w->n_all + kSweepThreads - 1) / kSweepThreads, kSweepThreads, 0, st>>>(d, pending_dt, dt,
+                                                                                       flags | SW_CLEAR_COUNTERS);
+    launch_scene_step(d, solve_smem(w), dt, (w->flags & NANS_WORLD_ALL_PAIRS) ? 1 : 0, st, h, 1);
+    if ((e = cudaGetLastError()) != cudaSuccess)
+        return e;
+    if ((e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edges, &nd)) != cudaSuccess)
+        return e;
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeIf;
+    p.conditional.size = 1;
+    cudaGraphNode_t node = nullptr;
+    if ((e = cudaGraphAddNode(&node, g, deps, edges, nd, &p)) != cudaSuccess)
+        return e;
+    if ((e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies)) !=
+        cudaSuccess)
+        return e;
+    cudaGraph_t body = p.conditional.phGraph_out[0];
+    if ((e = cudaStreamBeginCaptureToGraph(w->stream2, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) !=
+        cudaSuccess)
+        return e;
+    const cudaError_t et = enqueue_fused_tail(w, dt, w->stream2);
+    cudaGraph_t out = nullptr;
+    e = cudaStreamEndCapture(w->stream2, &out);
+    return et != cudaSuccess ? et : e;
 }
 
 // One step, stage by stage. With check_capacity the candidate count is read back after the
@@ -814,11 +869,21 @@ int capture_steps(nans_world *w, float dt, int gsteps, cudaGraphExec_t *exec, fl
     cudaGraph_t graph = nullptr;
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     DevWorld &d = w->dw;
+    const bool conditional = use_fused(w) && w->fused_conditional;
+    cudaError_t ec = cudaSuccess;
     for (int i = 0; i < gsteps; ++i)
     {
         if (use_fused(w))
         {
-            enqueue_fused(w, i == 0 ? pdt0 : dt, dt, i == 0 ? flags0 : (SW_INTEGRATE | SW_APPLY_VEL));
+            const float pdt = i == 0 ? pdt0 : dt;
+            const int fl = i == 0 ? flags0 : (SW_INTEGRATE | SW_APPLY_VEL);
+            if (conditional)
+            {
+                if (ec == cudaSuccess)
+                    ec = enqueue_fused_conditional(w, pdt, dt, fl);
+            }
+            else
+                enqueue_fused(w, pdt, dt, fl);
             continue;
         }
         cudaMemsetAsync(d.work_counter, 0, kWorkCounters * sizeof(int), st);
@@ -831,6 +896,24 @@ int capture_steps(nans_world *w, float dt, int gsteps, cudaGraphExec_t *exec, fl
         enqueue_narrow_solve(w, dt, nullptr);
     }
     cudaError_t e = cudaStreamEndCapture(st, &graph);
+    if (e == cudaSuccess && ec == cudaSuccess && conditional)
+    {
+        e = cudaGraphInstantiate(exec, graph, cudaGraphInstantiateFlagUseNodePriority);
+        cudaGraphDestroy(graph);
+        if (e == cudaSuccess)
+            return NANS_OK;
+        *exec = nullptr;
+    }
+    if (conditional)
+    {
+        // the conditional form did not capture or instantiate here: capture the unconditional
+        // tail instead (the same results), and keep to it for this world
+        if (graph && e == cudaSuccess && ec != cudaSuccess)
+            cudaGraphDestroy(graph);
+        cudaGetLastError();
+        w->fused_conditional = false;
+        return capture_steps(w, dt, gsteps, exec, pdt0, flags0);
+    }
     if (e != cudaSuccess)
         return fail(NANS_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
     e = cudaGraphInstantiate(exec, graph, cudaGraphInstantiateFlagUseNodePriority);

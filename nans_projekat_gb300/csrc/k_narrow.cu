@@ -1235,7 +1235,8 @@ size_t scene_step_smem(size_t solve_bytes)
     return std::max(std::max(sizeof(TinySmem), (size_t)(kSceneThreads / 32) * sizeof(EpaFast)), solve_bytes);
 }
 
-__global__ void __launch_bounds__(kSceneThreads) k_scene_step(DevWorld w, float dt, int all_pairs)
+__global__ void __launch_bounds__(kSceneThreads) k_scene_step(DevWorld w, float dt, int all_pairs,
+                                                               cudaGraphConditionalHandle cond, int signal)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     TinySmem &S = *reinterpret_cast<TinySmem *>(smem_raw);
@@ -1407,16 +1408,25 @@ __global__ void __launch_bounds__(kSceneThreads) k_scene_step(DevWorld w, float 
             solve_scene<false>(w, s, dt, s_dyn, sh, s_maxw);
         __syncthreads();
     }
+    // In a graph, the last block to finish opens the conditional node of the large tiers and the
+    // late pass when a scene went late (work counter 13, counted by escalate); one call per launch.
+    if (signal && tid == 0)
+    {
+        __threadfence();
+        if (atomicAdd(w.work_counter + 15, 1) == (int)gridDim.x - 1 && atomicAdd(w.work_counter + 13, 0) > 0)
+            cudaGraphSetConditional(cond, 1u);
+    }
 }
 
 // The fused step's launch: resident blocks on every SM, no more than the world's scenes.
-void launch_scene_step(const DevWorld &w, size_t solve_bytes, float dt, int all_pairs, cudaStream_t st)
+void launch_scene_step(const DevWorld &w, size_t solve_bytes, float dt, int all_pairs, cudaStream_t st,
+                       cudaGraphConditionalHandle cond, int signal)
 {
     const size_t smem = scene_step_smem(solve_bytes);
     int per = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_scene_step, kSceneThreads, smem);
     const int grid = std::max(1, std::min(w.n_scenes, std::max(1, per) * std::max(1, w.sm_count)));
-    k_scene_step<<<grid, kSceneThreads, smem, st>>>(w, dt, all_pairs);
+    k_scene_step<<<grid, kSceneThreads, smem, st>>>(w, dt, all_pairs, cond, signal);
 }
 
 static size_t medium_smem(int warps) { return sizeof(EpaFast) * (size_t)warps; }

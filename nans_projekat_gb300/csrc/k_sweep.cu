@@ -132,6 +132,8 @@ __device__ __forceinline__ void store_box(const DevWorld &w, int b, v3 lo, v3 hi
 __global__ void k_sweep(DevWorld w, float pending_dt, float dt, int flags)
 {
     int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((flags & SW_CLEAR_COUNTERS) && b < kWorkCounters)
+        w.work_counter[b] = 0;
     if (b >= w.n_all)
         return;
     const bool is_floor = b >= w.n_dyn;

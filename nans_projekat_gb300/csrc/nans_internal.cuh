@@ -94,7 +94,8 @@ struct DevWorld
                                         // [8] giant-EPA queue length, per-thread EPA queue
                                         // (s_order): [9] its long part (from the back), [10]
                                         // the others, [11] its head; [12] late-solve head,
-                                        // [13] late-scene count
+                                        // [13] late-scene count; fused step: [14] its scene
+                                        // head, [15] its blocks done
     int med_cap;                        // warp-EPA queue capacity
     int *med_cand;                      // candidates queued for the warp tier
     int2 *long_cand;                    // candidates whose GJK needs the long pass: (c, n | it << 8)

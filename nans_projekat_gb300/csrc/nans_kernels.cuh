@@ -14,6 +14,7 @@ enum SweepFlags
     SW_INTEGRATE = 2,   // RK4 + vertices + AABB
     SW_MODEL_INPUT = 4, // take Model from the uploaded records instead of rebuilding it
     SW_FORCES = 8,      // read (then clear) external forces and torques
+    SW_CLEAR_COUNTERS = 16, // zero the work counters first (the fused step, which has no memset)
 };
 
 // Global body ids of pair (type, i, j) of scene s whose cubes start at c0 (nc cubes).
@@ -113,7 +114,10 @@ int large_kernel_attrs();
 void launch_epa_medium(cudaStream_t st, const DevWorld &w);
 // the fused per-scene step (cull, GJK, per-thread and warp-tier EPA, solve) over every scene;
 // solve_bytes is the solver's dynamic shared memory (solve_smem)
-void launch_scene_step(const DevWorld &w, size_t solve_bytes, float dt, int all_pairs, cudaStream_t st);
+// cond: the handle of the graph's conditional node that runs the large EPA tiers and the late
+// solve pass, set to 1 by the launch when a scene went late (signal = 0 outside a graph)
+void launch_scene_step(const DevWorld &w, size_t solve_bytes, float dt, int all_pairs, cudaStream_t st,
+                       cudaGraphConditionalHandle cond, int signal);
 int tier_priority(); // the device's greatest stream priority
 int solve_threads(int max_scene_bodies);
 // scenes of up to this many bodies solve on a shared-memory copy of their velocities

@@ -101,7 +101,9 @@ void init_scene(nans_sim_state *S)
 
 int upload(nans_sim_state *S)
 {
-    nans_world_desc desc = {0, 0, 0};
+    // a scene of the reference's size (at most 16 cubes and 16 spheres): the fused step, one
+    // detect-and-solve launch per step instead of the staged kernels (the same results)
+    nans_world_desc desc = {0, NANS_WORLD_FUSED_STEP, 0};
     int rc = nans_world_create(&desc, &S->World);
     if (rc)
         return rc;
