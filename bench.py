@@ -744,6 +744,11 @@ def run_ours(args):
     # per-stage device time from a live event-timed pass over the same world
     prof_steps = 10
     stage_ms = w.profile(DT, prof_steps) / prof_steps
+    # the same steps' stage ends with the production overlap of the two streams (the step's
+    # critical path): from the step's start to the end of each stage
+    ends = w.timeline(DT, prof_steps)
+    end_names = ["sweep", "cull", "gjk_and_thread_epa", "warp_epa (stream 2)", "large_epa (stream 2)",
+                 "solve_pass0", "solve_pass1 (step end)"]
     names = ["k_sweep", "k_cull (3 kernels)", "k_narrow_tiny", "k_epa_medium", "k_narrow_big (block + giant tiers)", "k_solve"]
     dom = int(np.argmax(stage_ms))
     peak, peak_kind = measured_peaks()
@@ -840,6 +845,7 @@ def run_ours(args):
                          "peak_source": peak_kind + " hbm_gbs",
                          "bytes_per_launch": dom_bytes,
                          "stage_ms": {n: float(x) for n, x in zip(names, stage_ms)},
+                         "stage_end_ms": {n: float(x) for n, x in zip(end_names, ends)},
                          "sweep": {"basis_164B_per_body": {"achieved": sweep_gbs_164, "frac": sweep_gbs_164 / peak,
                                                            "bytes_per_launch": sweep_bytes_164},
                                    "basis_with_vertices": {"achieved": sweep_gbs, "frac": sweep_gbs / peak,

@@ -1218,6 +1218,8 @@ template <int WARPS> __global__ void __launch_bounds__(WARPS * 32) k_epa_medium(
 //   (4) the EPAs that outgrew it, one per warp on the warp tier's polytope (epa_run);
 //   (5) the solve (solve_scene), unless an EPA outgrew the warp tier: that pair goes to the
 //       block- and grid-wide tiers as in the staged step and its scene to the late solve pass.
+//       In a CUDA graph those launches sit in a conditional node, which the launch's last block
+//       to finish opens only when a scene went late.
 // The device functions are the staged kernels' own, so the results are the same bit for bit.
 // Every value the phases read from global memory was written by an earlier launch (the sweep)
 // or by the same block before a barrier.
