@@ -39,6 +39,21 @@ def test_record_layouts_match_header():
     assert "96 bytes" in text and PAIR_DTYPE.itemsize == 96
 
 
+def test_python_constants_match_header():
+    """The Python mirror's flag and error values are the header's #defines (NANS_WORLD_*,
+    NANS_UPLOAD_*, NANS_ERR_*), every one of them."""
+    from nans_projekat_gb300 import lib
+    text = open(HEADER).read()
+    defines = {m.group(1): int(m.group(2)) for m in re.finditer(r"^#define (NANS_\w+) (\d+)u?\b", text, re.M)}
+    flags = {k: v for k, v in defines.items() if k.startswith(("NANS_WORLD_", "NANS_UPLOAD_"))}
+    assert "NANS_WORLD_FUSED_STEP" in flags and len(flags) >= 8
+    for name, value in flags.items():
+        assert getattr(lib, name[len("NANS_"):]) == value, name
+    errors = {k: v for k, v in defines.items() if k.startswith("NANS_ERR_")}
+    assert errors and {v: k for k, v in errors.items()} == lib.ERRORS
+    assert defines["NANS_OK"] == lib.NANS_OK
+
+
 def test_last_error_is_empty_string_initially():
     from nans_projekat_gb300 import lib
     L = lib.load()
