@@ -140,9 +140,10 @@ typedef struct nans_contact_pair
                                       bodies; the candidate buffers hold every pair (the
                                       max_candidates request is raised to that); not with
                                       NANS_WORLD_WARM_START. nans_profile_steps and
-                                      nans_profile_timeline still time the staged kernels, and
-                                      the launch parameters of nans_batch_autotune /
-                                      nans_world_set_tuning do not apply to it. */
+                                      nans_profile_timeline still time the staged kernels; of
+                                      the launch parameters nans_batch_autotune and
+                                      nans_world_set_tuning set, only the late solve pass's
+                                      apply to it. */
 #define NANS_WORLD_WARM_START 8u   /* warm starting, the reference's TODO at its pair dedupe
                                       (code/nans.cpp:1386-1389): a pair (type, IndexA,
                                       IndexB) that was in contact at the previous step starts
