@@ -1507,12 +1507,6 @@ void launch_epa_medium(cudaStream_t st, const DevWorld &w)
     cudaLaunchKernelEx(&cfg, k_epa_medium<4>, w);
 }
 
-void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w)
-{
-    (void)warps;
-    launch_narrow_tiny(grid, st, w);
-    launch_epa_medium(st, w);
-}
 
 
 

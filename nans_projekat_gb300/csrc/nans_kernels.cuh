@@ -105,7 +105,6 @@ size_t epa_big_bytes();
 size_t epa_block_bytes();
 size_t epa_giant_scratch_bytes();
 int giant_grid(int sm_count);
-void launch_narrow_fast(int warps, int grid, cudaStream_t st, const DevWorld &w);
 int launch_narrow_big(cudaStream_t st, const DevWorld &w); // returns a cudaError_t
 void launch_narrow_tiny(int grid, cudaStream_t st, const DevWorld &w);
 int epa_tiny_grid(int sm_count);   // resident blocks of the per-thread EPA on sm_count SMs
